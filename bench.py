@@ -1,0 +1,319 @@
+#!/usr/bin/env python
+"""Throughput of SPHNJ's particle-step hot path on GB300 (particle-steps/s).
+
+Workload (default): the 4.15M-particle gas-liquid dam break - 1.0 x 2.0 m
+water column in a 4.0 x 3.0 m tank filled with air (rho 1.0), dx = 0.0017,
+h = 1.2 dx, 3 wall layers (~24.7k virtual particles), 10 shifting passes per
+step; synthetic lattice input generated by sphnj_gb300.cases.  One step = one
+fluid step (cell ids, lists, virtual particles, pair pass, update, max speed,
+10 shifting passes).  particle-steps/s = (N_fluid + N_solid) x steps / s.
+
+  python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+
+N > 1 (torchrun): every rank runs its own replica of the scene (the path has
+no data-path collective: scenes are independent), value = all ranks'
+particle-steps / max time over ranks ("scaling": "weak").
+--impl reference times the reference's CPU restatement (the oracle port: the
+reference itself has only a CUDA implementation) on the host cores.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+from pathlib import Path
+
+import numpy as np
+
+ROOT = Path(__file__).resolve().parent
+sys.path.insert(0, str(ROOT))
+
+METRIC = "particle-steps/s (1 GB300): mixed-prec+batched vs plain at stated FP64 error"
+UNIT = "particle-steps/s"
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=50)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--dx", type=float, default=0.0017)
+    ap.add_argument("--cpu-dx", type=float, default=0.0068,
+                    help="dx of the bounded CPU sample (same geometry, 1/16 of the particles)")
+    ap.add_argument("--cpu-steps", type=int, default=3)
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-e2e", action="store_true")
+    return ap.parse_args()
+
+
+def dist_env():
+    return (int(os.environ.get("RANK", 0)), int(os.environ.get("WORLD_SIZE", 1)),
+            int(os.environ.get("LOCAL_RANK", 0)))
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons sampled during the timed region."""
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,clocks_event_reasons.hw_slowdown,"
+         "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+         "clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu_index: int):
+        self.idx = gpu_index
+        self.rows = []
+        self.proc = None
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", f"--id={self.idx}", f"--query-gpu={self.Q}",
+                                          "--format=csv,noheader,nounits", "-lms", "100"],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except (FileNotFoundError, OSError):
+            self.proc = None
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.rows.append([c.strip() for c in line.split(",")])
+
+    def __exit__(self, *a):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+
+    def summary(self):
+        sm = [float(r[1]) for r in self.rows if len(r) >= 9 and r[1].replace(".", "").isdigit()]
+        mx = [float(r[2]) for r in self.rows if len(r) >= 9 and r[2].replace(".", "").isdigit()]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({names[k] for r in self.rows if len(r) >= 9 for k in range(4)
+                          if r[5 + k].lower().startswith("active")})
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(mx) if mx else None,
+                "reasons": reasons, "samples": len(sm)}
+
+
+def make_case(dx):
+    from sphnj_gb300 import cases
+
+    return cases.dam_break_gas(dx=dx)
+
+
+def cpu_rate(case, p, steps, normals=None):
+    """Oracle (reference precision, all host threads) particle-steps/s on a
+    case; setup (upload, wall normals) is outside the timed region."""
+    import oracle
+
+    arr = case.arrays()
+    if normals is not None:
+        arr["virt_normal"] = normals
+    o = oracle.OracleSim(p, oracle.REFERENCE_PRECISION, threads=0)
+    o.upload(arr)
+    o.step(1)  # first step sorts; keep it out of the timing like the GPU warm-up
+    t0 = time.perf_counter()
+    o.step(steps)
+    dt = time.perf_counter() - t0
+    o.close()
+    return (p.fluid_number_total + p.solid_number) * steps / dt, oracle.max_threads(), dt
+
+
+def run_reference(args):
+    rank, world, _ = dist_env()
+    if rank != 0:
+        return 0
+    import oracle
+
+    oracle.build()
+    case = make_case(args.cpu_dx)
+    p = case.params()
+    arr = case.arrays()
+    o = oracle.OracleSim(p, oracle.REFERENCE_PRECISION, threads=0)
+    o.upload(arr)
+    o.step(max(args.warmup, 1))
+    t0 = time.perf_counter()
+    o.step(args.steps)
+    dt = time.perf_counter() - t0
+    n = p.fluid_number_total + p.solid_number
+    v = n * args.steps / dt
+    sample = (f"gas-liquid dam break at dx={args.cpu_dx} ({n} particles, same geometry, h/dx and 10 shifts "
+              f"as the dx={args.dx} workload), {args.steps} full steps")
+    line = {
+        "impl": "reference", "metric": METRIC, "value": v, "unit": UNIT, "n_gpus": args.gpus,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": dt * 1e3 / args.steps,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+        "data": "synthetic (lattice dam break generated in-process)",
+        "config": {"workload": f"gas-liquid dam break, dx={args.dx}", "particles": n},
+        "cpu_baseline": {"value": v, "unit": UNIT, "cores": oracle.max_threads(), "kind": "port",
+                         "sample": sample},
+        "e2e": {"value": v, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+        "note": "the reference has no CPU implementation of the path (CUDA only); this arm is its CPU "
+                "restatement in oracle/, built with OpenMP",
+    }
+    print(json.dumps(line), flush=True)
+    return 0
+
+
+def run_ours(args):
+    import torch
+
+    import sphnj_gb300 as S
+    from sphnj_gb300 import abi, byte_model
+
+    rank, world, local = dist_env()
+    torch.cuda.set_device(local)
+    if world > 1:
+        import torch.distributed as dist
+
+        dist.init_process_group("nccl", device_id=torch.device("cuda", local))
+    S.build()
+    case = make_case(args.dx)
+    p = case.params()
+    arr = case.arrays()
+    nf, ns, nv = p.fluid_number_total, p.solid_number, p.virt_number
+    units = nf + ns
+    stream = torch.cuda.Stream()
+    sim = S.Simulation(p)
+    sim.set_stream(stream.cuda_stream)
+    sim.upload(arr)
+
+    def barrier():
+        if world > 1:
+            torch.distributed.barrier()
+
+    # warm-up
+    sim.step(args.warmup)
+    sim.synchronize()
+
+    # ---- timed region: inputs resident in HBM (state 0.3 GB > 129 MB L2) ---
+    l0 = sim.launches()
+    with ClockSampler(torch.cuda.current_device()) as clk:
+        barrier()
+        torch.cuda.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        sim.step(args.steps)
+        e1.record(stream)
+        torch.cuda.synchronize()
+        barrier()
+    launches = sim.launches() - l0
+    sim.synchronize()
+    ms = e0.elapsed_time(e1)
+    if world > 1:
+        t = torch.tensor([ms], device="cuda")
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        ms = float(t.item())
+    value = units * world * args.steps / (ms / 1e3)
+
+    # ---- per-stage device times (CUDA events on the launching stream) -------
+    sim.profile_enable(True)
+    sim.step(args.steps)
+    prof = sim.profile_read()
+    sim.profile_enable(False)
+    total_ms = sum(v[0] for v in prof.values())
+    dom = max(prof, key=lambda k: prof[k][0])
+    d_ms, d_calls, d_kern = prof[dom]
+    avg_ms = d_ms / max(d_calls, 1)
+    bpl = byte_model.bytes_per_launch(dom, nf, ns, nv)
+    peaks = {}
+    try:
+        peaks = json.loads((ROOT / "MEASURED_PEAKS.json").read_text())
+    except (OSError, ValueError):
+        pass
+    peak = float(peaks.get("hbm_gbs", 6800.0))
+    achieved = bpl / (avg_ms / 1e3) / 1e9
+    roofline = {"bound": "hbm", "kernel": dom, "achieved": achieved, "peak": peak, "unit": "GB/s",
+                "frac": achieved / peak, "traffic": None,
+                "peak_source": "MEASURED_PEAKS.json hbm_gbs (measured)" if peaks else "fallback 6.8 TB/s",
+                "bytes_per_launch": bpl, "avg_launch_ms": avg_ms,
+                "stage_share": {k: round(v[0] / total_ms, 4) for k, v in prof.items() if v[1]}}
+    step_bytes = byte_model.bytes_per_step(nf, ns, nv, p.shift_per_step, p.solid_sub_step)
+
+    # ---- end to end through the C ABI with pinned host buffers ---------------
+    e2e = None
+    if not args.no_e2e:
+        mask = abi.F_FLUID_KINEMATICS | abi.F_FLUID_THERMO
+
+        def pinned(shape, dtype):
+            return torch.empty(shape, dtype=dtype, pin_memory=True).numpy()
+
+        hin = {"fluid_position": pinned((nf, 2), torch.float32), "fluid_velocity": pinned((nf, 2), torch.float32),
+               "fluid_density": pinned((nf,), torch.float32), "fluid_pressure": pinned((nf,), torch.float32)}
+        hout = {k: pinned(v.shape, torch.float32) for k, v in hin.items()}
+        sim.download(mask, into=hin)  # start from the current state
+        h2d = sum(a.nbytes for a in hin.values())
+        d2h = sum(a.nbytes for a in hout.values())
+        ke = max(5, args.steps // 2)
+        barrier()
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        for _ in range(ke):
+            sim.upload_fields(mask, hin)
+            sim.step(1)
+            sim.download(mask, into=hout)
+            hin, hout = hout, hin
+        torch.cuda.synchronize()
+        dt = time.perf_counter() - t0
+        if world > 1:
+            t = torch.tensor([dt], device="cuda")
+            torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+            dt = float(t.item())
+        e2e = {"value": units * world * ke / dt, "unit": UNIT, "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
+               "steps": ke, "api": "sphnj_upload_fields + sphnj_step(1) + sphnj_download per step"}
+
+    normals = sim.download(abi.F_VIRT)["virt_normal"].copy()
+    sim.close()
+
+    cpu = None
+    if rank == 0 and world == 1 and not args.no_cpu_baseline:
+        ccase = make_case(args.cpu_dx)
+        cp = ccase.params()
+        v, cores, dt = cpu_rate(ccase, cp, args.cpu_steps)
+        cpu = {"value": v, "unit": UNIT, "cores": cores, "kind": "port",
+               "sample": f"oracle (reference precision, OpenMP) on the same dam break at dx={args.cpu_dx} "
+                         f"({cp.fluid_number_total} particles, same geometry, h/dx and shifts), {args.cpu_steps} "
+                         f"steps after one sort step, {dt:.1f} s"}
+
+    if world > 1:
+        torch.distributed.destroy_process_group()
+    if rank != 0:
+        return 0
+    line = {
+        "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": ms / args.steps, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f32",
+        "data": "synthetic (lattice gas-liquid dam break generated in-process, reference .dat layout)",
+        "config": {"workload": f"gas-liquid dam break, 1.0x2.0 m water in a 4.0x3.0 m air-filled tank, dx={args.dx}",
+                   "form": "plain (reference precision and cell-list order)", "n_fluid": nf, "n_liquid": p.fluid_number[0],
+                   "n_solid": ns, "n_virt": nv, "cells": p.cell_number_total, "shift_per_step": p.shift_per_step,
+                   "sort_every_step": p.sort_every_step, "dt": p.dt,
+                   "l2": "inputs larger than L2 (fluid state ~0.3 GB > 129 MB)",
+                   "parallelism": f"replicas x{world}" if world > 1 else "single GPU",
+                   "byte_model_bytes_per_step": step_bytes,
+                   "step_hbm_frac_of_byte_model": step_bytes / (ms / args.steps / 1e3) / 1e9 / peak},
+        "roofline": roofline,
+        "cpu_baseline": cpu,
+        "e2e": e2e,
+        "gpu_launches": launches,
+        "clocks": clk.summary(),
+    }
+    print(json.dumps(line), flush=True)
+    return 0
+
+
+def main():
+    args = parse()
+    if args.impl == "reference":
+        return run_reference(args)
+    return run_ours(args)
+
+
+if __name__ == "__main__":
+    sys.exit(main())

@@ -1,0 +1,230 @@
+"""ctypes mirror of include/sphnj.h (the C ABI of libsphnj).
+
+The structures below must match the header field for field; the library's
+``sphnj_abi_sizeof`` is checked against ``ctypes.sizeof`` when the library is
+loaded, and the ini-reading tests check field placement through values.
+"""
+from __future__ import annotations
+
+import ctypes as C
+
+OK = 0
+ERR_ARG, ERR_IO, ERR_CONFIG, ERR_COUNT, ERR_CUDA = 1, 2, 3, 4, 5
+ERR_CELL_OVERFLOW, ERR_OUT_OF_GRID, ERR_NONFINITE, ERR_WATCHDOG = 6, 7, 8, 9
+ERR_UNSUPPORTED, ERR_NO_DEVICE = 10, 11
+
+ERROR_NAMES = {
+    0: "ok", 1: "bad argument", 2: "file I/O", 3: "config", 4: "particle count mismatch", 5: "CUDA",
+    6: "cell overflow", 7: "particle out of cell grid", 8: "non-finite state", 9: "watchdog",
+    10: "unsupported", 11: "no CUDA device",
+}
+
+# enumerations (include/types.h:4-67)
+LIQUID, GAS = 0, 1
+SLIP, NO_SLIP, MOVING = 0, 1, 2
+SPLASH, FREE_SURFACE, VICINITY, INNER = 0, 1, 2, 3
+NO_PARTICLE, HAS_PARTICLE, HAS_NEAR_PARTICLE = 0, 1, 2
+LINEAR_ELASTIC, AUXETIC = 0, 1
+HYPER_ELASTIC, PLASTIC = 0, 1
+UNCONSTRAINED, FIXED = 0, 1
+STRESS_2D, STRAIN_2D = 0, 1
+TRANSIENT, STEADY = 0, 1
+
+CELL_SIZE = 64
+FORM_PLAIN = 0
+
+F_FLUID_KINEMATICS = 1 << 0
+F_FLUID_THERMO = 1 << 1
+F_FLUID_FLAGS = 1 << 2
+F_FLUID_DERIVED = 1 << 3
+F_SOLID_KINEMATICS = 1 << 4
+F_SOLID_MATERIAL = 1 << 5
+F_SOLID_DERIVED = 1 << 6
+F_VIRT = 1 << 7
+F_CELL_IDS = 1 << 8
+F_ALL = 0x1FF
+
+f32, f64, i32 = C.c_float, C.c_double, C.c_int32
+
+
+class Params(C.Structure):
+    _fields_ = [
+        ("gravity", f32 * 2), ("transient_type", i32),
+        ("fluid_number", i32 * 2), ("fluid_number_total", i32),
+        ("sound_speed", f32 * 2), ("reference_density", f32 * 2), ("reference_density_inverse", f32 * 2),
+        ("gamma", f32 * 2), ("viscosity", f32 * 2), ("particle_shift_coef", f32),
+        ("gamma_inv", f32 * 2), ("coefficient_p2rho", f32 * 2), ("coefficient_rho2p", f32 * 2),
+        ("min_pressure", f32), ("min_density", f32 * 2), ("is_fluid_viscid", i32),
+        ("solid_number", i32), ("solid_reference_density", f32), ("youngs_modulus", f32),
+        ("poisson_ratio", f32), ("lambda_", f32), ("nu", f32), ("bulk_modulus", f32),
+        ("artificial_viscosity", f32 * 2), ("solid_sound_speed", f32), ("fixed_speed", f64 * 2),
+        ("constitution_type", i32), ("plastic_type", i32),
+        ("auxetic_density", f32), ("auxetic_modulus", f32), ("auxetic_poisson_ratio", f32),
+        ("yield_strain", f32), ("yield_stress", f32), ("harden_strain", f32), ("harden_coef", f32),
+        ("auxetic_lambda", f32), ("auxetic_nu", f32),
+        ("virt_number", i32),
+        ("cell_xmin", f32 * 2), ("cell_xmax", f32 * 2), ("domain_xmin", f32 * 2), ("domain_xmax", f32 * 2),
+        ("cell_number", i32 * 2), ("interval", f32 * 2), ("interval_inv", f32 * 2), ("cell_number_total", i32),
+        ("dt", f32), ("istart", i32), ("iend", i32), ("solid_sub_step", i32), ("shift_per_step", i32),
+        ("result_interval", i32), ("sort_every_step", i32),
+        ("smoothing_length", f32), ("particle_diameter", f32), ("particle_volume", f32),
+        ("diameter_square", f32), ("thread_num", i32), ("smoothing_length_square", f32),
+        ("smoothing_length_inverse", f32), ("smoothing_length_inverse_square", f32),
+        ("impact_length_hsml_ratio", f32), ("impact_distance_square", f32),
+        ("kernel_coefficient_1", f32), ("kernel_coefficient_2", f32), ("kernel_differential", f32),
+        ("coefficient_3d_to_2d", f32),
+    ]
+
+    def to_dict(self) -> dict:
+        out = {}
+        for name, typ in self._fields_:
+            v = getattr(self, name)
+            out[name] = list(v) if hasattr(v, "__len__") else v
+        return out
+
+    def copy(self) -> "Params":
+        c = Params()
+        C.memmove(C.byref(c), C.byref(self), C.sizeof(Params))
+        return c
+
+
+PF, PD, PI = C.POINTER(C.c_float), C.POINTER(C.c_double), C.POINTER(C.c_int32)
+
+# (field, ctype pointer, numpy dtype, per-particle width, kind)
+STATE_FIELDS = [
+    ("fluid_position", PF, "float32", 2, "fluid"),
+    ("fluid_velocity", PF, "float32", 2, "fluid"),
+    ("fluid_density", PF, "float32", 1, "fluid"),
+    ("fluid_pressure", PF, "float32", 1, "fluid"),
+    ("fluid_phase", PI, "int32", 1, "fluid"),
+    ("fluid_boundary_type", PI, "int32", 1, "fluid"),
+    ("fluid_has_near_particle", PI, "int32", 1, "fluid"),
+    ("fluid_du_dx", PF, "float32", 4, "fluid"),
+    ("fluid_gradient", PF, "float32", 2, "fluid"),
+    ("fluid_du_dt", PF, "float32", 2, "fluid"),
+    ("fluid_color", PF, "float32", 1, "fluid"),
+    ("fluid_drho_dt", PF, "float32", 1, "fluid"),
+    ("fluid_cell_id", PI, "int32", 1, "fluid"),
+    ("solid_position", PD, "float64", 2, "solid"),
+    ("solid_reference_position", PD, "float64", 2, "solid"),
+    ("solid_velocity", PD, "float64", 2, "solid"),
+    ("solid_boundary_type", PI, "int32", 1, "solid"),
+    ("solid_material_type", PI, "int32", 1, "solid"),
+    ("solid_max_strain", PD, "float64", 4, "solid"),
+    ("solid_pressure", PF, "float32", 1, "solid"),
+    ("solid_deformation", PD, "float64", 4, "solid"),
+    ("solid_stress_1st_piola", PD, "float64", 4, "solid"),
+    ("solid_correction", PD, "float64", 4, "solid"),
+    ("solid_du_dt", PD, "float64", 2, "solid"),
+    ("solid_normal", PF, "float32", 2, "solid"),
+    ("solid_couple_dudt", PF, "float32", 2, "solid"),
+    ("solid_cell_id", PI, "int32", 1, "solid"),
+    ("virt_position", PF, "float32", 2, "virt"),
+    ("virt_normal", PF, "float32", 2, "virt"),
+    ("virt_velocity", PF, "float32", 2, "virt"),
+    ("virt_pressure", PF, "float32", 1, "virt"),
+    ("virt_density", PF, "float32", 1, "virt"),
+    ("virt_phase", PI, "int32", 1, "virt"),
+    ("virt_boundary_type", PI, "int32", 1, "virt"),
+    ("virt_cell_id", PI, "int32", 1, "virt"),
+]
+
+# the fields parsed from the .dat files (host_data.cuh:24-115)
+INPUT_FIELDS = {
+    "fluid_position", "fluid_velocity", "fluid_density", "fluid_pressure", "fluid_phase",
+    "solid_position", "solid_velocity", "solid_reference_position", "solid_material_type",
+    "solid_boundary_type", "virt_position", "virt_boundary_type",
+}
+
+
+class HostState(C.Structure):
+    _fields_ = [(name, ptr) for name, ptr, _, _, _ in STATE_FIELDS]
+
+
+def count_of(p: Params, kind: str) -> int:
+    return {"fluid": p.fluid_number_total, "solid": p.solid_number, "virt": p.virt_number}[kind]
+
+
+def state_struct(arrays: dict) -> HostState:
+    """HostState pointing into the given numpy arrays (missing -> NULL).
+    The caller must keep the arrays alive while the struct is used."""
+    import numpy as np
+
+    s = HostState()
+    for name, ptr, dtype, width, kind in STATE_FIELDS:
+        a = arrays.get(name)
+        if a is None:
+            continue
+        if not (isinstance(a, np.ndarray) and a.dtype == np.dtype(dtype) and a.flags.c_contiguous):
+            raise TypeError(f"{name}: need a C-contiguous {dtype} array")
+        setattr(s, name, a.ctypes.data_as(ptr))
+    return s
+
+
+def alloc_state(p: Params, fields=None) -> dict:
+    import numpy as np
+
+    out = {}
+    for name, _, dtype, width, kind in STATE_FIELDS:
+        if fields is not None and name not in fields:
+            continue
+        n = count_of(p, kind)
+        shape = (n,) if width == 1 else (n, width)
+        out[name] = np.zeros(shape, dtype=dtype)
+    return out
+
+
+def set_cells_args(cells):
+    """Arguments of *_debug_set_cells from [(count, list)] * 3 (None = empty);
+    returns (args, keepalive)."""
+    import numpy as np
+
+    args, keep = [], []
+    for item in cells:
+        if item is None:
+            args += [None, None]
+            continue
+        cnt, lst = (np.ascontiguousarray(a, dtype=np.int32) for a in item)
+        keep += [cnt, lst]
+        args += [cnt.ctypes.data_as(PI), lst.ctypes.data_as(PI) if lst.size else None]
+    return args, keep
+
+
+def declare(lib: C.CDLL, prefix: str) -> None:
+    """Set argtypes/restype for the context API under the given prefix
+    ('sphnj' for the GPU library, 'oracle' for the CPU oracle)."""
+    vp = C.c_void_p
+    g = lambda n: getattr(lib, f"{prefix}_{n}")
+    if prefix == "sphnj":
+        g("create").argtypes = [C.POINTER(Params), C.c_int, C.POINTER(vp)]
+        g("set_stream").argtypes = [vp, vp]
+        g("set_stream").restype = C.c_int
+        g("last_error").argtypes = [vp]
+        g("last_error").restype = C.c_char_p
+        g("synchronize").argtypes = [vp]
+        g("synchronize").restype = C.c_int
+    else:
+        g("create").argtypes = [C.POINTER(Params), C.c_int, C.c_int, C.POINTER(vp)]
+        g("error").argtypes = [vp]
+        g("error").restype = C.c_int
+        g("max_threads").argtypes = []
+        g("max_threads").restype = C.c_int
+    g("create").restype = C.c_int
+    g("upload").argtypes = [vp, C.POINTER(HostState)]
+    g("upload").restype = C.c_int
+    g("step").argtypes = [vp, C.c_int]
+    g("step").restype = C.c_int
+    g("download").argtypes = [vp, C.c_uint32, C.POINTER(HostState)]
+    g("download").restype = C.c_int
+    g("debug_cells").argtypes = [vp, C.c_int, PI, PI, PI, PI]
+    g("debug_cells").restype = C.c_int
+    g("debug_max_speed").argtypes = [vp, PF]
+    g("debug_max_speed").restype = C.c_int
+    g("get_step").argtypes = [vp, PI]
+    g("get_step").restype = C.c_int
+    g("debug_set_cells").argtypes = [vp, PI, PI, PI, PI, PI, PI]
+    g("debug_set_cells").restype = C.c_int
+    g("debug_set_step").argtypes = [vp, C.c_int]
+    g("debug_set_step").restype = C.c_int
+    g("destroy").argtypes = [vp]
+    g("destroy").restype = None

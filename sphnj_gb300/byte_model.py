@@ -1,0 +1,58 @@
+"""Algorithmic (compulsory) HBM bytes of each pass of the particle step.
+
+Each pass reads each particle's inputs once and writes its outputs once;
+neighbour re-reads are not counted.  Sizes are those of the plain form
+(fluid FP32, solid FP64, 1-byte enums).  Per particle:
+
+  pass                      bytes   made of
+  bin (cell ids)            12      read position 8, write cell id 4
+  rebuild (fluid lists)     15      cell id 4 + list entry r 4 / w 4 + ranges ~3
+  sort (every 50 steps)     2       amortised
+  fluid_pair                67      read pos 8, vel 8, rho 4, p 4, phase 1, cell 4 = 29 (26 +
+                                    cell id); write drho 4, du_dt 8, near 1, color 4,
+                                    gradient 8, du_dx 16 = 41
+  fluid_update              57      read pos 8, vel 8, du_dt 8, rho 4, drho 4, phase 1 = 33;
+                                    write pos 8, vel 8, rho 4, p 4 = 24
+  shift_gradient            16      read pos 8 (+ cell id), write gradient 8
+  shift_update              63      read gradient 8, color 4, near 1, phase 1, du_dx 16,
+                                    pos 8, vel 8 = 46; write pos 8, vel 8, boundary 1 = 17
+  virt_data (per virtual)   34      read pos 8, normal 8, phase 1, boundary 1, cell 4;
+                                    write vel 8, p 4, rho 4, phase 1 (~34 with the cell id)
+  solid per fluid step      48      bin 20 + coupling 28
+  solid per sub-step        440     deformation ~178 + force ~181 + update ~81
+
+B_step = N_f (153 + 79 S) + N_v 46 + N_s (48 + 440 k)   (S shifts, k sub-steps)
+"""
+from __future__ import annotations
+
+PER_PARTICLE = {
+    "bin": 12,
+    "rebuild": 15,
+    "sort": 2 * 50,  # per sort call (the amortised 2 B/step of the model, over 50 steps)
+    "fluid_pair": 67,
+    "fluid_update": 57,
+    "shift_gradient": 16,
+    "shift_update": 63,
+    "virt_data": 34,
+    "solid_couple": 28,
+    "solid_deformation": 178,
+    "solid_force": 181,
+    "solid_update": 81,
+}
+
+# which particle count a stage's bytes scale with
+STAGE_KIND = {
+    "bin": "all", "rebuild": "fluid", "sort": "fluid", "fluid_pair": "fluid", "fluid_update": "fluid",
+    "shift_gradient": "fluid", "shift_update": "fluid", "virt_data": "virt", "solid_couple": "solid",
+    "solid_deformation": "solid", "solid_force": "solid", "solid_update": "solid", "capacity": "none",
+}
+
+
+def bytes_per_launch(stage: str, nf: int, ns: int, nv: int) -> float:
+    kind = STAGE_KIND.get(stage, "none")
+    n = {"all": nf + ns + nv, "fluid": nf, "solid": ns, "virt": nv, "none": 0}[kind]
+    return float(PER_PARTICLE.get(stage, 0) * n)
+
+
+def bytes_per_step(nf: int, ns: int, nv: int, shifts: int, substeps: int) -> float:
+    return float(nf * (153 + 79 * shifts) + nv * 46 + ns * (48 + 440 * substeps))

@@ -1,0 +1,742 @@
+// C-ABI context of libsphnj: device arena, upload/download, and the step
+// sequencer that issues the particle-step stages on one CUDA stream.
+//
+// Stage order per fluid step (DeviceCalculation::calculation,
+// calculation.cu:28-43; outputs are the host driver's business):
+//   1 cell ids                      particleCellUpdate    pair.cu:47-64
+//   2 sort every sort_every_step    sortParticle          sort.cu:139-151
+//     otherwise incremental lists   fillCell              pair.cu:170-181
+//   3 solid coupling                coupleCalculation     solid.cu:494-507
+//   4 virtual particles             virtUpdate            virt.cu:151-161
+//   5 fluid pair pass + update      fluidCalculation      fluid.cu:289-302
+//   6 k solid sub-steps             solidCalculation      solid.cu:473-492
+//   7 S shifting passes             fluidCorrection       fluid.cu:442-459
+// Nothing in a step reads device data on the host: the reference's per-step
+// device-to-host copy of all fluid velocities (getMaxSpeed) is a device
+// reduction here, and every launch is asynchronous on the context stream.
+#include "kernels.h"
+
+#include <algorithm>
+#include <cstdio>
+#include <cstring>
+#include <string>
+#include <vector>
+
+using namespace sphnj;
+
+namespace {
+
+inline size_t align256(size_t x) { return (x + 255) & ~size_t(255); }
+
+// Two-pass arena carving: first pass sizes, second pass assigns.
+struct Carver {
+    char *base;
+    size_t off = 0;
+    template <class T> T *take(size_t n) {
+        T *r = base ? reinterpret_cast<T *>(base + off) : nullptr;
+        off += align256((n ? n : 1) * sizeof(T));
+        return r;
+    }
+};
+
+__global__ void k_u8_from_i32(uint8_t *dst, const int32_t *src, int n) {
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n) dst[i] = (uint8_t)src[i];
+}
+__global__ void k_i32_from_u8(int32_t *dst, const uint8_t *src, int n) {
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n) dst[i] = (int32_t)src[i];
+}
+__global__ void k_fill_u8(uint8_t *dst, uint8_t v, int n) {
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n) dst[i] = v;
+}
+__global__ void k_fill_dmat2(dmat2 *dst, dmat2 v, int n) {
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n) dst[i] = v;
+}
+__global__ void k_fill_f32(float *dst, float v, int n) {
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n) dst[i] = v;
+}
+
+}  // namespace
+
+namespace sphnj {
+void launch_u8_from_i32(cudaStream_t st, uint8_t *dst, const int32_t *src, int n) {
+    if (n > 0) k_u8_from_i32<<<grid_for(n, 256), 256, 0, st>>>(dst, src, n);
+}
+void launch_i32_from_u8(cudaStream_t st, int32_t *dst, const uint8_t *src, int n) {
+    if (n > 0) k_i32_from_u8<<<grid_for(n, 256), 256, 0, st>>>(dst, src, n);
+}
+void launch_fill_u8(cudaStream_t st, uint8_t *dst, uint8_t v, int n) {
+    if (n > 0) k_fill_u8<<<grid_for(n, 256), 256, 0, st>>>(dst, v, n);
+}
+void launch_fill_dmat2(cudaStream_t st, dmat2 *dst, dmat2 v, int n) {
+    if (n > 0) k_fill_dmat2<<<grid_for(n, 256), 256, 0, st>>>(dst, v, n);
+}
+void launch_fill_f32(cudaStream_t st, float *dst, float v, int n) {
+    if (n > 0) k_fill_f32<<<grid_for(n, 256), 256, 0, st>>>(dst, v, n);
+}
+}  // namespace sphnj
+
+namespace {
+enum Stage {
+    ST_BIN, ST_SORT, ST_REBUILD, ST_CAPACITY, ST_SOLID_COUPLE, ST_VIRT_DATA, ST_FLUID_PAIR, ST_FLUID_UPDATE,
+    ST_SOLID_DEFORM, ST_SOLID_FORCE, ST_SOLID_UPDATE, ST_SHIFT_GRADIENT, ST_SHIFT_UPDATE, ST_COUNT
+};
+const char *kStageNames[ST_COUNT] = {"bin", "sort", "rebuild", "capacity", "solid_couple", "virt_data",
+                                     "fluid_pair", "fluid_update", "solid_deformation", "solid_force",
+                                     "solid_update", "shift_gradient", "shift_update"};
+struct ProfRec {
+    int stage, kernels;
+    cudaEvent_t a, b;
+};
+}  // namespace
+
+struct sphnj_ctx {
+    sphnj_params p;
+    // measurement
+    bool prof = false;
+    std::vector<ProfRec> pending;
+    std::vector<cudaEvent_t> pool;
+    double prof_ms[ST_COUNT] = {};
+    int64_t prof_calls[ST_COUNT] = {}, prof_kernels[ST_COUNT] = {};
+    uint64_t launches = 0;
+    int form = SPHNJ_FORM_PLAIN;
+    int device = 0;
+    cudaStream_t own = nullptr, st = nullptr;
+    char *arena = nullptr;
+    size_t arena_bytes = 0;
+    DevState d{};
+    CellList lf[2]{}, ls[2]{}, lv{};
+    ListScratch sc{};
+    void *payload = nullptr;
+    DevErr *h_err = nullptr;  // pinned
+    int step = 0;
+    int parity = 0;
+    bool virt_sorted = false;
+    bool uploaded = false;
+    std::string msg = "ok";
+};
+
+namespace {
+
+int fail(sphnj_ctx *c, int code, const std::string &m) {
+    if (c) c->msg = m;
+    return code;
+}
+
+int cuda_fail(sphnj_ctx *c, cudaError_t e, const char *where) {
+    return fail(c, SPHNJ_ERR_CUDA, std::string(where) + ": " + cudaGetErrorString(e));
+}
+
+#define CK(call)                                                       \
+    do {                                                               \
+        cudaError_t e_ = (call);                                       \
+        if (e_ != cudaSuccess) return cuda_fail(ctx, e_, #call);       \
+    } while (0)
+
+size_t layout(sphnj_ctx *ctx, char *base) {
+    const sphnj_params &p = ctx->p;
+    const int nf = p.fluid_number_total, ns = p.solid_number, nv = p.virt_number, C = p.cell_number_total;
+    const int nmax = std::max(nf, std::max(ns, nv));
+    Carver a{base};
+    DevState &d = ctx->d;
+    d.f_pos = a.take<float2>(nf); d.f_vel = a.take<float2>(nf);
+    d.f_grad = a.take<float2>(nf); d.f_dudt = a.take<float2>(nf);
+    d.f_rho = a.take<float>(nf); d.f_p = a.take<float>(nf);
+    d.f_color = a.take<float>(nf); d.f_drho = a.take<float>(nf);
+    d.f_dudx = a.take<float4>(nf);
+    d.f_phase = a.take<uint8_t>(nf); d.f_fbt = a.take<uint8_t>(nf); d.f_near = a.take<uint8_t>(nf);
+    d.f_cell = a.take<int>(nf);
+    d.s_pos = a.take<double2>(ns); d.s_ref = a.take<double2>(ns);
+    d.s_vel = a.take<double2>(ns); d.s_dudt = a.take<double2>(ns);
+    d.s_F = a.take<dmat2>(ns); d.s_P = a.take<dmat2>(ns); d.s_L = a.take<dmat2>(ns);
+    d.s_maxstrain = a.take<dmat2>(ns);
+    d.s_p = a.take<float>(ns); d.s_normal = a.take<float2>(ns); d.s_couple = a.take<float2>(ns);
+    d.s_bt = a.take<uint8_t>(ns); d.s_mat = a.take<uint8_t>(ns); d.s_cell = a.take<int>(ns);
+    d.v_pos = a.take<float2>(nv); d.v_normal = a.take<float2>(nv); d.v_vel = a.take<float2>(nv);
+    d.v_p = a.take<float>(nv); d.v_rho = a.take<float>(nv);
+    d.v_phase = a.take<uint8_t>(nv); d.v_bt = a.take<uint8_t>(nv); d.v_cell = a.take<int>(nv);
+    for (int k = 0; k < 2; ++k) {
+        ctx->lf[k].rng = a.take<int2>(C); ctx->lf[k].lst = a.take<int>(nf);
+        ctx->ls[k].rng = a.take<int2>(C); ctx->ls[k].lst = a.take<int>(ns);
+    }
+    ctx->lv.rng = a.take<int2>(C); ctx->lv.lst = a.take<int>(nv);
+    ctx->sc.cnt9 = a.take<int>((size_t)9 * C);
+    ctx->sc.cnt = a.take<int>(C);
+    ctx->sc.local = a.take<int>(C);
+    ctx->sc.sums = a.take<int>(SCAN_MAX_TILES);
+    ctx->sc.cursor = a.take<int>(C);
+    ctx->sc.bucket = a.take<int>(nmax);
+    ctx->sc.sorted = a.take<int>(nmax);
+    size_t pay = std::max((size_t)nf * 30, std::max((size_t)ns * 86, (size_t)nv * 21)) + 8 * 256;
+    ctx->payload = a.take<char>(pay);
+    d.max_speed2_bits = a.take<unsigned int>(1);
+    d.err = a.take<DevErr>(1);
+    return a.off;
+}
+
+void bind_lists(sphnj_ctx *ctx) {
+    ctx->d.rng_f = ctx->lf[ctx->parity].rng;
+    ctx->d.lst_f = ctx->lf[ctx->parity].lst;
+    ctx->d.rng_s = ctx->ls[ctx->parity].rng;
+    ctx->d.lst_s = ctx->ls[ctx->parity].lst;
+    ctx->d.rng_v = ctx->lv.rng;
+    ctx->d.lst_v = ctx->lv.lst;
+}
+
+cudaEvent_t take_event(sphnj_ctx *ctx) {
+    if (!ctx->pool.empty()) {
+        cudaEvent_t e = ctx->pool.back();
+        ctx->pool.pop_back();
+        return e;
+    }
+    cudaEvent_t e = nullptr;
+    cudaEventCreate(&e);
+    return e;
+}
+
+int check_device_error(sphnj_ctx *ctx) {
+    CK(cudaMemcpyAsync(ctx->h_err, ctx->d.err, sizeof(DevErr), cudaMemcpyDeviceToHost, ctx->st));
+    CK(cudaStreamSynchronize(ctx->st));
+    const DevErr &e = *ctx->h_err;
+    if (e.code == 0) return SPHNJ_OK;
+    char buf[256];
+    switch (e.code) {
+    case SPHNJ_ERR_OUT_OF_GRID:
+        snprintf(buf, sizeof buf, "particle outside the cell grid (kind %d, index %d, cell id %d)", e.info[0],
+                 e.info[1], e.info[2]);
+        break;
+    case SPHNJ_ERR_CELL_OVERFLOW:
+        snprintf(buf, sizeof buf, "cell %d holds %d particles, more than the reference's %d slots", e.info[0],
+                 e.info[1], SPHNJ_CELL_SIZE);
+        break;
+    default:
+        snprintf(buf, sizeof buf, "device error %d (%d %d %d)", e.code, e.info[0], e.info[1], e.info[2]);
+    }
+    return fail(ctx, e.code, buf);
+}
+
+template <class T> int h2d(sphnj_ctx *ctx, T *dst, const void *src, size_t n) {
+    if (n == 0) return SPHNJ_OK;
+    CK(cudaMemcpyAsync(dst, src, n * sizeof(T), cudaMemcpyHostToDevice, ctx->st));
+    return SPHNJ_OK;
+}
+template <class T> int d2h(sphnj_ctx *ctx, void *dst, const T *src, size_t n) {
+    if (n == 0 || !dst) return SPHNJ_OK;
+    CK(cudaMemcpyAsync(dst, src, n * sizeof(T), cudaMemcpyDeviceToHost, ctx->st));
+    return SPHNJ_OK;
+}
+// 32-bit enum array on the host <-> uint8 on the device, through the bucket
+// scratch (free outside a step).
+int enum_h2d(sphnj_ctx *ctx, uint8_t *dst, const int32_t *src, int n) {
+    if (n == 0) return SPHNJ_OK;
+    CK(cudaMemcpyAsync(ctx->sc.bucket, src, n * sizeof(int32_t), cudaMemcpyHostToDevice, ctx->st));
+    launch_u8_from_i32(ctx->st, dst, ctx->sc.bucket, n);
+    // the staging buffer is reused by the next field: order through the stream
+    return SPHNJ_OK;
+}
+int enum_d2h(sphnj_ctx *ctx, int32_t *dst, const uint8_t *src, int n) {
+    if (n == 0 || !dst) return SPHNJ_OK;
+    launch_i32_from_u8(ctx->st, ctx->sc.bucket, src, n);
+    CK(cudaMemcpyAsync(dst, ctx->sc.bucket, n * sizeof(int32_t), cudaMemcpyDeviceToHost, ctx->st));
+    CK(cudaStreamSynchronize(ctx->st));  // staging reused by the next field
+    return SPHNJ_OK;
+}
+
+#define RET(x)                      \
+    do {                            \
+        int r_ = (x);               \
+        if (r_) return r_;          \
+    } while (0)
+
+}  // namespace
+
+extern "C" {
+
+int sphnj_create(const sphnj_params *p, int form, sphnj_ctx **out) {
+    if (!p || !out) return SPHNJ_ERR_ARG;
+    *out = nullptr;
+    if (form != SPHNJ_FORM_PLAIN) return SPHNJ_ERR_UNSUPPORTED;
+    if (p->fluid_number_total < 0 || p->solid_number < 0 || p->virt_number < 0) return SPHNJ_ERR_ARG;
+    if (p->cell_number[0] < 3 || p->cell_number[1] < 3 ||
+        (long)p->cell_number[0] * p->cell_number[1] != p->cell_number_total)
+        return SPHNJ_ERR_ARG;
+    if ((p->cell_number_total + SCAN_TILE - 1) / SCAN_TILE > SCAN_MAX_TILES) return SPHNJ_ERR_UNSUPPORTED;
+    if (p->sort_every_step < 1 || p->solid_sub_step < 1 || p->shift_per_step < 0) return SPHNJ_ERR_ARG;
+    int ndev = 0;
+    if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0) {
+        cudaGetLastError();
+        return SPHNJ_ERR_NO_DEVICE;
+    }
+    sphnj_ctx *ctx = new sphnj_ctx;
+    ctx->p = *p;
+    ctx->form = form;
+    cudaGetDevice(&ctx->device);
+    ctx->arena_bytes = layout(ctx, nullptr);
+    cudaError_t e = cudaMalloc(&ctx->arena, ctx->arena_bytes);
+    if (e != cudaSuccess) {
+        cudaGetLastError();
+        delete ctx;
+        return SPHNJ_ERR_CUDA;
+    }
+    layout(ctx, ctx->arena);
+    if (cudaStreamCreateWithFlags(&ctx->own, cudaStreamNonBlocking) != cudaSuccess ||
+        cudaMallocHost(&ctx->h_err, sizeof(DevErr)) != cudaSuccess) {
+        cudaGetLastError();
+        sphnj_destroy(ctx);
+        return SPHNJ_ERR_CUDA;
+    }
+    ctx->st = ctx->own;
+    if (cudaMemsetAsync(ctx->arena, 0, ctx->arena_bytes, ctx->st) != cudaSuccess ||
+        cudaStreamSynchronize(ctx->st) != cudaSuccess) {
+        sphnj_destroy(ctx);
+        return SPHNJ_ERR_CUDA;
+    }
+    bind_lists(ctx);
+    *out = ctx;
+    return SPHNJ_OK;
+}
+
+void sphnj_destroy(sphnj_ctx *ctx) {
+    if (!ctx) return;
+    cudaSetDevice(ctx->device);
+    if (ctx->st) cudaStreamSynchronize(ctx->st);
+    for (auto &r : ctx->pending) {
+        cudaEventDestroy(r.a);
+        cudaEventDestroy(r.b);
+    }
+    for (auto e : ctx->pool) cudaEventDestroy(e);
+    if (ctx->arena) cudaFree(ctx->arena);
+    if (ctx->h_err) cudaFreeHost(ctx->h_err);
+    if (ctx->own) cudaStreamDestroy(ctx->own);
+    delete ctx;
+}
+
+int sphnj_set_stream(sphnj_ctx *ctx, void *stream) {
+    if (!ctx) return SPHNJ_ERR_ARG;
+    cudaSetDevice(ctx->device);
+    CK(cudaStreamSynchronize(ctx->st));
+    ctx->st = stream ? static_cast<cudaStream_t>(stream) : ctx->own;
+    return SPHNJ_OK;
+}
+
+int sphnj_upload(sphnj_ctx *ctx, const sphnj_host_state *s) {
+    if (!ctx || !s) return SPHNJ_ERR_ARG;
+    cudaSetDevice(ctx->device);
+    const sphnj_params &p = ctx->p;
+    const int nf = p.fluid_number_total, ns = p.solid_number, nv = p.virt_number, C = p.cell_number_total;
+    DevState &d = ctx->d;
+    cudaStream_t st = ctx->st;
+    // fluid (host_data.cuh:24-46)
+    if (s->fluid_position) RET(h2d(ctx, d.f_pos, s->fluid_position, nf)); else CK(cudaMemsetAsync(d.f_pos, 0, 8ul * nf, st));
+    if (s->fluid_velocity) RET(h2d(ctx, d.f_vel, s->fluid_velocity, nf)); else CK(cudaMemsetAsync(d.f_vel, 0, 8ul * nf, st));
+    if (s->fluid_density) RET(h2d(ctx, d.f_rho, s->fluid_density, nf)); else CK(cudaMemsetAsync(d.f_rho, 0, 4ul * nf, st));
+    if (s->fluid_pressure) RET(h2d(ctx, d.f_p, s->fluid_pressure, nf)); else CK(cudaMemsetAsync(d.f_p, 0, 4ul * nf, st));
+    if (s->fluid_phase) RET(enum_h2d(ctx, d.f_phase, s->fluid_phase, nf)); else CK(cudaMemsetAsync(d.f_phase, 0, nf, st));
+    if (s->fluid_boundary_type) RET(enum_h2d(ctx, d.f_fbt, s->fluid_boundary_type, nf));
+    else launch_fill_u8(st, d.f_fbt, SPHNJ_FREE_SURFACE, nf);
+    if (s->fluid_has_near_particle) RET(enum_h2d(ctx, d.f_near, s->fluid_has_near_particle, nf));
+    else CK(cudaMemsetAsync(d.f_near, SPHNJ_NO_PARTICLE, nf, st));
+    if (s->fluid_du_dx) RET(h2d(ctx, d.f_dudx, s->fluid_du_dx, nf)); else CK(cudaMemsetAsync(d.f_dudx, 0, 16ul * nf, st));
+    if (s->fluid_gradient) RET(h2d(ctx, d.f_grad, s->fluid_gradient, nf)); else CK(cudaMemsetAsync(d.f_grad, 0, 8ul * nf, st));
+    if (s->fluid_du_dt) RET(h2d(ctx, d.f_dudt, s->fluid_du_dt, nf)); else CK(cudaMemsetAsync(d.f_dudt, 0, 8ul * nf, st));
+    if (s->fluid_color) RET(h2d(ctx, d.f_color, s->fluid_color, nf)); else CK(cudaMemsetAsync(d.f_color, 0, 4ul * nf, st));
+    if (s->fluid_drho_dt) RET(h2d(ctx, d.f_drho, s->fluid_drho_dt, nf)); else CK(cudaMemsetAsync(d.f_drho, 0, 4ul * nf, st));
+    // solid (host_data.cuh:64-87)
+    const dmat2 I = {1.0, 0.0, 0.0, 1.0}, Z = {0.0, 0.0, 0.0, 0.0};
+    const dmat2 MS = {-(double)p.yield_strain, 0.0, 0.0, -(double)p.yield_strain};
+    if (s->solid_position) RET(h2d(ctx, d.s_pos, s->solid_position, ns)); else CK(cudaMemsetAsync(d.s_pos, 0, 16ul * ns, st));
+    if (s->solid_reference_position) RET(h2d(ctx, d.s_ref, s->solid_reference_position, ns));
+    else CK(cudaMemsetAsync(d.s_ref, 0, 16ul * ns, st));
+    if (s->solid_velocity) RET(h2d(ctx, d.s_vel, s->solid_velocity, ns)); else CK(cudaMemsetAsync(d.s_vel, 0, 16ul * ns, st));
+    if (s->solid_boundary_type) RET(enum_h2d(ctx, d.s_bt, s->solid_boundary_type, ns)); else CK(cudaMemsetAsync(d.s_bt, 0, ns, st));
+    if (s->solid_material_type) RET(enum_h2d(ctx, d.s_mat, s->solid_material_type, ns)); else CK(cudaMemsetAsync(d.s_mat, 0, ns, st));
+    if (s->solid_max_strain) RET(h2d(ctx, d.s_maxstrain, s->solid_max_strain, ns)); else launch_fill_dmat2(st, d.s_maxstrain, MS, ns);
+    if (s->solid_pressure) RET(h2d(ctx, d.s_p, s->solid_pressure, ns)); else CK(cudaMemsetAsync(d.s_p, 0, 4ul * ns, st));
+    if (s->solid_deformation) RET(h2d(ctx, d.s_F, s->solid_deformation, ns)); else launch_fill_dmat2(st, d.s_F, I, ns);
+    if (s->solid_stress_1st_piola) RET(h2d(ctx, d.s_P, s->solid_stress_1st_piola, ns)); else launch_fill_dmat2(st, d.s_P, Z, ns);
+    if (s->solid_correction) RET(h2d(ctx, d.s_L, s->solid_correction, ns)); else launch_fill_dmat2(st, d.s_L, I, ns);
+    if (s->solid_du_dt) RET(h2d(ctx, d.s_dudt, s->solid_du_dt, ns)); else CK(cudaMemsetAsync(d.s_dudt, 0, 16ul * ns, st));
+    if (s->solid_normal) RET(h2d(ctx, d.s_normal, s->solid_normal, ns)); else CK(cudaMemsetAsync(d.s_normal, 0, 8ul * ns, st));
+    if (s->solid_couple_dudt) RET(h2d(ctx, d.s_couple, s->solid_couple_dudt, ns)); else CK(cudaMemsetAsync(d.s_couple, 0, 8ul * ns, st));
+    // virtual (host_data.cuh:99-115)
+    if (s->virt_position) RET(h2d(ctx, d.v_pos, s->virt_position, nv)); else CK(cudaMemsetAsync(d.v_pos, 0, 8ul * nv, st));
+    if (s->virt_velocity) RET(h2d(ctx, d.v_vel, s->virt_velocity, nv)); else CK(cudaMemsetAsync(d.v_vel, 0, 8ul * nv, st));
+    if (s->virt_pressure) RET(h2d(ctx, d.v_p, s->virt_pressure, nv)); else CK(cudaMemsetAsync(d.v_p, 0, 4ul * nv, st));
+    if (s->virt_density) RET(h2d(ctx, d.v_rho, s->virt_density, nv)); else launch_fill_f32(st, d.v_rho, p.reference_density[0], nv);
+    if (s->virt_phase) RET(enum_h2d(ctx, d.v_phase, s->virt_phase, nv)); else CK(cudaMemsetAsync(d.v_phase, SPHNJ_LIQUID, nv, st));
+    if (s->virt_boundary_type) RET(enum_h2d(ctx, d.v_bt, s->virt_boundary_type, nv)); else CK(cudaMemsetAsync(d.v_bt, 0, nv, st));
+    // cell lists start empty (Cell(), cell.cuh:31-46)
+    for (int k = 0; k < 2; ++k) {
+        CK(cudaMemsetAsync(ctx->lf[k].rng, 0, sizeof(int2) * C, st));
+        CK(cudaMemsetAsync(ctx->ls[k].rng, 0, sizeof(int2) * C, st));
+    }
+    CK(cudaMemsetAsync(ctx->lv.rng, 0, sizeof(int2) * C, st));
+    CK(cudaMemsetAsync(d.err, 0, sizeof(DevErr), st));
+    CK(cudaMemsetAsync(d.max_speed2_bits, 0, sizeof(unsigned), st));
+    ctx->parity = 0;
+    ctx->virt_sorted = false;
+    ctx->step = p.istart;
+    bind_lists(ctx);
+    // wall normals once before the loop (virtNormalCalculation, calculation.cu:28)
+    if (s->virt_normal) RET(h2d(ctx, d.v_normal, s->virt_normal, nv));
+    else launch_virt_normal(st, p, d);
+    CK(cudaGetLastError());
+    CK(cudaStreamSynchronize(st));
+    ctx->uploaded = true;
+    return SPHNJ_OK;
+}
+
+int sphnj_step(sphnj_ctx *ctx, int n) {
+    if (!ctx || n < 0) return SPHNJ_ERR_ARG;
+    if (!ctx->uploaded) return fail(ctx, SPHNJ_ERR_ARG, "sphnj_step before sphnj_upload");
+    cudaSetDevice(ctx->device);
+    const sphnj_params &p = ctx->p;
+    const int nf = p.fluid_number_total, ns = p.solid_number, nv = p.virt_number;
+    cudaStream_t st = ctx->st;
+    DevState &d = ctx->d;
+    // kernels each launcher issues (kernels_*.cu)
+    constexpr int kSortKernels = 7, kRebuildKernels = 4;
+    auto stage = [&](int s, int kernels, auto &&fn) {
+        ProfRec r{s, kernels, nullptr, nullptr};
+        if (ctx->prof) {
+            r.a = take_event(ctx);
+            r.b = take_event(ctx);
+            cudaEventRecord(r.a, st);
+        }
+        fn();
+        if (ctx->prof) {
+            cudaEventRecord(r.b, st);
+            ctx->pending.push_back(r);
+        }
+        ctx->launches += (uint64_t)kernels;
+    };
+    for (int it = 0; it < n; ++it) {
+        ctx->step++;
+        const bool is_sort = ((ctx->step - 1) % p.sort_every_step) == 0;  // SimTime::isSort
+        stage(ST_BIN, 1, [&] { launch_bin(st, p, d, !ctx->virt_sorted); });
+        if (is_sort) {
+            if (nf > 0)
+                stage(ST_SORT, kSortKernels,
+                      [&] { launch_sort_kind(st, p, d, KF, nf, d.f_cell, ctx->sc, ctx->lf[ctx->parity], ctx->payload); });
+            if (ns > 0)
+                stage(ST_SORT, kSortKernels,
+                      [&] { launch_sort_kind(st, p, d, KS, ns, d.s_cell, ctx->sc, ctx->ls[ctx->parity], ctx->payload); });
+            if (nv > 0 && !ctx->virt_sorted) {
+                // virtual particles never move: after this first sort their
+                // order, cell ids and lists stay as they are (a stable sort of
+                // sorted keys is the identity)
+                stage(ST_SORT, kSortKernels,
+                      [&] { launch_sort_kind(st, p, d, KV, nv, d.v_cell, ctx->sc, ctx->lv, ctx->payload); });
+                ctx->virt_sorted = true;
+            }
+        } else {
+            ctx->parity ^= 1;
+            const int cur = ctx->parity, prev = cur ^ 1;
+            if (nf > 0)
+                stage(ST_REBUILD, kRebuildKernels,
+                      [&] { launch_rebuild_kind(st, p, nf, d.f_cell, ctx->lf[prev], ctx->lf[cur], ctx->sc, d.err); });
+            if (ns > 0)
+                stage(ST_REBUILD, kRebuildKernels,
+                      [&] { launch_rebuild_kind(st, p, ns, d.s_cell, ctx->ls[prev], ctx->ls[cur], ctx->sc, d.err); });
+        }
+        bind_lists(ctx);
+        stage(ST_CAPACITY, 1, [&] { launch_capacity_check(st, p, d); });
+        if (nf > 0 && ns > 0) stage(ST_SOLID_COUPLE, 1, [&] { launch_solid_couple(st, p, d); });
+        if (nv > 0) stage(ST_VIRT_DATA, 1, [&] { launch_virt_data(st, p, d); });
+        if (nf > 0) {
+            stage(ST_FLUID_PAIR, 1, [&] { launch_fluid_pair(st, p, d); });
+            stage(ST_FLUID_UPDATE, 1, [&] { launch_fluid_update(st, p, d); });
+        }
+        if (ns > 0)
+            for (int k = 0; k < p.solid_sub_step; ++k) {
+                stage(ST_SOLID_DEFORM, 1, [&] { launch_solid_deformation(st, p, d); });
+                stage(ST_SOLID_FORCE, 1, [&] { launch_solid_force(st, p, d); });
+                stage(ST_SOLID_UPDATE, 1, [&] { launch_solid_update(st, p, d); });
+            }
+        if (nf > 0)
+            for (int k = 0; k < p.shift_per_step; ++k) {
+                stage(ST_SHIFT_GRADIENT, 1, [&] { launch_shift_gradient(st, p, d); });
+                stage(ST_SHIFT_UPDATE, 1, [&] { launch_shift_update(st, p, d); });
+            }
+        CK(cudaGetLastError());
+    }
+    return SPHNJ_OK;
+}
+
+int sphnj_upload_fields(sphnj_ctx *ctx, uint32_t mask, const sphnj_host_state *s) {
+    if (!ctx || !s) return SPHNJ_ERR_ARG;
+    if (!ctx->uploaded) return fail(ctx, SPHNJ_ERR_ARG, "sphnj_upload_fields before sphnj_upload");
+    cudaSetDevice(ctx->device);
+    const sphnj_params &p = ctx->p;
+    const int nf = p.fluid_number_total, ns = p.solid_number, nv = p.virt_number;
+    DevState &d = ctx->d;
+    if (mask & SPHNJ_F_FLUID_KINEMATICS) {
+        if (s->fluid_position) RET(h2d(ctx, d.f_pos, s->fluid_position, nf));
+        if (s->fluid_velocity) RET(h2d(ctx, d.f_vel, s->fluid_velocity, nf));
+    }
+    if (mask & SPHNJ_F_FLUID_THERMO) {
+        if (s->fluid_density) RET(h2d(ctx, d.f_rho, s->fluid_density, nf));
+        if (s->fluid_pressure) RET(h2d(ctx, d.f_p, s->fluid_pressure, nf));
+        if (s->fluid_phase) RET(enum_h2d(ctx, d.f_phase, s->fluid_phase, nf));
+    }
+    if (mask & SPHNJ_F_FLUID_FLAGS) {
+        if (s->fluid_boundary_type) RET(enum_h2d(ctx, d.f_fbt, s->fluid_boundary_type, nf));
+        if (s->fluid_has_near_particle) RET(enum_h2d(ctx, d.f_near, s->fluid_has_near_particle, nf));
+    }
+    if (mask & SPHNJ_F_FLUID_DERIVED) {
+        if (s->fluid_du_dx) RET(h2d(ctx, d.f_dudx, s->fluid_du_dx, nf));
+        if (s->fluid_gradient) RET(h2d(ctx, d.f_grad, s->fluid_gradient, nf));
+        if (s->fluid_du_dt) RET(h2d(ctx, d.f_dudt, s->fluid_du_dt, nf));
+        if (s->fluid_color) RET(h2d(ctx, d.f_color, s->fluid_color, nf));
+        if (s->fluid_drho_dt) RET(h2d(ctx, d.f_drho, s->fluid_drho_dt, nf));
+    }
+    if (mask & SPHNJ_F_SOLID_KINEMATICS) {
+        if (s->solid_position) RET(h2d(ctx, d.s_pos, s->solid_position, ns));
+        if (s->solid_reference_position) RET(h2d(ctx, d.s_ref, s->solid_reference_position, ns));
+        if (s->solid_velocity) RET(h2d(ctx, d.s_vel, s->solid_velocity, ns));
+    }
+    if (mask & SPHNJ_F_SOLID_MATERIAL) {
+        if (s->solid_boundary_type) RET(enum_h2d(ctx, d.s_bt, s->solid_boundary_type, ns));
+        if (s->solid_material_type) RET(enum_h2d(ctx, d.s_mat, s->solid_material_type, ns));
+        if (s->solid_max_strain) RET(h2d(ctx, d.s_maxstrain, s->solid_max_strain, ns));
+    }
+    if (mask & SPHNJ_F_SOLID_DERIVED) {
+        if (s->solid_pressure) RET(h2d(ctx, d.s_p, s->solid_pressure, ns));
+        if (s->solid_deformation) RET(h2d(ctx, d.s_F, s->solid_deformation, ns));
+        if (s->solid_stress_1st_piola) RET(h2d(ctx, d.s_P, s->solid_stress_1st_piola, ns));
+        if (s->solid_correction) RET(h2d(ctx, d.s_L, s->solid_correction, ns));
+        if (s->solid_du_dt) RET(h2d(ctx, d.s_dudt, s->solid_du_dt, ns));
+        if (s->solid_normal) RET(h2d(ctx, d.s_normal, s->solid_normal, ns));
+        if (s->solid_couple_dudt) RET(h2d(ctx, d.s_couple, s->solid_couple_dudt, ns));
+    }
+    if (mask & SPHNJ_F_VIRT) {
+        // positions of virtual particles are fixed after their first sort
+        if (s->virt_normal) RET(h2d(ctx, d.v_normal, s->virt_normal, nv));
+        if (s->virt_velocity) RET(h2d(ctx, d.v_vel, s->virt_velocity, nv));
+        if (s->virt_pressure) RET(h2d(ctx, d.v_p, s->virt_pressure, nv));
+        if (s->virt_density) RET(h2d(ctx, d.v_rho, s->virt_density, nv));
+        if (s->virt_phase) RET(enum_h2d(ctx, d.v_phase, s->virt_phase, nv));
+    }
+    CK(cudaGetLastError());
+    CK(cudaStreamSynchronize(ctx->st));
+    return SPHNJ_OK;
+}
+
+int sphnj_profile_stage_count(void) { return ST_COUNT; }
+const char *sphnj_profile_stage_name(int s) { return s >= 0 && s < ST_COUNT ? kStageNames[s] : ""; }
+
+int sphnj_profile_enable(sphnj_ctx *ctx, int on) {
+    if (!ctx) return SPHNJ_ERR_ARG;
+    cudaSetDevice(ctx->device);
+    CK(cudaStreamSynchronize(ctx->st));
+    for (auto &r : ctx->pending) {
+        ctx->pool.push_back(r.a);
+        ctx->pool.push_back(r.b);
+    }
+    ctx->pending.clear();
+    ctx->prof = on != 0;
+    for (int s = 0; s < ST_COUNT; ++s) ctx->prof_ms[s] = 0.0, ctx->prof_calls[s] = ctx->prof_kernels[s] = 0;
+    return SPHNJ_OK;
+}
+
+int sphnj_profile_read(sphnj_ctx *ctx, double *ms, int64_t *calls, int64_t *kernels) {
+    if (!ctx) return SPHNJ_ERR_ARG;
+    cudaSetDevice(ctx->device);
+    CK(cudaStreamSynchronize(ctx->st));
+    for (auto &r : ctx->pending) {
+        float t = 0.0f;
+        CK(cudaEventElapsedTime(&t, r.a, r.b));
+        ctx->prof_ms[r.stage] += t;
+        ctx->prof_calls[r.stage] += 1;
+        ctx->prof_kernels[r.stage] += r.kernels;
+        ctx->pool.push_back(r.a);
+        ctx->pool.push_back(r.b);
+    }
+    ctx->pending.clear();
+    for (int s = 0; s < ST_COUNT; ++s) {
+        if (ms) ms[s] = ctx->prof_ms[s];
+        if (calls) calls[s] = ctx->prof_calls[s];
+        if (kernels) kernels[s] = ctx->prof_kernels[s];
+    }
+    return SPHNJ_OK;
+}
+
+int sphnj_stat_launches(const sphnj_ctx *ctx, uint64_t *launches) {
+    if (!ctx || !launches) return SPHNJ_ERR_ARG;
+    *launches = ctx->launches;
+    return SPHNJ_OK;
+}
+
+int sphnj_synchronize(sphnj_ctx *ctx) {
+    if (!ctx) return SPHNJ_ERR_ARG;
+    cudaSetDevice(ctx->device);
+    return check_device_error(ctx);
+}
+
+int sphnj_download(sphnj_ctx *ctx, uint32_t mask, sphnj_host_state *s) {
+    if (!ctx || !s) return SPHNJ_ERR_ARG;
+    cudaSetDevice(ctx->device);
+    const sphnj_params &p = ctx->p;
+    const int nf = p.fluid_number_total, ns = p.solid_number, nv = p.virt_number;
+    const DevState &d = ctx->d;
+    if (mask & SPHNJ_F_FLUID_KINEMATICS) {
+        RET(d2h(ctx, s->fluid_position, d.f_pos, nf));
+        RET(d2h(ctx, s->fluid_velocity, d.f_vel, nf));
+    }
+    if (mask & SPHNJ_F_FLUID_THERMO) {
+        RET(d2h(ctx, s->fluid_density, d.f_rho, nf));
+        RET(d2h(ctx, s->fluid_pressure, d.f_p, nf));
+        RET(enum_d2h(ctx, s->fluid_phase, d.f_phase, nf));
+    }
+    if (mask & SPHNJ_F_FLUID_FLAGS) {
+        RET(enum_d2h(ctx, s->fluid_boundary_type, d.f_fbt, nf));
+        RET(enum_d2h(ctx, s->fluid_has_near_particle, d.f_near, nf));
+    }
+    if (mask & SPHNJ_F_FLUID_DERIVED) {
+        RET(d2h(ctx, s->fluid_du_dx, d.f_dudx, nf));
+        RET(d2h(ctx, s->fluid_gradient, d.f_grad, nf));
+        RET(d2h(ctx, s->fluid_du_dt, d.f_dudt, nf));
+        RET(d2h(ctx, s->fluid_color, d.f_color, nf));
+        RET(d2h(ctx, s->fluid_drho_dt, d.f_drho, nf));
+    }
+    if (mask & SPHNJ_F_SOLID_KINEMATICS) {
+        RET(d2h(ctx, s->solid_position, d.s_pos, ns));
+        RET(d2h(ctx, s->solid_reference_position, d.s_ref, ns));
+        RET(d2h(ctx, s->solid_velocity, d.s_vel, ns));
+    }
+    if (mask & SPHNJ_F_SOLID_MATERIAL) {
+        RET(enum_d2h(ctx, s->solid_boundary_type, d.s_bt, ns));
+        RET(enum_d2h(ctx, s->solid_material_type, d.s_mat, ns));
+        RET(d2h(ctx, s->solid_max_strain, d.s_maxstrain, ns));
+    }
+    if (mask & SPHNJ_F_SOLID_DERIVED) {
+        RET(d2h(ctx, s->solid_pressure, d.s_p, ns));
+        RET(d2h(ctx, s->solid_deformation, d.s_F, ns));
+        RET(d2h(ctx, s->solid_stress_1st_piola, d.s_P, ns));
+        RET(d2h(ctx, s->solid_correction, d.s_L, ns));
+        RET(d2h(ctx, s->solid_du_dt, d.s_dudt, ns));
+        RET(d2h(ctx, s->solid_normal, d.s_normal, ns));
+        RET(d2h(ctx, s->solid_couple_dudt, d.s_couple, ns));
+    }
+    if (mask & SPHNJ_F_VIRT) {
+        RET(d2h(ctx, s->virt_position, d.v_pos, nv));
+        RET(d2h(ctx, s->virt_normal, d.v_normal, nv));
+        RET(d2h(ctx, s->virt_velocity, d.v_vel, nv));
+        RET(d2h(ctx, s->virt_pressure, d.v_p, nv));
+        RET(d2h(ctx, s->virt_density, d.v_rho, nv));
+        RET(enum_d2h(ctx, s->virt_phase, d.v_phase, nv));
+        RET(enum_d2h(ctx, s->virt_boundary_type, d.v_bt, nv));
+    }
+    if (mask & SPHNJ_F_CELL_IDS) {
+        RET(d2h(ctx, s->fluid_cell_id, d.f_cell, nf));
+        RET(d2h(ctx, s->solid_cell_id, d.s_cell, ns));
+        RET(d2h(ctx, s->virt_cell_id, d.v_cell, nv));
+    }
+    return check_device_error(ctx);
+}
+
+int sphnj_get_step(const sphnj_ctx *ctx, int *step) {
+    if (!ctx || !step) return SPHNJ_ERR_ARG;
+    *step = ctx->step;
+    return SPHNJ_OK;
+}
+
+int sphnj_debug_cells(sphnj_ctx *ctx, int type, int32_t *start, int32_t *count, int32_t *list, int32_t *n_listed) {
+    if (!ctx || type < 0 || type > 2) return SPHNJ_ERR_ARG;
+    cudaSetDevice(ctx->device);
+    const int C = ctx->p.cell_number_total;
+    const CellList &L = type == 0 ? ctx->lf[ctx->parity] : type == 1 ? ctx->ls[ctx->parity] : ctx->lv;
+    const int n = type == 0 ? ctx->p.fluid_number_total : type == 1 ? ctx->p.solid_number : ctx->p.virt_number;
+    int2 *h = new int2[C > 0 ? C : 1];
+    cudaError_t e = cudaMemcpyAsync(h, L.rng, sizeof(int2) * C, cudaMemcpyDeviceToHost, ctx->st);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(ctx->st);
+    if (e != cudaSuccess) {
+        delete[] h;
+        return cuda_fail(ctx, e, "debug_cells");
+    }
+    int total = 0;
+    for (int c = 0; c < C; ++c) {
+        if (start) start[c] = h[c].x;
+        if (count) count[c] = h[c].y;
+        total += h[c].y;
+    }
+    delete[] h;
+    if (n_listed) *n_listed = total;
+    if (list && total > 0 && total <= n) {
+        CK(cudaMemcpyAsync(list, L.lst, sizeof(int) * total, cudaMemcpyDeviceToHost, ctx->st));
+        CK(cudaStreamSynchronize(ctx->st));
+    }
+    return check_device_error(ctx);
+}
+
+int sphnj_debug_set_cells(sphnj_ctx *ctx, const int32_t *cf, const int32_t *lf, const int32_t *cs,
+                          const int32_t *ls, const int32_t *cv, const int32_t *lv) {
+    if (!ctx) return SPHNJ_ERR_ARG;
+    cudaSetDevice(ctx->device);
+    const int C = ctx->p.cell_number_total;
+    const int ns_[3] = {ctx->p.fluid_number_total, ctx->p.solid_number, ctx->p.virt_number};
+    const int32_t *cnt[3] = {cf, cs, cv}, *lst[3] = {lf, ls, lv};
+    CellList L[3] = {ctx->lf[ctx->parity], ctx->ls[ctx->parity], ctx->lv};
+    int2 *h = new int2[C > 0 ? C : 1];
+    long listed[3] = {0, 0, 0};
+    for (int k = 0; k < 3; ++k) {
+        long acc = 0;
+        for (int c = 0; c < C; ++c) {
+            int n = cnt[k] ? cnt[k][c] : 0;
+            h[c] = make_int2((int)acc, n);
+            acc += n;
+        }
+        listed[k] = acc;
+        if (acc > ns_[k] || (acc > 0 && !lst[k])) {
+            delete[] h;
+            return fail(ctx, SPHNJ_ERR_ARG, "debug_set_cells: list longer than the particle count");
+        }
+        for (long q = 0; q < acc; ++q)
+            if (lst[k][q] < 0 || lst[k][q] >= ns_[k]) {
+                delete[] h;
+                return fail(ctx, SPHNJ_ERR_ARG, "debug_set_cells: particle index out of range");
+            }
+        cudaError_t e = cudaMemcpyAsync(L[k].rng, h, sizeof(int2) * C, cudaMemcpyHostToDevice, ctx->st);
+        if (e == cudaSuccess && acc > 0)
+            e = cudaMemcpyAsync(L[k].lst, lst[k], sizeof(int) * acc, cudaMemcpyHostToDevice, ctx->st);
+        if (e == cudaSuccess) e = cudaStreamSynchronize(ctx->st);
+        if (e != cudaSuccess) {
+            delete[] h;
+            return cuda_fail(ctx, e, "debug_set_cells");
+        }
+    }
+    delete[] h;
+    // virtual lists that hold every virtual particle mean the first sort
+    // already happened (their order and ids are final)
+    ctx->virt_sorted = ns_[2] > 0 && listed[2] == ns_[2];
+    bind_lists(ctx);
+    return SPHNJ_OK;
+}
+
+int sphnj_debug_set_step(sphnj_ctx *ctx, int step) {
+    if (!ctx) return SPHNJ_ERR_ARG;
+    ctx->step = step;
+    return SPHNJ_OK;
+}
+
+int sphnj_debug_max_speed(sphnj_ctx *ctx, float *ms) {
+    if (!ctx || !ms) return SPHNJ_ERR_ARG;
+    cudaSetDevice(ctx->device);
+    unsigned int bits = 0;
+    CK(cudaMemcpyAsync(&bits, ctx->d.max_speed2_bits, sizeof bits, cudaMemcpyDeviceToHost, ctx->st));
+    CK(cudaStreamSynchronize(ctx->st));
+    float v2;
+    std::memcpy(&v2, &bits, sizeof v2);
+    float vmax = sqrtf(v2);
+    float cap = 0.1f * std::min(ctx->p.sound_speed[0], ctx->p.sound_speed[1]);
+    *ms = std::min(vmax, cap);
+    return SPHNJ_OK;
+}
+
+const char *sphnj_last_error(const sphnj_ctx *ctx) { return ctx ? ctx->msg.c_str() : "null context"; }
+
+}  // extern "C"

@@ -1,0 +1,135 @@
+// Device-side building blocks of libsphnj: the SoA pointer table passed to
+// every kernel, the cell grid, error flagging and small vector helpers.
+//
+// HBM layout (one arena per context, every sub-buffer 256-byte aligned):
+//   fluid  : pos float2, vel float2, rho float, p float, phase/boundary/near
+//            uint8, du_dx float4 (column-major 2x2), gradient float2,
+//            du_dt float2, color float, drho_dt float, cell int32
+//   solid  : pos/ref/vel/du_dt double2, F/P/L/max_strain dmat2 (32 B),
+//            pressure float, normal/couple float2, boundary/material uint8,
+//            cell int32
+//   virtual: pos/normal/vel float2, p/rho float, phase/boundary uint8,
+//            cell int32
+//   cells  : per particle kind a CSR range table int2{start,count}[C] and
+//            an index list int32[N]; fluid and solid tables are double
+//            buffered (previous/current) for the incremental rebuild.
+#pragma once
+
+#include <cstdint>
+#include <cuda_runtime.h>
+
+#include "../../include/sphnj.h"
+
+namespace sphnj {
+
+struct __align__(32) dmat2 {
+    double m00, m10, m01, m11;  // column-major, as Eigen::Matrix2d
+};
+
+struct DevErr {
+    int code;       // first error wins (atomicCAS from 0)
+    int info[3];
+};
+
+// Pointers to one scene's device state.  Passed by value to kernels.
+struct DevState {
+    // fluid
+    float2 *f_pos, *f_vel, *f_grad, *f_dudt;
+    float *f_rho, *f_p, *f_color, *f_drho;
+    float4 *f_dudx;
+    uint8_t *f_phase, *f_fbt, *f_near;
+    int *f_cell;
+    // solid
+    double2 *s_pos, *s_ref, *s_vel, *s_dudt;
+    dmat2 *s_F, *s_P, *s_L, *s_maxstrain;
+    float *s_p;
+    float2 *s_normal, *s_couple;
+    uint8_t *s_bt, *s_mat;
+    int *s_cell;
+    // virtual
+    float2 *v_pos, *v_normal, *v_vel;
+    float *v_p, *v_rho;
+    uint8_t *v_phase, *v_bt;
+    int *v_cell;
+    // current cell lists (CSR) used by the neighbour sweeps
+    const int2 *rng_f, *rng_s, *rng_v;
+    const int *lst_f, *lst_s, *lst_v;
+    // scalars
+    unsigned int *max_speed2_bits;  // max over fluid of |v|^2 (float bits)
+    DevErr *err;
+};
+
+__device__ __forceinline__ void raise_error(DevErr *e, int code, int a = 0, int b = 0, int c = 0) {
+    if (atomicCAS(&e->code, 0, code) == 0) {
+        e->info[0] = a;
+        e->info[1] = b;
+        e->info[2] = c;
+    }
+}
+
+// findPositionCell, pair.cu:8-18: x-major cell id from the float position,
+// (y - ymin) * inv_dy truncated toward zero plus the column index times ny.
+// Explicit round-to-nearest intrinsics keep the result independent of
+// contraction, so ids are bit-identical to the reference's host/device math.
+__device__ __forceinline__ int cell_of(const sphnj_params &p, float x, float y) {
+    int iy = (int)__fmul_rn(__fsub_rn(y, p.cell_xmin[1]), p.interval_inv[1]);
+    int ix = (int)__fmul_rn(__fsub_rn(x, p.cell_xmin[0]), p.interval_inv[0]);
+    return iy + ix * p.cell_number[1];
+}
+
+// Neighbour slot n (0..8) of cell c: n = 3*(di+1) + (dj+1), di the column
+// (x) offset, dj the row (y) offset, -1 outside the grid - the table built
+// by Sim::createCell, sim.cu:175-193.
+__device__ __forceinline__ int neighbour_cell(int c, int n, int nx, int ny) {
+    int ci = c / ny, cj = c - ci * ny;
+    int i = ci + n / 3 - 1, j = cj + n % 3 - 1;
+    if (i < 0 || i >= nx || j < 0 || j >= ny) return -1;
+    return i * ny + j;
+}
+
+// Gaussian kernel-gradient factor exp(-q^2) * Kd * C32 (fluid.cu:44-46)
+__device__ __forceinline__ float grad_w(const sphnj_params &p, float q2) {
+    return expf(-q2) * p.kernel_differential * p.coefficient_3d_to_2d;
+}
+// Truncated-Gaussian Shepard weight (exp(-q^2) - e^{-R^2}) * C2 * C32
+// (virt.cu:71-74, solid.cu:381-386)
+__device__ __forceinline__ float shepard_w(const sphnj_params &p, float q2) {
+    return (expf(-q2) - p.kernel_coefficient_1) * p.kernel_coefficient_2 * p.coefficient_3d_to_2d;
+}
+
+__device__ __forceinline__ float sqn(float2 a) { return a.x * a.x + a.y * a.y; }
+__device__ __forceinline__ float dot2(float2 a, float2 b) { return a.x * b.x + a.y * b.y; }
+__device__ __forceinline__ float2 sub2(float2 a, float2 b) { return make_float2(a.x - b.x, a.y - b.y); }
+// Eigen normalized(): zero vector returned unchanged
+__device__ __forceinline__ float2 normalized(float2 a) {
+    float z = sqn(a);
+    if (z > 0.0f) {
+        float s = sqrtf(z);
+        return make_float2(a.x / s, a.y / s);
+    }
+    return a;
+}
+__device__ __forceinline__ float2 to_f2(double2 a) { return make_float2((float)a.x, (float)a.y); }
+
+__device__ __forceinline__ dmat2 dmul(const dmat2 &a, const dmat2 &b) {
+    return {a.m00 * b.m00 + a.m01 * b.m10, a.m10 * b.m00 + a.m11 * b.m10,
+            a.m00 * b.m01 + a.m01 * b.m11, a.m10 * b.m01 + a.m11 * b.m11};
+}
+__device__ __forceinline__ double2 dmv(const dmat2 &a, double2 v) {
+    return make_double2(a.m00 * v.x + a.m01 * v.y, a.m10 * v.x + a.m11 * v.y);
+}
+__device__ __forceinline__ dmat2 dtrans(const dmat2 &a) { return {a.m00, a.m01, a.m10, a.m11}; }
+__device__ __forceinline__ double ddet(const dmat2 &a) { return a.m00 * a.m11 - a.m10 * a.m01; }
+__device__ __forceinline__ dmat2 dinv(const dmat2 &a) {
+    double inv = 1.0 / ddet(a);
+    return {a.m11 * inv, -a.m10 * inv, -a.m01 * inv, a.m00 * inv};
+}
+
+constexpr float EPS_FOR_SUM = 0.1f;   // global.h:6
+constexpr float LARGE_FLOAT = 1.0E6f; // global.h:7
+constexpr int SCAN_TILE = 1024;       // cells per block in the two-level scans
+constexpr int SCAN_MAX_TILES = 4096;  // => up to 4M cells per scene
+
+inline unsigned grid_for(long n, int block) { return (unsigned)((n + block - 1) / block); }
+
+}  // namespace sphnj

@@ -1,0 +1,366 @@
+// Virtual (wall) and solid passes on sm_103a, reference precision:
+// virtual/fluid FP32, solid state FP64 with FP32 kernel weights
+// (include/particle.cuh:104-115, solid.cu:18-19,271-272).
+//
+//   k_virt_normal      getVirtNormal (virt.cu:8-48): O(N_v^2) wall normals
+//                      in index order (setup only), tiles of positions
+//                      staged in shared memory.
+//   k_virt_data        getVirtData + virtDataCalculate (virt.cu:61-149)
+//   k_solid_couple     solidCoupleUpdate (solid.cu:355-444)
+//   k_solid_deform     solidDeformationCalculate (solid.cu:7-23,169-209)
+//                      with the SVK / auxetic-plastic stress (solid.cu:80-167)
+//   k_solid_force      solidForceCalculate (solid.cu:211-353)
+//   k_solid_update     solidUpdate (solid.cu:446-471)
+#include "kernels.h"
+
+namespace sphnj {
+
+namespace {
+
+constexpr int kBlock = 128;
+
+__device__ __forceinline__ float fdiv(float a, float b) { return __fdividef(a, b); }
+__device__ __forceinline__ float gw(const sphnj_params &p, float q2) {
+    return __expf(-q2) * p.kernel_differential * p.coefficient_3d_to_2d;
+}
+__device__ __forceinline__ float sw(const sphnj_params &p, float q2) {
+    return (__expf(-q2) - p.kernel_coefficient_1) * p.kernel_coefficient_2 * p.coefficient_3d_to_2d;
+}
+__device__ __forceinline__ float by_phase(const float (&a)[2], int ph) { return ph ? a[1] : a[0]; }
+
+__global__ void __launch_bounds__(256) k_virt_normal(sphnj_params p, DevState d) {
+    __shared__ float2 tile[256];
+    const int nv = p.virt_number;
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    const float R2 = p.impact_distance_square, hinv2 = p.smoothing_length_inverse_square;
+    const float2 x_i = i < nv ? d.v_pos[i] : make_float2(0.f, 0.f);
+    float2 nrm = make_float2(0.f, 0.f);
+    for (int base = 0; base < nv; base += 256) {
+        const int idx = base + threadIdx.x;
+        tile[threadIdx.x] = idx < nv ? d.v_pos[idx] : make_float2(0.f, 0.f);
+        __syncthreads();
+        const int cnt = min(256, nv - base);
+        for (int t = 0; t < cnt; ++t) {
+            const float2 dx = sub2(tile[t], x_i);
+            if (sqn(dx) < R2) {
+                const float kc = gw(p, sqn(dx) * hinv2);
+                nrm.x -= dx.x * kc;
+                nrm.y -= dx.y * kc;
+            }
+        }
+        __syncthreads();
+    }
+    if (i < nv) d.v_normal[i] = sqrtf(sqn(nrm)) < EPS_FOR_SUM ? make_float2(0.f, 0.f) : normalized(nrm);
+}
+
+__global__ void __launch_bounds__(kBlock) k_virt_data(sphnj_params p, DevState d) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= p.virt_number) return;
+    const int nx = p.cell_number[0], ny = p.cell_number[1];
+    const float R2 = p.impact_distance_square, hinv2 = p.smoothing_length_inverse_square;
+    const float gx = p.gravity[0], gy = p.gravity[1];
+    const float2 x_i = d.v_pos[i];
+    float2 vel = make_float2(0.f, 0.f);
+    float pr = 0.f, sum = 0.f, nearest = LARGE_FLOAT;
+    int phase = d.v_phase[i];
+    const int c = d.v_cell[i];
+    for (int n = 0; n < 9; ++n) {
+        const int m = neighbour_cell(c, n, nx, ny);
+        if (m < 0) continue;
+        const int2 rf = __ldg(&d.rng_f[m]);
+        for (int t = rf.x; t < rf.x + rf.y; ++t) {
+            const int j = __ldg(&d.lst_f[t]);
+            const float2 dx = sub2(__ldg(&d.f_pos[j]), x_i);
+            const float d2 = sqn(dx);
+            if (!(d2 < R2)) continue;
+            const float kc = sw(p, d2 * hinv2);
+            sum += kc;
+            const float2 vj = __ldg(&d.f_vel[j]);
+            vel.x += vj.x * kc;
+            vel.y += vj.y * kc;
+            pr += (__ldg(&d.f_p[j]) - __ldg(&d.f_rho[j]) * (gx * dx.x + gy * dx.y)) * kc;
+            if (d2 < nearest) {
+                phase = __ldg(&d.f_phase[j]);
+                nearest = d2;
+            }
+        }
+    }
+    float2 v;
+    float pv;
+    if (sum != 0.0f) {
+        v = make_float2(vel.x / sum, vel.y / sum);
+        pv = pr / sum;
+    } else {
+        v = make_float2(0.f, 0.f);
+        pv = 0.f;
+    }
+    const int bt = d.v_bt[i];
+    if (bt == SPHNJ_SLIP) {
+        const float2 nn = d.v_normal[i];
+        const float t = 2.0f * dot2(v, nn);
+        v = make_float2(v.x - t * nn.x, v.y - t * nn.y);
+    } else if (bt == SPHNJ_NO_SLIP) {
+        v = make_float2(-v.x, -v.y);
+    }
+    if (nearest == LARGE_FLOAT) phase = SPHNJ_LIQUID;
+    d.v_vel[i] = v;
+    d.v_p[i] = pv;
+    d.v_phase[i] = (uint8_t)phase;
+    // pressureToDensity, fluid.cu:6-13
+    d.v_rho[i] = by_phase(p.reference_density, phase) *
+                 powf(pv * by_phase(p.coefficient_p2rho, phase) + 1.0f, by_phase(p.gamma_inv, phase));
+}
+
+__global__ void __launch_bounds__(kBlock) k_solid_couple(sphnj_params p, DevState d) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= p.solid_number) return;
+    const int nx = p.cell_number[0], ny = p.cell_number[1];
+    const float R2 = p.impact_distance_square, hinv2 = p.smoothing_length_inverse_square;
+    const float2 x_i = to_f2(d.s_pos[i]);
+    float2 nrm = make_float2(0.f, 0.f);
+    float pr = 0.f, sum = 0.f;
+    const int c = d.s_cell[i];
+    for (int n = 0; n < 9; ++n) {
+        const int m = neighbour_cell(c, n, nx, ny);
+        if (m < 0) continue;
+        const int2 rf = __ldg(&d.rng_f[m]);
+        for (int t = rf.x; t < rf.x + rf.y; ++t) {
+            const int j = __ldg(&d.lst_f[t]);
+            const float2 dx = sub2(__ldg(&d.f_pos[j]), x_i);
+            if (!(sqn(dx) < R2)) continue;
+            const float kc = sw(p, sqn(dx) * hinv2);
+            sum += kc;
+            pr += __ldg(&d.f_p[j]) * kc;
+        }
+        const int2 rs = __ldg(&d.rng_s[m]);
+        for (int t = rs.x; t < rs.x + rs.y; ++t) {
+            const int j = __ldg(&d.lst_s[t]);
+            const float2 dx = sub2(to_f2(d.s_pos[j]), x_i);
+            if (!(sqn(dx) < R2)) continue;
+            const float kc = gw(p, sqn(dx) * hinv2);
+            nrm.x -= dx.x * kc;
+            nrm.y -= dx.y * kc;
+        }
+    }
+    d.s_normal[i] = sqrtf(sqn(nrm)) < EPS_FOR_SUM ? make_float2(0.f, 0.f) : normalized(nrm);
+    d.s_p[i] = sum != 0.0f ? fmaxf(pr / sum, p.min_pressure) : 0.0f;
+}
+
+// ---- stress (solid.cu:80-167) ---------------------------------------------
+__device__ double plastic_elastic(const sphnj_params &p, double strain, double &max_strain) {
+    const float modulus = p.auxetic_modulus, yield_stress = p.yield_stress;
+    const float harden_strain = p.harden_strain, harden_coef = p.harden_coef;
+    const double ts = strain > -0.5 ? sqrt(1.0 + 2.0 * strain) - 1.0 : -1.0;
+    if (ts > max_strain) return modulus * (ts - max_strain) - yield_stress;
+    if (ts > -harden_strain) {
+        if (max_strain > ts && p.plastic_type == SPHNJ_PLASTIC) max_strain = ts;
+        return -yield_stress;
+    }
+    if (max_strain > ts && p.plastic_type == SPHNJ_PLASTIC) max_strain = ts;
+    const double dd = fabs(-harden_strain - ts);
+    return -(harden_coef * (dd * dd) + yield_stress);
+}
+
+__device__ dmat2 green(const dmat2 &F) {
+    const dmat2 ftf = dmul(dtrans(F), F);
+    return {0.5 * (ftf.m00 - 1.0), 0.5 * (ftf.m10 - 0.0), 0.5 * (ftf.m01 - 0.0), 0.5 * (ftf.m11 - 1.0)};
+}
+
+__device__ dmat2 auxetic_stress(const sphnj_params &p, const dmat2 &F, dmat2 &max_strain) {
+    const dmat2 g = green(F);
+    const double mid = 0.5 * (g.m00 + g.m11);
+    const double df = g.m00 - g.m11;
+    const double rad = sqrt(0.25 * (df * df) + g.m01 * g.m10);
+    const double alpha = 0.5 * atan2(g.m01 + g.m10, g.m00 - g.m11);
+    double sa, ca;
+    sincos(alpha, &sa, &ca);
+    const dmat2 rot = {ca, sa, -sa, ca};
+    const dmat2 rinv = dinv(rot);
+    dmat2 msp = dmul(dmul(rinv, max_strain), rot);
+    dmat2 ps = {0.0, 0.0, 0.0, 0.0};
+    ps.m00 = plastic_elastic(p, mid + rad, msp.m00);
+    ps.m11 = plastic_elastic(p, mid - rad, msp.m11);
+    max_strain = dmul(dmul(rot, msp), rinv);
+    return dmul(dmul(dmul(F, rot), ps), rinv);
+}
+
+__device__ dmat2 linear_stress(const sphnj_params &p, const dmat2 &F) {
+    const double lambda = p.lambda, nu = p.nu;
+    const dmat2 g = green(F);
+    const double a = 2.0 * nu, b = lambda * (g.m00 + g.m11);
+    const dmat2 S = {a * g.m00 + b * 1.0, a * g.m10 + b * 0.0, a * g.m01 + b * 0.0, a * g.m11 + b * 1.0};
+    return dmul(F, S);
+}
+
+__device__ __forceinline__ float ref_q2(const sphnj_params &p, double2 dref) {
+    return __double2float_rn((dref.x * dref.x + dref.y * dref.y) * (double)p.smoothing_length_inverse_square);
+}
+__device__ __forceinline__ bool ref_within(const sphnj_params &p, double2 dref) {
+    return __double2float_rn(dref.x * dref.x + dref.y * dref.y) < p.impact_distance_square;
+}
+
+__global__ void __launch_bounds__(kBlock) k_solid_deform(sphnj_params p, DevState d) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= p.solid_number) return;
+    const int nx = p.cell_number[0], ny = p.cell_number[1];
+    dmat2 L = {0, 0, 0, 0}, Ft = {0, 0, 0, 0};
+    const double2 xr_i = d.s_ref[i], x_i = d.s_pos[i];
+    const int c = d.s_cell[i];
+    for (int n = 0; n < 9; ++n) {
+        const int m = neighbour_cell(c, n, nx, ny);
+        if (m < 0) continue;
+        const int2 rs = __ldg(&d.rng_s[m]);
+        for (int t = rs.x; t < rs.x + rs.y; ++t) {
+            const int j = __ldg(&d.lst_s[t]);
+            const double2 xr_j = d.s_ref[j];
+            const double2 dref = make_double2(xr_j.x - xr_i.x, xr_j.y - xr_i.y);
+            if (!ref_within(p, dref)) continue;
+            const double2 x_j = d.s_pos[j];
+            const double2 dx = make_double2(x_j.x - x_i.x, x_j.y - x_i.y);
+            const double kc = (double)gw(p, ref_q2(p, dref));
+            Ft.m00 += dx.x * dref.x * kc;
+            Ft.m10 += dx.y * dref.x * kc;
+            Ft.m01 += dx.x * dref.y * kc;
+            Ft.m11 += dx.y * dref.y * kc;
+            L.m00 += dref.x * dref.x * kc;
+            L.m10 += dref.y * dref.x * kc;
+            L.m01 += dref.x * dref.y * kc;
+            L.m11 += dref.y * dref.y * kc;
+        }
+    }
+    if (ddet(L) != 0.0) L = dinv(L);
+    else L = {1.0, 0.0, 0.0, 1.0};
+    const dmat2 F = dmul(Ft, L);
+    d.s_F[i] = F;
+    dmat2 ms = d.s_maxstrain[i];
+    const int mat = d.s_mat[i];
+    dmat2 P = {0, 0, 0, 0};
+    if (mat == SPHNJ_AUXETIC) {
+        P = auxetic_stress(p, F, ms);
+        d.s_maxstrain[i] = ms;
+    } else if (mat == SPHNJ_LINEAR_ELASTIC) {
+        P = linear_stress(p, F);
+    }
+    d.s_P[i] = P;
+    d.s_L[i] = L;
+}
+
+__global__ void __launch_bounds__(kBlock) k_solid_force(sphnj_params p, DevState d) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= p.solid_number) return;
+    const int nx = p.cell_number[0], ny = p.cell_number[1];
+    const float R2 = p.impact_distance_square, hinv2 = p.smoothing_length_inverse_square;
+    const float alpha = p.artificial_viscosity[0], beta = p.artificial_viscosity[1];
+    const float eps = 0.01f * p.smoothing_length_square;
+    const float cs_s = p.solid_sound_speed, hs = p.smoothing_length;
+    const double2 x_id = d.s_pos[i], v_id = d.s_vel[i], xr_i = d.s_ref[i];
+    const float2 x_i = to_f2(x_id), u_i = to_f2(v_id);
+    const float rho_ref = d.s_mat[i] == SPHNJ_AUXETIC ? p.auxetic_density : p.solid_reference_density;
+    const double rho_ref_d = (double)rho_ref;
+    const dmat2 F_i = d.s_F[i], L_i = d.s_L[i];
+    const dmat2 PL_i = dmul(d.s_P[i], L_i);
+    const float p_i = d.s_p[i];
+    float2 couple = make_float2(0.f, 0.f);
+    double2 acc = make_double2(0.0, 0.0);
+    const int c = d.s_cell[i];
+    for (int n = 0; n < 9; ++n) {
+        const int m = neighbour_cell(c, n, nx, ny);
+        if (m < 0) continue;
+        const int2 rf = __ldg(&d.rng_f[m]);
+        for (int t = rf.x; t < rf.x + rf.y; ++t) {  // solidFluidCouple, solid.cu:211-255
+            const int j = __ldg(&d.lst_f[t]);
+            const float2 dx = sub2(__ldg(&d.f_pos[j]), x_i);
+            if (!(sqn(dx) < R2)) continue;
+            const float kc = gw(p, sqn(dx) * hinv2);
+            const float p_j = __ldg(&d.f_p[j]);
+            const float cs = by_phase(p.sound_speed, __ldg(&d.f_phase[j]));
+            const float rho_j = __ldg(&d.f_rho[j]), rho_i = rho_j;
+            const float2 u_j = __ldg(&d.f_vel[j]);
+            float ps = fdiv(rho_i * p_j + rho_j * p_i, rho_i + rho_j);
+            float2 nn = sqn(dx) > 0.f ? make_float2(fdiv(dx.x, sqrtf(sqn(dx))), fdiv(dx.y, sqrtf(sqn(dx)))) : dx;
+            const float du = dot2(sub2(u_i, u_j), nn);
+            if (du >= 0.0f) ps += fdiv(rho_i * rho_j * du, rho_i + rho_j) * fminf(3.0f * du, cs);
+            const float am = fdiv(-2.0f * ps, rho_ref);
+            couple.x += am * dx.x * kc;
+            couple.y += am * dx.y * kc;
+        }
+        const int2 rs = __ldg(&d.rng_s[m]);
+        for (int t = rs.x; t < rs.x + rs.y; ++t) {  // solidSolidForce, solid.cu:257-305
+            const int j = __ldg(&d.lst_s[t]);
+            const double2 xr_j = d.s_ref[j];
+            const double2 dref = make_double2(xr_j.x - xr_i.x, xr_j.y - xr_i.y);
+            if (!ref_within(p, dref)) continue;
+            const double kc = (double)gw(p, ref_q2(p, dref));
+            const dmat2 PL = dmul(d.s_P[j], d.s_L[j]);
+            const dmat2 M = {PL.m00 + PL_i.m00, PL.m10 + PL_i.m10, PL.m01 + PL_i.m01, PL.m11 + PL_i.m11};
+            const double2 tv = dmv(M, dref);
+            acc.x += tv.x * kc / rho_ref_d;
+            acc.y += tv.y * kc / rho_ref_d;
+            const double2 x_j = d.s_pos[j], v_j = d.s_vel[j];
+            const double2 dx = make_double2(x_j.x - x_id.x, x_j.y - x_id.y);
+            const double2 dv = make_double2(v_j.x - v_id.x, v_j.y - v_id.y);
+            const float dvdx = __double2float_rn(dv.x * dx.x + dv.y * dx.y);
+            const float dis2 = __double2float_rn(dx.x * dx.x + dx.y * dx.y);
+            const float nuv = hs * dvdx / (dis2 + eps);
+            float visc = alpha * nuv * cs_s;
+            visc -= beta * nuv * nuv;
+            const double vd = (double)visc;
+            const dmat2 Fv = {F_i.m00 * vd, F_i.m10 * vd, F_i.m01 * vd, F_i.m11 * vd};
+            const double2 w = dmv(dmul(Fv, L_i), dref);
+            acc.x += w.x * kc;
+            acc.y += w.y * kc;
+        }
+    }
+    d.s_couple[i] = couple;
+    d.s_dudt[i] = make_double2(acc.x + (double)couple.x, acc.y + (double)couple.y);
+}
+
+__global__ void __launch_bounds__(256) k_solid_update(sphnj_params p, DevState d) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= p.solid_number) return;
+    const double dt = (double)(p.dt / (float)p.solid_sub_step);
+    const int bt = d.s_bt[i];
+    double2 x = d.s_pos[i], v = d.s_vel[i];
+    if (bt == SPHNJ_FIXED) {
+        v = make_double2(p.fixed_speed[0], p.fixed_speed[1]);
+        x.x += v.x * dt;
+        x.y += v.y * dt;
+        d.s_dudt[i] = make_double2(0.0, 0.0);
+    } else if (bt == SPHNJ_UNCONSTRAINED) {
+        double2 a = d.s_dudt[i];
+        if (p.transient_type == SPHNJ_STEADY) {
+            a.x += -0.1 * v.x;
+            a.y += -0.1 * v.y;
+            d.s_dudt[i] = a;
+        }
+        x.x += v.x * dt;
+        x.y += v.y * dt;
+        v.x += (a.x + (double)p.gravity[0]) * dt;
+        v.y += (a.y + (double)p.gravity[1]) * dt;
+    }
+    d.s_pos[i] = x;
+    d.s_vel[i] = v;
+}
+
+}  // namespace
+
+void launch_virt_normal(cudaStream_t st, const sphnj_params &p, const DevState &d) {
+    if (p.virt_number > 0) k_virt_normal<<<grid_for(p.virt_number, 256), 256, 0, st>>>(p, d);
+}
+void launch_virt_data(cudaStream_t st, const sphnj_params &p, const DevState &d) {
+    if (p.virt_number > 0) k_virt_data<<<grid_for(p.virt_number, kBlock), kBlock, 0, st>>>(p, d);
+}
+void launch_solid_couple(cudaStream_t st, const sphnj_params &p, const DevState &d) {
+    if (p.solid_number > 0) k_solid_couple<<<grid_for(p.solid_number, kBlock), kBlock, 0, st>>>(p, d);
+}
+void launch_solid_deformation(cudaStream_t st, const sphnj_params &p, const DevState &d) {
+    if (p.solid_number > 0) k_solid_deform<<<grid_for(p.solid_number, kBlock), kBlock, 0, st>>>(p, d);
+}
+void launch_solid_force(cudaStream_t st, const sphnj_params &p, const DevState &d) {
+    if (p.solid_number > 0) k_solid_force<<<grid_for(p.solid_number, kBlock), kBlock, 0, st>>>(p, d);
+}
+void launch_solid_update(cudaStream_t st, const sphnj_params &p, const DevState &d) {
+    if (p.solid_number > 0) k_solid_update<<<grid_for(p.solid_number, 256), 256, 0, st>>>(p, d);
+}
+
+}  // namespace sphnj

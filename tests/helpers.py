@@ -1,0 +1,117 @@
+"""Shared test helpers: case loading, state transfer between implementations,
+and field comparison with stated tolerances."""
+from __future__ import annotations
+
+import tempfile
+from pathlib import Path
+
+import numpy as np
+
+import sphnj_gb300 as S
+from sphnj_gb300 import abi, cases
+
+GOLDEN = Path(__file__).resolve().parent / "golden"
+
+FLUID_FIELDS = ["fluid_position", "fluid_velocity", "fluid_density", "fluid_pressure", "fluid_du_dx",
+                "fluid_gradient", "fluid_du_dt", "fluid_color", "fluid_drho_dt"]
+FLUID_ENUMS = ["fluid_phase", "fluid_boundary_type", "fluid_has_near_particle"]
+SOLID_FIELDS = ["solid_position", "solid_velocity", "solid_pressure", "solid_deformation",
+                "solid_stress_1st_piola", "solid_correction", "solid_du_dt", "solid_normal",
+                "solid_couple_dudt", "solid_max_strain"]
+SOLID_ENUMS = ["solid_boundary_type", "solid_material_type"]
+VIRT_FIELDS = ["virt_normal", "virt_velocity", "virt_pressure", "virt_density"]
+VIRT_ENUMS = ["virt_phase", "virt_boundary_type"]
+CELL_IDS = ["fluid_cell_id", "solid_cell_id", "virt_cell_id"]
+
+
+def load(case: cases.Case):
+    """Writes the case in the reference format and reads it back through the
+    library's host I/O (the drop-in path)."""
+    with tempfile.TemporaryDirectory() as t:
+        case.write(t)
+        return S.load_case(t)
+
+
+def counts_of(p):
+    return {"fluid": p.fluid_number_total, "solid": p.solid_number, "virt": p.virt_number}
+
+
+def nonempty(p, names):
+    c = counts_of(p)
+    return [n for n in names if c[n.split("_")[0]] > 0]
+
+
+def cells_of(sim, p):
+    """[(count, list)] * 3 for set_cells, plus the start arrays."""
+    out = []
+    for k in range(3):
+        start, count, lst = sim.cells(k)
+        out.append((count, lst))
+    return out
+
+
+def transfer(src, dst, p):
+    """Copies the complete state, cell lists and step counter of src into dst."""
+    st = src.download()
+    dst.upload(st)
+    dst.set_cells(*cells_of(src, p))
+    dst.set_step(src.step_index)
+    return st
+
+
+def norm_err(a, b):
+    """max |a - b| / max(max |b|, tiny): the error relative to the field scale."""
+    a = np.asarray(a, np.float64)
+    b = np.asarray(b, np.float64)
+    if a.size == 0:
+        return 0.0
+    scale = max(float(np.max(np.abs(b))), 1e-30)
+    return float(np.max(np.abs(a - b))) / scale
+
+
+def field_errors(a: dict, b: dict, names) -> dict:
+    return {n: norm_err(a[n], b[n]) for n in names}
+
+
+def assert_lists_equal(sim_a, sim_b, p, what=""):
+    for k, kind in enumerate(("fluid", "solid", "virt")):
+        sa, ca, la = sim_a.cells(k)
+        sb, cb, lb = sim_b.cells(k)
+        assert np.array_equal(ca, cb), f"{what}: {kind} per-cell counts differ in {np.sum(ca != cb)} cells"
+        assert np.array_equal(la, lb), f"{what}: {kind} cell lists differ at {np.sum(la != lb)} entries"
+
+
+def golden(name):
+    path = GOLDEN / f"{name}.npz"
+    if not path.exists():
+        return None
+    return np.load(path, allow_pickle=False)
+
+
+def golden_state(g, step, p):
+    """Host-state dict of a reference dump (fields reshaped to the ABI)."""
+    st = {}
+    for name, ptr, dtype, width, kind in abi.STATE_FIELDS:
+        key = f"s{step}/{name}"
+        if key in g.files:
+            a = np.asarray(g[key]).astype(dtype)
+            st[name] = a.reshape(-1, width) if width > 1 else a
+    return st
+
+
+def golden_cells(g, step, p):
+    cnt = np.asarray(g[f"s{step}/cell_counts"]).reshape(-1, 3)
+    return [(cnt[:, 0].copy(), np.asarray(g[f"s{step}/cell_list_fluid"])),
+            (cnt[:, 1].copy(), np.asarray(g[f"s{step}/cell_list_solid"])),
+            (cnt[:, 2].copy(), np.asarray(g[f"s{step}/cell_list_virt"]))]
+
+
+def golden_case(name):
+    """Regenerates the case a fixture was made from (tests/golden/make_fixtures.py)."""
+    import json
+
+    g = golden(name)
+    gen, kw = json.loads(str(g["generator"]))
+    case = cases.by_name(gen, **kw)
+    assert case.ini_text() == str(g["ini"]), f"{name}: generator output changed since the fixture was made"
+    return case, g
