@@ -116,6 +116,7 @@ struct sphnj_ctx {
     int step = 0;
     int parity = 0;
     bool virt_sorted = false;
+    bool virt_cells_valid = false;  // virtual cell ids computed since the last upload
     bool uploaded = false;
     std::string msg = "ok";
 };
@@ -379,6 +380,7 @@ int sphnj_upload(sphnj_ctx *ctx, const sphnj_host_state *s) {
     CK(cudaMemsetAsync(d.max_speed2_bits, 0, sizeof(unsigned), st));
     ctx->parity = 0;
     ctx->virt_sorted = false;
+    ctx->virt_cells_valid = false;
     ctx->step = p.istart;
     bind_lists(ctx);
     // wall normals once before the loop (virtNormalCalculation, calculation.cu:28)
@@ -417,7 +419,11 @@ int sphnj_step(sphnj_ctx *ctx, int n) {
     for (int it = 0; it < n; ++it) {
         ctx->step++;
         const bool is_sort = ((ctx->step - 1) % p.sort_every_step) == 0;  // SimTime::isSort
-        stage(ST_BIN, 1, [&] { launch_bin(st, p, d, !ctx->virt_sorted); });
+        // virtual particles are binned until their first sort (and once after
+        // an upload); afterwards their ids never change
+        const bool bin_virt = !ctx->virt_sorted || !ctx->virt_cells_valid;
+        stage(ST_BIN, 1, [&] { launch_bin(st, p, d, bin_virt); });
+        ctx->virt_cells_valid = true;
         if (is_sort) {
             if (nf > 0)
                 stage(ST_SORT, kSortKernels,

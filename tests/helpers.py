@@ -59,18 +59,33 @@ def transfer(src, dst, p):
     return st
 
 
-def norm_err(a, b):
-    """max |a - b| / max(max |b|, tiny): the error relative to the field scale."""
+def norm_err(a, b, floor=0.0):
+    """max |a - b| / max(max |b|, floor): the error relative to the field
+    scale.  The floor is the field's physical scale, for fields that can be
+    pure rounding noise (a kernel-gradient sum inside a completely filled
+    domain, the stress of an undeformed solid)."""
     a = np.asarray(a, np.float64)
     b = np.asarray(b, np.float64)
     if a.size == 0:
         return 0.0
-    scale = max(float(np.max(np.abs(b))), 1e-30)
+    scale = max(float(np.max(np.abs(b))), floor, 1e-30)
     return float(np.max(np.abs(a - b))) / scale
 
 
-def field_errors(a: dict, b: dict, names) -> dict:
-    return {n: norm_err(a[n], b[n]) for n in names}
+def floors(p) -> dict:
+    """Physical scales of the fields that can vanish: 1/h for the kernel-
+    gradient sum (a free-surface particle has |sum dx W'| ~ colour/h), 1e-6 E
+    for stresses (strain 1e-6), the matching acceleration 1e-6 E/(rho_s h)."""
+    h = float(p.smoothing_length)
+    E = float(p.youngs_modulus)
+    rs = float(p.solid_reference_density)
+    return {"fluid_gradient": 1.0 / h, "solid_stress_1st_piola": 1e-6 * E, "solid_du_dt": 1e-6 * E / (rs * h),
+            "fluid_du_dx": 1e-3 * float(max(p.sound_speed[0], p.sound_speed[1])) / h}
+
+
+def field_errors(a: dict, b: dict, names, p=None) -> dict:
+    fl = floors(p) if p is not None else {}
+    return {n: norm_err(a[n], b[n], fl.get(n, 0.0)) for n in names}
 
 
 def assert_lists_equal(sim_a, sim_b, p, what=""):

@@ -39,7 +39,7 @@ def test_fullsize_first_step_matches_oracle(big):
             assert np.array_equal(sg[n], so[n])
         assert_lists_equal(g, o, p, "4M step 1")
         errs = field_errors(sg, so, ["fluid_position", "fluid_velocity", "fluid_density", "fluid_pressure",
-                                     "fluid_du_dt", "fluid_drho_dt", "fluid_color", "virt_pressure"])
+                                     "fluid_du_dt", "fluid_drho_dt", "fluid_color", "virt_pressure"], p)
         assert all(v < 1e-3 for v in errs.values()), errs
 
 

@@ -48,7 +48,7 @@ def check_step(g, o, p, what, tol_scale=1.0, enum_slack=0.002):
         assert np.array_equal(sg[n], so[n]), f"{what}: {n} differ at {np.sum(sg[n] != so[n])} particles"
     assert_lists_equal(g, o, p, what)
     names = nonempty(p, FLUID_FIELDS + SOLID_FIELDS + VIRT_FIELDS)
-    errs = field_errors(sg, so, names)
+    errs = field_errors(sg, so, names, p)
     bad = {k: v for k, v in errs.items() if v > TOL_STEP[k] * tol_scale}
     assert not bad, f"{what}: field errors above tolerance {bad}"
     enums = nonempty(p, FLUID_ENUMS + SOLID_ENUMS + VIRT_ENUMS)
@@ -120,7 +120,7 @@ def test_free_run_against_oracle(name, steps, tol):
         sg, so = g.download(), o.download()
     names = nonempty(p, ["fluid_position", "fluid_velocity", "fluid_density", "fluid_pressure",
                          "solid_position", "solid_velocity", "solid_deformation"])
-    errs = field_errors(sg, so, names)
+    errs = field_errors(sg, so, names, p)
     bad = {k: v for k, v in errs.items() if v > tol}
     assert not bad, f"{name} after {steps} steps: {bad}"
 
@@ -194,7 +194,7 @@ def _compare_to_golden(g, gz, step, p, what, tol_scale=4.0):
         _, count, got = g.cells(k)
         assert np.array_equal(count, cnt) and np.array_equal(got, lst), f"{what}: lists of kind {k} differ"
     names = nonempty(p, FLUID_FIELDS + SOLID_FIELDS + VIRT_FIELDS)
-    errs = field_errors(sg, ref, names)
+    errs = field_errors(sg, ref, names, p)
     bad = {k: v for k, v in errs.items() if v > TOL_STEP[k] * tol_scale}
     assert not bad, f"{what}: {bad}"
 
