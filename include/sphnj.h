@@ -331,6 +331,39 @@ int  sphnj_profile_read(sphnj_ctx *ctx, double *ms, int64_t *calls, int64_t *ker
 /* Kernels launched by this context since it was created. */
 int  sphnj_stat_launches(const sphnj_ctx *ctx, uint64_t *launches);
 
+/* ---- cell-list rebuild without device allocation --------------------------
+ * This entry point has no counterpart in the reference.  It is for callers
+ * that cannot call cudaMalloc - code running while a host framework owns all
+ * device memory through its own pool allocator, plugin hosts that forbid
+ * allocation after start-up, real-time loops that must not enter the
+ * driver's allocator - and so supply every buffer themselves.
+ *
+ * It performs one incremental cell-list rebuild of one particle kind, the
+ * operation sphnj_step does on each step that is not a sort step
+ * (fillCellList, pair.cu:66-154), with the same kernels and the same result:
+ * from the previous lists and the particles' new cell ids, the new per-cell
+ * lists in the reference's order.
+ *
+ * All pointers are device pointers owned by the caller:
+ *   cell_id     [n_particles]       new cell id of each particle (0..nx*ny-1)
+ *   prev_range  [2*nx*ny]           previous {start, count} per cell (8-byte aligned)
+ *   prev_list   [sum of counts]     previous lists, a valid CSR over 0..n_particles-1
+ *   range_out   [2*nx*ny]           new {start, count} per cell (8-byte aligned)
+ *   list_out    [n_particles]       new lists
+ * stream is a cudaStream_t (NULL = legacy default stream); the call only
+ * enqueues work.  It allocates nothing: its scratch is a static device array
+ * for at most SPHNJ_NOALLOC_MAX_CELLS cells (about 2.6 MB, held by every GPU
+ * that loads the library until the process exits).  nx*ny above that limit
+ * returns SPHNJ_ERR_UNSUPPORTED.  The first call on a device looks up that
+ * array's device address (cudaGetSymbolAddress); make that first call before
+ * any stream capture.  All calls share the one array, so calls that overlap
+ * on the GPU (different streams, or different host threads) race and must
+ * be serialised by the caller. */
+#define SPHNJ_NOALLOC_MAX_CELLS 65536
+int  sphnj_rebuild_cell_lists_noalloc(int nx, int ny, int n_particles, const int32_t *cell_id,
+                                      const int32_t *prev_range, const int32_t *prev_list,
+                                      int32_t *range_out, int32_t *list_out, void *stream);
+
 /* Message of the last error on this context (never NULL). */
 const char *sphnj_last_error(const sphnj_ctx *ctx);
 
