@@ -49,6 +49,8 @@ def parse():
     ap.add_argument("--cpu-steps", type=int, default=3)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--untiled", action="store_true", help="one thread per particle in the neighbour sweeps")
+    ap.add_argument("--tile-h", type=int, default=16, help="cells per tile of the neighbour sweeps")
     return ap.parse_args()
 
 
@@ -182,6 +184,7 @@ def run_ours(args):
     stream = torch.cuda.Stream()
     sim = S.Simulation(p)
     sim.set_stream(stream.cuda_stream)
+    sim.set_tiling(not args.untiled, args.tile_h)
     sim.upload(arr)
 
     def barrier():
@@ -291,7 +294,8 @@ def run_ours(args):
         "vs_baseline": None, "dtype": "f32",
         "data": "synthetic (lattice gas-liquid dam break generated in-process, reference .dat layout)",
         "config": {"workload": f"gas-liquid dam break, 1.0x2.0 m water in a 4.0x3.0 m air-filled tank, dx={args.dx}",
-                   "form": "plain (reference precision and cell-list order)", "n_fluid": nf, "n_liquid": p.fluid_number[0],
+                   "form": "plain (reference precision and cell-list order)",
+                   "sweeps": "per-particle" if args.untiled else f"tiled, {args.tile_h} cells per tile", "n_fluid": nf, "n_liquid": p.fluid_number[0],
                    "n_solid": ns, "n_virt": nv, "cells": p.cell_number_total, "shift_per_step": p.shift_per_step,
                    "sort_every_step": p.sort_every_step, "dt": p.dt,
                    "l2": "inputs larger than L2 (fluid state ~0.3 GB > 129 MB)",

@@ -311,6 +311,13 @@ int  sphnj_debug_set_step(sphnj_ctx *ctx, int step);
  * (getMaxSpeed, fluid.cu:429-440). */
 int  sphnj_debug_max_speed(sphnj_ctx *ctx, float *max_speed);
 
+/* Launch configuration of the fluid neighbour sweeps (pair pass and shifting
+ * gradient): tiled != 0 stages the neighbours of a column segment of tile_h
+ * cells (1..64) in shared memory per block; 0 runs one thread per particle.
+ * Both sum the same terms in the same order, so results are identical; only
+ * the speed differs.  Default: tiled, tile_h = 16. */
+int  sphnj_set_tiling(sphnj_ctx *ctx, int tiled, int tile_h);
+
 /* ---- measurement (the reference has only a host clock() around its loop,
  * calculation.cu:24-46) -------------------------------------------------- */
 

@@ -118,6 +118,9 @@ struct sphnj_ctx {
     bool virt_sorted = false;
     bool virt_cells_valid = false;  // virtual cell ids computed since the last upload
     bool uploaded = false;
+    int *f_listed_total = nullptr;
+    int stamp = 0;  // increases every step (marks the listed fluid particles)
+    TileConfig tiles;
     std::string msg = "ok";
 };
 
@@ -151,6 +154,12 @@ size_t layout(sphnj_ctx *ctx, char *base) {
     d.f_dudx = a.take<float4>(nf);
     d.f_phase = a.take<uint8_t>(nf); d.f_fbt = a.take<uint8_t>(nf); d.f_near = a.take<uint8_t>(nf);
     d.f_cell = a.take<int>(nf);
+    d.f_listed = a.take<int>(nf);
+    ctx->f_listed_total = a.take<int>(1);
+    d.f_listed_total = ctx->f_listed_total;
+    d.f_nbr = a.take<uint4>((size_t)kNbrChunks * nf);
+    d.f_nbr_cnt = a.take<uint8_t>(nf);
+    d.disp2_bits = a.take<unsigned int>(1 + kMaskShifts);
     d.s_pos = a.take<double2>(ns); d.s_ref = a.take<double2>(ns);
     d.s_vel = a.take<double2>(ns); d.s_dudt = a.take<double2>(ns);
     d.s_F = a.take<dmat2>(ns); d.s_P = a.take<dmat2>(ns); d.s_L = a.take<dmat2>(ns);
@@ -376,6 +385,8 @@ int sphnj_upload(sphnj_ctx *ctx, const sphnj_host_state *s) {
         CK(cudaMemsetAsync(ctx->ls[k].rng, 0, sizeof(int2) * C, st));
     }
     CK(cudaMemsetAsync(ctx->lv.rng, 0, sizeof(int2) * C, st));
+    CK(cudaMemsetAsync(d.f_listed, 0xFF, sizeof(int) * (size_t)nf, st));
+    CK(cudaMemsetAsync(ctx->f_listed_total, 0, sizeof(int), st));
     CK(cudaMemsetAsync(d.err, 0, sizeof(DevErr), st));
     CK(cudaMemsetAsync(d.max_speed2_bits, 0, sizeof(unsigned), st));
     ctx->parity = 0;
@@ -416,8 +427,11 @@ int sphnj_step(sphnj_ctx *ctx, int n) {
         }
         ctx->launches += (uint64_t)kernels;
     };
+    const int sweep_kernels = ctx->tiles.tiled ? 2 : 1;  // tiled sweep + fallback for unlisted particles
     for (int it = 0; it < n; ++it) {
         ctx->step++;
+        d.stamp = ++ctx->stamp;
+        const Listing lgf{d.f_listed, ctx->stamp, ctx->f_listed_total};
         const bool is_sort = ((ctx->step - 1) % p.sort_every_step) == 0;  // SimTime::isSort
         // virtual particles are binned until their first sort (and once after
         // an upload); afterwards their ids never change
@@ -427,7 +441,10 @@ int sphnj_step(sphnj_ctx *ctx, int n) {
         if (is_sort) {
             if (nf > 0)
                 stage(ST_SORT, kSortKernels,
-                      [&] { launch_sort_kind(st, p, d, KF, nf, d.f_cell, ctx->sc, ctx->lf[ctx->parity], ctx->payload); });
+                      [&] {
+                          launch_sort_kind(st, p, d, KF, nf, d.f_cell, ctx->sc, ctx->lf[ctx->parity], ctx->payload,
+                                           lgf);
+                      });
             if (ns > 0)
                 stage(ST_SORT, kSortKernels,
                       [&] { launch_sort_kind(st, p, d, KS, ns, d.s_cell, ctx->sc, ctx->ls[ctx->parity], ctx->payload); });
@@ -444,7 +461,9 @@ int sphnj_step(sphnj_ctx *ctx, int n) {
             const int cur = ctx->parity, prev = cur ^ 1;
             if (nf > 0)
                 stage(ST_REBUILD, kRebuildKernels,
-                      [&] { launch_rebuild_kind(st, p, nf, d.f_cell, ctx->lf[prev], ctx->lf[cur], ctx->sc, d.err); });
+                      [&] {
+                          launch_rebuild_kind(st, p, nf, d.f_cell, ctx->lf[prev], ctx->lf[cur], ctx->sc, d.err, lgf);
+                      });
             if (ns > 0)
                 stage(ST_REBUILD, kRebuildKernels,
                       [&] { launch_rebuild_kind(st, p, ns, d.s_cell, ctx->ls[prev], ctx->ls[cur], ctx->sc, d.err); });
@@ -454,7 +473,7 @@ int sphnj_step(sphnj_ctx *ctx, int n) {
         if (nf > 0 && ns > 0) stage(ST_SOLID_COUPLE, 1, [&] { launch_solid_couple(st, p, d); });
         if (nv > 0) stage(ST_VIRT_DATA, 1, [&] { launch_virt_data(st, p, d); });
         if (nf > 0) {
-            stage(ST_FLUID_PAIR, 1, [&] { launch_fluid_pair(st, p, d); });
+            stage(ST_FLUID_PAIR, sweep_kernels, [&] { launch_fluid_pair(st, p, d, ctx->tiles); });
             stage(ST_FLUID_UPDATE, 1, [&] { launch_fluid_update(st, p, d); });
         }
         if (ns > 0)
@@ -465,8 +484,8 @@ int sphnj_step(sphnj_ctx *ctx, int n) {
             }
         if (nf > 0)
             for (int k = 0; k < p.shift_per_step; ++k) {
-                stage(ST_SHIFT_GRADIENT, 1, [&] { launch_shift_gradient(st, p, d); });
-                stage(ST_SHIFT_UPDATE, 1, [&] { launch_shift_update(st, p, d); });
+                stage(ST_SHIFT_GRADIENT, sweep_kernels, [&] { launch_shift_gradient(st, p, d, ctx->tiles, k); });
+                stage(ST_SHIFT_UPDATE, 1, [&] { launch_shift_update(st, p, d, k); });
             }
         CK(cudaGetLastError());
     }
@@ -529,6 +548,13 @@ int sphnj_upload_fields(sphnj_ctx *ctx, uint32_t mask, const sphnj_host_state *s
     }
     CK(cudaGetLastError());
     CK(cudaStreamSynchronize(ctx->st));
+    return SPHNJ_OK;
+}
+
+int sphnj_set_tiling(sphnj_ctx *ctx, int tiled, int tile_h) {
+    if (!ctx || tile_h < 1 || tile_h > 64) return SPHNJ_ERR_ARG;
+    ctx->tiles.tiled = tiled != 0;
+    ctx->tiles.tile_h = tile_h;
     return SPHNJ_OK;
 }
 

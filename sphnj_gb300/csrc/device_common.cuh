@@ -54,6 +54,23 @@ struct DevState {
     // current cell lists (CSR) used by the neighbour sweeps
     const int2 *rng_f, *rng_s, *rng_v;
     const int *lst_f, *lst_s, *lst_v;
+    // which fluid particles the current lists hold (listed[i] == stamp) and
+    // how many
+    int *f_listed;
+    const int *f_listed_total;
+    int stamp;
+    // neighbour lists of this step, indexed by the particle's position h in
+    // the fluid CSR list: the tile slots (uint16) of the fluid entries that
+    // were within the cutoff plus skin when the pair pass ran, in the
+    // reference's order, 128 bytes per particle moved in 16-byte chunks of 8
+    // slots (row h = f_nbr[h * kNbrChunks .. +kNbrChunks)), and their count
+    // (kNbrNone: no list - the stencil holds solid or virtual entries, the
+    // tile was not staged, or the list would exceed kNbrCap)
+    uint4 *f_nbr;
+    uint8_t *f_nbr_cnt;
+    // max |displacement|^2 (float bits) of each position update since the
+    // pair pass: [0] fluid update, [1 + k] shifting pass k
+    unsigned int *disp2_bits;
     // scalars
     unsigned int *max_speed2_bits;  // max over fluid of |v|^2 (float bits)
     DevErr *err;
@@ -97,8 +114,14 @@ __device__ __forceinline__ float shepard_w(const sphnj_params &p, float q2) {
     return (expf(-q2) - p.kernel_coefficient_1) * p.kernel_coefficient_2 * p.coefficient_3d_to_2d;
 }
 
-__device__ __forceinline__ float sqn(float2 a) { return a.x * a.x + a.y * a.y; }
-__device__ __forceinline__ float dot2(float2 a, float2 b) { return a.x * b.x + a.y * b.y; }
+// Sums of two products are written with explicit round-to-nearest
+// intrinsics: left to the compiler, `a*b + c*d` may be contracted into an FMA
+// around either product, and the choice can differ between the kernels a
+// helper is inlined into - which would make the tiled and per-particle sweeps
+// differ in the last bit.
+__device__ __forceinline__ float sum2(float a, float b, float c, float d) { return __fmaf_rn(c, d, __fmul_rn(a, b)); }
+__device__ __forceinline__ float sqn(float2 a) { return sum2(a.x, a.x, a.y, a.y); }
+__device__ __forceinline__ float dot2(float2 a, float2 b) { return sum2(a.x, b.x, a.y, b.y); }
 __device__ __forceinline__ float2 sub2(float2 a, float2 b) { return make_float2(a.x - b.x, a.y - b.y); }
 // Eigen normalized(): zero vector returned unchanged
 __device__ __forceinline__ float2 normalized(float2 a) {
@@ -125,6 +148,11 @@ __device__ __forceinline__ dmat2 dinv(const dmat2 &a) {
     return {a.m11 * inv, -a.m10 * inv, -a.m01 * inv, a.m00 * inv};
 }
 
+constexpr int kMaskShifts = 32;       // shifting passes tracked by disp2_bits
+constexpr float kSkin = 0.05f;        // list radius = cutoff * (1 + kSkin)
+constexpr int kNbrCap = 64;           // neighbour-list entries per particle
+constexpr int kNbrChunks = kNbrCap / 8;  // 16-byte chunks per list
+constexpr uint8_t kNbrNone = 0xFF;
 constexpr float EPS_FOR_SUM = 0.1f;   // global.h:6
 constexpr float LARGE_FLOAT = 1.0E6f; // global.h:7
 constexpr int SCAN_TILE = 1024;       // cells per block in the two-level scans

@@ -41,6 +41,7 @@ __global__ void k_bin(sphnj_params p, DevState d, int with_virt) {
     const int C = p.cell_number_total;
     long t = (long)blockIdx.x * blockDim.x + threadIdx.x;
     if (t == 0) *d.max_speed2_bits = 0u;
+    if (t < 1 + kMaskShifts) d.disp2_bits[t] = 0u;  // grid has >= 256 threads
     int kind, i, c;
     if (t < nf) {
         kind = 0;
@@ -140,8 +141,9 @@ __global__ void __launch_bounds__(kBlock) k_scan_tile(int C, int nx, int ny, con
     if (threadIdx.x == 0) sums[blockIdx.x] = total;
 }
 
-// In-place exclusive scan of the tile sums (<= SCAN_MAX_TILES) by one block.
-__global__ void __launch_bounds__(1024) k_scan_sums(int ntiles, int *sums) {
+// In-place exclusive scan of the tile sums (<= SCAN_MAX_TILES) by one block;
+// the grand total goes to *total when given.
+__global__ void __launch_bounds__(1024) k_scan_sums(int ntiles, int *sums, int *total = nullptr) {
     __shared__ int ws[33];
     const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
     int v[4], tsum = 0;
@@ -174,6 +176,7 @@ __global__ void __launch_bounds__(1024) k_scan_sums(int ntiles, int *sums) {
     for (int k = 0; k < 4; ++k) {
         int t = threadIdx.x * 4 + k;
         if (t < ntiles) sums[t] = ex;
+        if (total && t == ntiles - 1) *total = ex + v[k];
         ex += v[k];
     }
 }
@@ -225,9 +228,11 @@ struct FluidPayload {
     uint8_t *phase, *fbt;
     int *cell;
 };
-__global__ void k_gather_fluid(int n, const int *sorted, DevState d, FluidPayload o, int *lst) {
+__global__ void k_gather_fluid(int n, const int *sorted, DevState d, FluidPayload o, int *lst, int *listed,
+                               int stamp) {
     int k = blockIdx.x * blockDim.x + threadIdx.x;
     if (k >= n) return;
+    if (listed) listed[k] = stamp;
     int s = sorted[k];
     o.pos[k] = d.f_pos[s];
     o.vel[k] = d.f_vel[s];
@@ -337,7 +342,8 @@ __global__ void k_rebuild_count(int C, int nx, int ny, const int2 *prng, const i
 }
 
 __global__ void k_rebuild_write(int C, int nx, int ny, const int2 *prng, const int *plst, const int *cell,
-                                const int *cnt9, const int *local, const int *sums, int2 *crng, int *clst) {
+                                const int *cnt9, const int *local, const int *sums, int2 *crng, int *clst,
+                                int *listed, int stamp) {
     int m = blockIdx.x * blockDim.x + threadIdx.x;
     if (m >= C) return;
     const int mi = m / ny, mj = m - mi * ny;
@@ -365,6 +371,7 @@ __global__ void k_rebuild_write(int C, int nx, int ny, const int2 *prng, const i
         for (int q = 0; q < 9; ++q)
             if (q == s) dst = base[q]++;
         clst[dst] = pidx;
+        if (listed) listed[pidx] = stamp;
     }
 }
 
@@ -389,19 +396,19 @@ void launch_bin(cudaStream_t st, const sphnj_params &p, const DevState &d, bool 
     k_bin<<<grid_for(n > 0 ? n : 1, kBlock), kBlock, 0, st>>>(p, d, with_virt ? 1 : 0);
 }
 
-static void scan_counts(cudaStream_t st, int C, const int *cnt, int *local, int *sums) {
+static void scan_counts(cudaStream_t st, int C, const int *cnt, int *local, int *sums, int *total) {
     int tiles = (C + SCAN_TILE - 1) / SCAN_TILE;
     k_scan_tile<false><<<tiles, kBlock, 0, st>>>(C, 0, 1, cnt, nullptr, nullptr, local, sums);
-    k_scan_sums<<<1, 1024, 0, st>>>(tiles, sums);
+    k_scan_sums<<<1, 1024, 0, st>>>(tiles, sums, total);
 }
 
 void launch_sort_kind(cudaStream_t st, const sphnj_params &p, const DevState &d, Kind k, int n, int *cell,
-                      ListScratch sc, CellList cur, void *payload_scratch) {
+                      ListScratch sc, CellList cur, void *payload_scratch, Listing lg) {
     const int C = p.cell_number_total;
     cudaMemsetAsync(sc.cnt, 0, sizeof(int) * C, st);
     cudaMemsetAsync(sc.cursor, 0, sizeof(int) * C, st);
     if (n > 0) k_hist<<<grid_for(n, kBlock), kBlock, 0, st>>>(n, cell, sc.cnt);
-    scan_counts(st, C, sc.cnt, sc.local, sc.sums);
+    scan_counts(st, C, sc.cnt, sc.local, sc.sums, lg.total);
     if (n > 0) k_bucket<<<grid_for(n, kBlock), kBlock, 0, st>>>(n, cell, sc.local, sc.sums, sc.cursor, sc.bucket);
     k_cellsort<<<grid_for((long)C * 32, kBlock), kBlock, 0, st>>>(C, sc.cnt, sc.local, sc.sums, sc.bucket,
                                                                     sc.sorted, cur.rng);
@@ -413,7 +420,7 @@ void launch_sort_kind(cudaStream_t st, const sphnj_params &p, const DevState &d,
         o.rho = carve<float>(q, n); o.p = carve<float>(q, n);
         o.phase = carve<uint8_t>(q, n); o.fbt = carve<uint8_t>(q, n);
         o.cell = carve<int>(q, n);
-        k_gather_fluid<<<grid_for(n, kBlock), kBlock, 0, st>>>(n, sc.sorted, d, o, cur.lst);
+        k_gather_fluid<<<grid_for(n, kBlock), kBlock, 0, st>>>(n, sc.sorted, d, o, cur.lst, lg.listed, lg.stamp);
         k_scatter_back_fluid<<<grid_for(n, kBlock), kBlock, 0, st>>>(n, d, o);
     } else if (k == KS) {
         SolidPayload o;
@@ -434,16 +441,16 @@ void launch_sort_kind(cudaStream_t st, const sphnj_params &p, const DevState &d,
 }
 
 void launch_rebuild_kind(cudaStream_t st, const sphnj_params &p, int n, const int *cell, CellList prev,
-                         CellList cur, ListScratch sc, DevErr *err) {
+                         CellList cur, ListScratch sc, DevErr *err, Listing lg) {
     (void)n;
     (void)err;
     const int C = p.cell_number_total, nx = p.cell_number[0], ny = p.cell_number[1];
     const int tiles = (C + SCAN_TILE - 1) / SCAN_TILE;
     k_rebuild_count<<<grid_for(C, kBlock), kBlock, 0, st>>>(C, nx, ny, prev.rng, prev.lst, cell, sc.cnt9);
     k_scan_tile<true><<<tiles, kBlock, 0, st>>>(C, nx, ny, nullptr, sc.cnt9, cur.rng, sc.local, sc.sums);
-    k_scan_sums<<<1, 1024, 0, st>>>(tiles, sc.sums);
+    k_scan_sums<<<1, 1024, 0, st>>>(tiles, sc.sums, lg.total);
     k_rebuild_write<<<grid_for(C, kBlock), kBlock, 0, st>>>(C, nx, ny, prev.rng, prev.lst, cell, sc.cnt9, sc.local,
-                                                            sc.sums, cur.rng, cur.lst);
+                                                            sc.sums, cur.rng, cur.lst, lg.listed, lg.stamp);
 }
 
 void launch_capacity_check(cudaStream_t st, const sphnj_params &p, const DevState &d) {

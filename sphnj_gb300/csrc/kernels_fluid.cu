@@ -1,6 +1,6 @@
 // Fluid passes on sm_103a, reference precision (FP32 fluid state).
 //
-//   k_fluid_pair     findFluidPair + fluidFluid/Solid/VirtCalculate
+//   fluid pair       findFluidPair + fluidFluid/Solid/VirtCalculate
 //                    (fluid.cu:25-254): Riemann continuity and momentum,
 //                    velocity gradient, colour, kernel-gradient sum and the
 //                    near-free-surface flag, summed over the 3x3 stencil in
@@ -13,9 +13,20 @@
 //                    multiplies and adds and compared as float bits, which
 //                    equals the reference's host loop over |v| (sqrt is
 //                    monotone), so max_speed is bit-identical.
-//   k_shift_gradient correctionCalculate (fluid.cu:304-367)
+//   shift gradient   correctionCalculate (fluid.cu:304-367)
 //   k_shift_update   shiftDisplacementCalculate + correctionUpdate
 //                    (fluid.cu:369-427)
+//
+// The two neighbour sweeps are tiled: a block owns a column segment of
+// `tile_h` cells and stages the fluid neighbours of that segment - three
+// column strips of tile_h + 2 cells, each a contiguous range of the CSR list
+// - into shared memory once.  Every thread then walks its own particle's 3x3
+// stencil in the reference's order, reading fluid neighbours from shared
+// memory (solid and virtual neighbours, rare, from global memory), so the
+// per-particle sums are the same sums in the same order as the per-particle
+// form.  Particles that are in no cell list (moved more than one cell since
+// the last sort) are handled by per-particle fallback kernels, which return
+// at once when every particle is listed.
 //
 // Math: the neighbour sweeps use __expf and __fdividef, the approximations
 // that the reference's -use_fast_math build uses for expf and '/'
@@ -28,7 +39,9 @@ namespace sphnj {
 namespace {
 
 constexpr int kPairBlock = 128;
+constexpr int kTileBlock = 256;  // tiled sweeps: ~208 particles per 16-cell tile
 constexpr int kBlock = 256;
+constexpr int kFallbackBlocks = 304;  // 2 x 152 SMs, grid-stride
 
 __device__ __forceinline__ float fdiv(float a, float b) { return __fdividef(a, b); }
 __device__ __forceinline__ float gw(const sphnj_params &p, float q2) {
@@ -44,6 +57,41 @@ __device__ __forceinline__ float2 nrm_fast(float2 a) {
 }
 __device__ __forceinline__ float by_phase(const float (&a)[2], int ph) { return ph ? a[1] : a[0]; }
 
+// ---- where fluid neighbours come from ----------------------------------------
+// key(t): handle of the t-th entry of a fluid range; the other members read
+// that neighbour's fields.  Global: through the CSR index list.  Tile: from
+// the block's shared-memory copy.
+struct SrcGlobal {
+    const DevState *d;
+    __device__ __forceinline__ int2 range(int, int2 r) const { return r; }
+    __device__ __forceinline__ int key(int t) const { return __ldg(&d->lst_f[t]); }
+    __device__ __forceinline__ float2 x(int k) const { return __ldg(&d->f_pos[k]); }
+    __device__ __forceinline__ float2 u(int k) const { return __ldg(&d->f_vel[k]); }
+    __device__ __forceinline__ float rho(int k) const { return __ldg(&d->f_rho[k]); }
+    __device__ __forceinline__ float pr(int k) const { return __ldg(&d->f_p[k]); }
+    __device__ __forceinline__ int phase(int k) const { return __ldg(&d->f_phase[k]); }
+    __device__ __forceinline__ int fbt(int k) const { return __ldg(&d->f_fbt[k]); }
+    __device__ __forceinline__ int pid(int k) const { return k; }
+};
+
+struct SrcTile {
+    const float2 *pos, *vel, *rp;  // rp = {rho, p}
+    const uint8_t *flags;          // phase | boundary type << 1
+    const int *idx;                // particle index of each staged entry
+    const int *base, *off;         // per column strip: first CSR position, first slot
+    __device__ __forceinline__ int2 range(int strip, int2 r) const {
+        return make_int2(off[strip] + r.x - base[strip], r.y);
+    }
+    __device__ __forceinline__ int key(int t) const { return t; }
+    __device__ __forceinline__ float2 x(int k) const { return pos[k]; }
+    __device__ __forceinline__ float2 u(int k) const { return vel[k]; }
+    __device__ __forceinline__ float rho(int k) const { return rp[k].x; }
+    __device__ __forceinline__ float pr(int k) const { return rp[k].y; }
+    __device__ __forceinline__ int phase(int k) const { return flags[k] & 1; }
+    __device__ __forceinline__ int fbt(int k) const { return flags[k] >> 1; }
+    __device__ __forceinline__ int pid(int k) const { return idx[k]; }
+};
+
 struct FAcc {
     float velo_div, color;
     float2 du_dt, grad;
@@ -56,11 +104,11 @@ struct FAcc {
 __device__ __forceinline__ void riemann(float2 u_i, float2 u_j, float p_i, float p_j, float rho_i, float rho_j,
                                         float cs, float2 dx, float kc, FAcc &a) {
     const float rs = rho_i + rho_j;
-    float ps = fdiv(rho_i * p_j + rho_j * p_i, rs);
+    float ps = fdiv(sum2(rho_i, p_j, rho_j, p_i), rs);
     float2 n = nrm_fast(dx);
     float du = dot2(sub2(u_i, u_j), n);
     if (du >= 0.0f) ps += fdiv(rho_i * rho_j * du, rs) * fminf(3.0f * du, cs);
-    float2 vs = make_float2(fdiv(rho_i * u_i.x + rho_j * u_j.x, rs), fdiv(rho_i * u_i.y + rho_j * u_j.y, rs));
+    float2 vs = make_float2(fdiv(sum2(rho_i, u_i.x, rho_j, u_j.x), rs), fdiv(sum2(rho_i, u_i.y, rho_j, u_j.y), rs));
     float t = fdiv(fdiv(p_i - p_j, rs), cs);
     vs.x += t * n.x;
     vs.y += t * n.y;
@@ -84,52 +132,91 @@ __device__ __forceinline__ void viscous(const sphnj_params &p, float2 u_i, float
     a.du_dt.y += am * dx.y * kc;
 }
 
-__global__ void __launch_bounds__(kPairBlock) k_fluid_pair(sphnj_params p, DevState d) {
-    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+// State of particle i that every pair term reads.
+struct PairI {
+    int i, ph;
+    float2 x, u;
+    float p, rho, cs;
+};
+
+__device__ __forceinline__ PairI load_pair_i(const sphnj_params &p, const DevState &d, int i) {
+    PairI s;
+    s.i = i;
+    s.x = d.f_pos[i];
+    s.u = d.f_vel[i];
+    s.p = d.f_p[i];
+    s.rho = d.f_rho[i];
+    s.ph = d.f_phase[i];
+    s.cs = by_phase(p.sound_speed, s.ph);
+    return s;
+}
+
+__device__ __forceinline__ void zero(FAcc &a) {
+    a.velo_div = 0.f;
+    a.color = 0.f;
+    a.du_dt = make_float2(0.f, 0.f);
+    a.grad = make_float2(0.f, 0.f);
+    a.du_dx = make_float4(0.f, 0.f, 0.f, 0.f);
+    a.near = SPHNJ_NO_PARTICLE;
+}
+
+// fluidFluidCalculate (fluid.cu:25-80) for a neighbour inside the cutoff
+template <class Src>
+__device__ __forceinline__ void fluid_term(const sphnj_params &p, const Src &src, int k, const PairI &s, float2 dx,
+                                           FAcc &a) {
+    const float R2 = p.impact_distance_square;
+    const float kc = gw(p, sqn(dx) * p.smoothing_length_inverse_square);
+    const float2 u_j = src.u(k);
+    riemann(s.u, u_j, s.p, src.pr(k), s.rho, src.rho(k), s.cs, dx, kc, a);
+    const int ph_j = src.phase(k);
+    if (!(s.ph == SPHNJ_LIQUID && ph_j == SPHNJ_GAS)) {
+        a.color += dot2(dx, dx) * kc;
+        a.grad.x += dx.x * kc;
+        a.grad.y += dx.y * kc;
+    }
+    if (src.fbt(k) == SPHNJ_FREE_SURFACE && s.ph == SPHNJ_LIQUID && s.i != src.pid(k)) {
+        if (sqn(dx) < 0.25f * R2) a.near = SPHNJ_HAS_NEAR_PARTICLE;
+        else if (a.near == SPHNJ_NO_PARTICLE) a.near = SPHNJ_HAS_PARTICLE;
+    }
+    if (p.is_fluid_viscid) viscous(p, s.u, u_j, s.rho, s.ph, dx, kc, a);
+}
+
+__device__ __forceinline__ void store_pair(const DevState &d, int i, const FAcc &a) {
+    d.f_drho[i] = a.velo_div;
+    d.f_dudt[i] = a.du_dt;
+    d.f_near[i] = (uint8_t)a.near;
+    d.f_color[i] = a.color;
+    d.f_grad[i] = a.grad;
+    d.f_dudx[i] = a.du_dx;
+}
+
+// findFluidPair for particle i (fluid.cu:193-254)
+template <class Src>
+__device__ __forceinline__ void pair_particle(const sphnj_params &p, const DevState &d, const Src &src, int i) {
     const int nf = p.fluid_number_total;
-    if (i >= nf) return;
     const int nx = p.cell_number[0], ny = p.cell_number[1];
     const float R2 = p.impact_distance_square, hinv2 = p.smoothing_length_inverse_square;
     const bool viscid = p.is_fluid_viscid != 0;
-    const float2 x_i = d.f_pos[i], u_i = d.f_vel[i];
-    const float p_i = d.f_p[i], rho_i = d.f_rho[i];
-    const int ph_i = d.f_phase[i];
-    const float cs = by_phase(p.sound_speed, ph_i);
+    const PairI si = load_pair_i(p, d, i);
+    const float2 x_i = si.x, u_i = si.u;
+    const float p_i = si.p, rho_i = si.rho, cs = si.cs;
+    const int ph_i = si.ph;
     const int c = d.f_cell[i];
     FAcc a;
-    a.velo_div = 0.f; a.color = 0.f;
-    a.du_dt = make_float2(0.f, 0.f); a.grad = make_float2(0.f, 0.f);
-    a.du_dx = make_float4(0.f, 0.f, 0.f, 0.f);
-    a.near = SPHNJ_NO_PARTICLE;
+    zero(a);
     for (int n = 0; n < 9; ++n) {
         const int m = neighbour_cell(c, n, nx, ny);
         if (m < 0) continue;
-        const int2 rf = __ldg(&d.rng_f[m]);
+        const int2 rf = src.range(n / 3, __ldg(&d.rng_f[m]));
         for (int t = rf.x; t < rf.x + rf.y; ++t) {
-            const int j = __ldg(&d.lst_f[t]);
-            const float2 x_j = __ldg(&d.f_pos[j]);
-            const float2 dx = sub2(x_j, x_i);
-            if (!(sqn(dx) < R2)) continue;
-            const float kc = gw(p, sqn(dx) * hinv2);
-            const float2 u_j = __ldg(&d.f_vel[j]);
-            riemann(u_i, u_j, p_i, __ldg(&d.f_p[j]), rho_i, __ldg(&d.f_rho[j]), cs, dx, kc, a);
-            const int ph_j = __ldg(&d.f_phase[j]);
-            if (!(ph_i == SPHNJ_LIQUID && ph_j == SPHNJ_GAS)) {
-                a.color += dot2(dx, dx) * kc;
-                a.grad.x += dx.x * kc;
-                a.grad.y += dx.y * kc;
-            }
-            if (__ldg(&d.f_fbt[j]) == SPHNJ_FREE_SURFACE && ph_i == SPHNJ_LIQUID && i != j) {
-                if (sqn(dx) < 0.25f * R2) a.near = SPHNJ_HAS_NEAR_PARTICLE;
-                else if (a.near == SPHNJ_NO_PARTICLE) a.near = SPHNJ_HAS_PARTICLE;
-            }
-            if (viscid) viscous(p, u_i, u_j, rho_i, ph_i, dx, kc, a);
+            const int k = src.key(t);
+            const float2 dx = sub2(src.x(k), x_i);
+            if (sqn(dx) < R2) fluid_term(p, src, k, si, dx, a);
         }
         const int2 rs = __ldg(&d.rng_s[m]);
         for (int t = rs.x; t < rs.x + rs.y; ++t) {
             const int j = __ldg(&d.lst_s[t]);
-            const float2 x_j = to_f2(d.s_pos[j]);
-            const float2 dx = sub2(x_j, x_i);
+            const float2 dx = sub2(to_f2(d.s_pos[j]), x_i);
             if (!(sqn(dx) < R2)) continue;
             const float kc = gw(p, sqn(dx) * hinv2);
             const float2 u_j = to_f2(d.s_vel[j]);
@@ -141,8 +228,7 @@ __global__ void __launch_bounds__(kPairBlock) k_fluid_pair(sphnj_params p, DevSt
         const int2 rv = __ldg(&d.rng_v[m]);
         for (int t = rv.x; t < rv.x + rv.y; ++t) {
             const int j = __ldg(&d.lst_v[t]);
-            const float2 x_j = __ldg(&d.v_pos[j]);
-            const float2 dx = sub2(x_j, x_i);
+            const float2 dx = sub2(__ldg(&d.v_pos[j]), x_i);
             if (!(sqn(dx) < R2)) continue;
             const float kc = gw(p, sqn(dx) * hinv2);
             const float rho_j = by_phase(p.reference_density, __ldg(&d.v_phase[j]));
@@ -159,65 +245,12 @@ __global__ void __launch_bounds__(kPairBlock) k_fluid_pair(sphnj_params p, DevSt
             if (viscid) viscous(p, u_i, u_j, rho_i, ph_i, dx, kc, a);
         }
     }
-    d.f_drho[i] = a.velo_div;
-    d.f_dudt[i] = a.du_dt;
-    d.f_near[i] = (uint8_t)a.near;
-    d.f_color[i] = a.color;
-    d.f_grad[i] = a.grad;
-    d.f_dudx[i] = a.du_dx;
+    store_pair(d, i, a);
 }
 
-// densityToPressure, fluid.cu:15-23
-__device__ __forceinline__ float density_to_pressure(const sphnj_params &p, float rho, int ph) {
-    float pr = (powf(rho * by_phase(p.reference_density_inverse, ph), by_phase(p.gamma, ph)) - 1.0f) *
-               by_phase(p.coefficient_rho2p, ph);
-    return fmaxf(pr, p.min_pressure);
-}
-
-__global__ void __launch_bounds__(kBlock) k_fluid_update(sphnj_params p, DevState d) {
-    const int i = blockIdx.x * blockDim.x + threadIdx.x;
-    unsigned int sp2 = 0u;
-    if (i < p.fluid_number_total) {
-        const int ph = d.f_phase[i];
-        const float dt = p.dt;
-        float2 x = d.f_pos[i], v = d.f_vel[i], a = d.f_dudt[i];
-        if (p.transient_type == SPHNJ_STEADY) {
-            a.x += -0.1f * v.x;
-            a.y += -0.1f * v.y;
-            d.f_dudt[i] = a;
-        }
-        x.x += v.x * dt;
-        x.y += v.y * dt;
-        v.x += (a.x + p.gravity[0]) * dt;
-        v.y += (a.y + p.gravity[1]) * dt;
-        float rho = d.f_rho[i] + d.f_drho[i] * dt;
-        rho = fmaxf(rho, by_phase(p.min_density, ph));
-        d.f_rho[i] = rho;
-        d.f_p[i] = density_to_pressure(p, rho, ph);
-        x.x = fminf(fmaxf(x.x, p.domain_xmin[0]), p.domain_xmax[0]);
-        x.y = fminf(fmaxf(x.y, p.domain_xmin[1]), p.domain_xmax[1]);
-        d.f_pos[i] = x;
-        d.f_vel[i] = v;
-        float s2 = __fadd_rn(__fmul_rn(v.x, v.x), __fmul_rn(v.y, v.y));
-        if (s2 == s2) sp2 = __float_as_uint(s2);  // NaN never wins, as on the host
-    }
-    // block max of non-negative float bits, one atomic per block
-#pragma unroll
-    for (int o = 16; o > 0; o >>= 1) sp2 = max(sp2, __shfl_xor_sync(0xffffffffu, sp2, o));
-    __shared__ unsigned int wmax[kBlock / 32];
-    if ((threadIdx.x & 31) == 0) wmax[threadIdx.x >> 5] = sp2;
-    __syncthreads();
-    if (threadIdx.x < 32) {
-        unsigned int v = threadIdx.x < kBlock / 32 ? wmax[threadIdx.x] : 0u;
-#pragma unroll
-        for (int o = 16; o > 0; o >>= 1) v = max(v, __shfl_xor_sync(0xffffffffu, v, o));
-        if (threadIdx.x == 0 && v) atomicMax(d.max_speed2_bits, v);
-    }
-}
-
-__global__ void __launch_bounds__(kPairBlock) k_shift_gradient(sphnj_params p, DevState d) {
-    const int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= p.fluid_number_total) return;
+// correctionCalculate for particle i (fluid.cu:316-367)
+template <class Src>
+__device__ __forceinline__ void shift_particle(const sphnj_params &p, const DevState &d, const Src &src, int i) {
     const int nx = p.cell_number[0], ny = p.cell_number[1];
     const float R2 = p.impact_distance_square, hinv2 = p.smoothing_length_inverse_square;
     const float2 x_i = d.f_pos[i];
@@ -226,9 +259,9 @@ __global__ void __launch_bounds__(kPairBlock) k_shift_gradient(sphnj_params p, D
     for (int n = 0; n < 9; ++n) {
         const int m = neighbour_cell(c, n, nx, ny);
         if (m < 0) continue;
-        const int2 rf = __ldg(&d.rng_f[m]);
+        const int2 rf = src.range(n / 3, __ldg(&d.rng_f[m]));
         for (int t = rf.x; t < rf.x + rf.y; ++t) {
-            const float2 dx = sub2(__ldg(&d.f_pos[__ldg(&d.lst_f[t])]), x_i);
+            const float2 dx = sub2(src.x(src.key(t)), x_i);
             if (sqn(dx) < R2) {
                 const float kc = gw(p, sqn(dx) * hinv2);
                 g.x += dx.x * kc;
@@ -257,6 +290,353 @@ __global__ void __launch_bounds__(kPairBlock) k_shift_gradient(sphnj_params p, D
     d.f_grad[i] = g;
 }
 
+// ---- neighbour lists ----------------------------------------------------------
+// When the 3x3 stencil of cell c holds only fluid entries, the stencil's
+// candidates in the reference's order (slots 0..8, fluid/solid/virtual per
+// cell) are exactly three contiguous CSR ranges, one per column (rows
+// cj-1..cj+1 of a column are consecutive cell ids).  The pair pass records
+// the tile slots of the candidates within cutoff * (1 + kSkin), in that
+// order; the pair terms and the shifting passes of the same step visit only
+// those entries - in the same order, with the exact cutoff test - while the
+// positions have moved by less than half the skin.  The tile staging is the
+// same in every pass of a step (same lists, same tile height), so the slots
+// stay valid.
+struct Strips {
+    int base[3], len[3];
+};
+
+__device__ __forceinline__ Strips strips_of(const sphnj_params &p, const DevState &d, int c, bool &only_fluid) {
+    const int nx = p.cell_number[0], ny = p.cell_number[1];
+    const int ci = c / ny, cj = c - ci * ny;
+    const int r0 = max(cj - 1, 0), r1 = min(cj + 1, ny - 1);
+    Strips S;
+    only_fluid = true;
+#pragma unroll
+    for (int s = 0; s < 3; ++s) {
+        const int col = ci + s - 1;
+        S.base[s] = 0;
+        S.len[s] = 0;
+        if (col < 0 || col >= nx) continue;
+        const int2 a = __ldg(&d.rng_f[col * ny + r0]), b = __ldg(&d.rng_f[col * ny + r1]);
+        S.base[s] = a.x;
+        S.len[s] = b.x + b.y - a.x;
+        if (S.len[s] > 64) only_fluid = false;
+        for (int r = r0; r <= r1; ++r) {
+            const int m = col * ny + r;
+            if (__ldg(&d.rng_s[m]).y | __ldg(&d.rng_v[m]).y) only_fluid = false;
+        }
+    }
+    return S;
+}
+
+__device__ __forceinline__ float list_radius2(const sphnj_params &p) {
+    return p.impact_distance_square * ((1.0f + kSkin) * (1.0f + kSkin));
+}
+
+// Pair pass for particle i at CSR position h; records its neighbour list
+// when `listable` (its tile was staged, so the source is the tile).
+template <class Src>
+__device__ __forceinline__ void pair_particle_listed(const sphnj_params &p, const DevState &d, const Src &src, int i,
+                                                     int h, bool listable) {
+    const int nf = p.fluid_number_total;
+    bool ok = false;
+    Strips S;
+    if (listable) S = strips_of(p, d, d.f_cell[i], ok);
+    if (!ok) {
+        d.f_nbr_cnt[h] = kNbrNone;
+        pair_particle(p, d, src, i);
+        return;
+    }
+    (void)nf;
+    const float R2 = p.impact_distance_square, Rs2 = list_radius2(p);
+    const PairI si = load_pair_i(p, d, i);
+    uint4 *row = d.f_nbr + (size_t)h * kNbrChunks;
+    // 8-slot FIFO in four registers: each push shifts the 128-bit value down
+    // by 16 bits and inserts at the top, so after 8 pushes the first slot is
+    // in the low half of b0; full chunks go out as one 16-byte store.
+    unsigned b0 = 0u, b1 = 0u, b2 = 0u, b3 = 0u;
+    int n = 0;
+#pragma unroll
+    for (int s = 0; s < 3; ++s) {
+        const int2 rr = src.range(s, make_int2(S.base[s], S.len[s]));
+        for (int t = rr.x; t < rr.x + rr.y; ++t)
+            if (sqn(sub2(src.x(src.key(t)), si.x)) < Rs2) {
+                if (n < kNbrCap) {
+                    b0 = __funnelshift_r(b0, b1, 16);
+                    b1 = __funnelshift_r(b1, b2, 16);
+                    b2 = __funnelshift_r(b2, b3, 16);
+                    b3 = __funnelshift_r(b3, (unsigned)t, 16);
+                    if ((n & 7) == 7) row[n >> 3] = make_uint4(b0, b1, b2, b3);
+                }
+                ++n;
+            }
+    }
+    if (n > kNbrCap) {
+        d.f_nbr_cnt[h] = kNbrNone;
+        pair_particle(p, d, src, i);
+        return;
+    }
+    if (n & 7) {  // last, partial chunk: move its slots to the low end
+        for (int e = n & 7; e < 8; ++e) {
+            b0 = __funnelshift_r(b0, b1, 16);
+            b1 = __funnelshift_r(b1, b2, 16);
+            b2 = __funnelshift_r(b2, b3, 16);
+            b3 = b3 >> 16;
+        }
+        row[n >> 3] = make_uint4(b0, b1, b2, b3);
+    }
+    d.f_nbr_cnt[h] = (uint8_t)n;
+    FAcc a;
+    zero(a);
+    for (int c = 0; c < n; c += 8) {
+        const uint4 v = row[c >> 3];
+        const unsigned w[4] = {v.x, v.y, v.z, v.w};
+#pragma unroll
+        for (int e = 0; e < 8; ++e) {
+            if (c + e < n) {
+                const int k = src.key((int)((w[e >> 1] >> (16 * (e & 1))) & 0xFFFFu));
+                const float2 dx = sub2(src.x(k), si.x);
+                if (sqn(dx) < R2) fluid_term(p, src, k, si, dx, a);
+            }
+        }
+    }
+    store_pair(d, i, a);
+}
+
+// Shifting gradient of particle i at CSR position h through its neighbour
+// list when use_list (and it has one).
+template <class Src>
+__device__ __forceinline__ void shift_particle_listed(const sphnj_params &p, const DevState &d, const Src &src, int i,
+                                                      int h, bool use_list) {
+    const int n = use_list ? (int)d.f_nbr_cnt[h] : (int)kNbrNone;
+    if (n == kNbrNone) {
+        shift_particle(p, d, src, i);
+        return;
+    }
+    const float R2 = p.impact_distance_square, hinv2 = p.smoothing_length_inverse_square;
+    const float2 x_i = d.f_pos[i];
+    const uint4 *row = d.f_nbr + (size_t)h * kNbrChunks;
+    float2 g = make_float2(0.f, 0.f);
+    for (int c = 0; c < n; c += 8) {
+        const uint4 v = __ldg(&row[c >> 3]);
+        const unsigned w[4] = {v.x, v.y, v.z, v.w};
+        float2 x_j[8];
+#pragma unroll
+        for (int e = 0; e < 8; ++e)  // all eight loads in flight first
+            x_j[e] = src.x(src.key((int)((w[e >> 1] >> (16 * (e & 1))) & 0xFFFFu)));
+#pragma unroll
+        for (int e = 0; e < 8; ++e) {
+            if (c + e < n) {
+                const float2 dx = sub2(x_j[e], x_i);
+                if (sqn(dx) < R2) {
+                    const float kc = gw(p, sqn(dx) * hinv2);
+                    g.x += dx.x * kc;
+                    g.y += dx.y * kc;
+                }
+            }
+        }
+    }
+    d.f_grad[i] = g;
+}
+
+// The lists of this step still hold every pair within the cutoff when twice
+// the summed per-update maximum displacement since the pair pass is inside
+// the skin (margin 0.9 for rounding).  `pass` shifting updates came before.
+__device__ __forceinline__ bool lists_valid(const sphnj_params &p, const DevState &d, int pass) {
+    if (pass >= kMaskShifts) return false;
+    float moved = 0.0f;
+    for (int k = 0; k <= pass; ++k) moved += sqrtf(__uint_as_float(d.disp2_bits[k]));
+    return 2.0f * moved < 0.9f * kSkin * sqrtf(p.impact_distance_square);
+}
+
+// Block-wide max of non-negative float bits, one atomicMax per block.
+template <int kThreads>
+__device__ __forceinline__ void block_max_to(unsigned int v, unsigned int *dst) {
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v = max(v, __shfl_xor_sync(0xffffffffu, v, o));
+    __shared__ unsigned int wmax[kThreads / 32];
+    if ((threadIdx.x & 31) == 0) wmax[threadIdx.x >> 5] = v;
+    __syncthreads();
+    if (threadIdx.x < 32) {
+        unsigned int w = threadIdx.x < kThreads / 32 ? wmax[threadIdx.x] : 0u;
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) w = max(w, __shfl_xor_sync(0xffffffffu, w, o));
+        if (threadIdx.x == 0 && w) atomicMax(dst, w);
+    }
+}
+
+__device__ __forceinline__ unsigned int disp2(float2 a, float2 b) {
+    const float dx = b.x - a.x, dy = b.y - a.y;
+    const float v = dx * dx + dy * dy;
+    return v == v ? __float_as_uint(v) : 0x7f800000u;  // NaN: treat as unbounded
+}
+
+// ---- tiles ---------------------------------------------------------------
+// Block b owns home cells (ci, cj0 .. cj1-1) of one column.  Its fluid
+// neighbours are the cells (ci-1..ci+1, cj0-1..cj1): per column one
+// contiguous CSR range ("strip").  Returns false (uniformly) when the block
+// has no home particle.
+struct TileGeom {
+    int home_b, home_e, total;
+};
+
+__device__ __forceinline__ bool tile_setup(const sphnj_params &p, const DevState &d, int tile_h, int *s_base,
+                                           int *s_off, TileGeom &g) {
+    const int nx = p.cell_number[0], ny = p.cell_number[1];
+    const int tiles_y = (ny + tile_h - 1) / tile_h;
+    const int ci = blockIdx.x / tiles_y, cj0 = (blockIdx.x - ci * tiles_y) * tile_h;
+    const int cj1 = min(cj0 + tile_h, ny);
+    const int2 h0 = __ldg(&d.rng_f[ci * ny + cj0]), h1 = __ldg(&d.rng_f[ci * ny + cj1 - 1]);
+    g.home_b = h0.x;
+    g.home_e = h1.x + h1.y;
+    if (g.home_e <= g.home_b) return false;
+    __shared__ int s_len[3];
+    if (threadIdx.x < 3) {
+        const int col = ci + (int)threadIdx.x - 1;
+        int base = 0, len = 0;
+        if (col >= 0 && col < nx) {
+            const int r0 = max(cj0 - 1, 0), r1 = min(cj1, ny - 1);
+            const int2 a = __ldg(&d.rng_f[col * ny + r0]), b = __ldg(&d.rng_f[col * ny + r1]);
+            base = a.x;
+            len = b.x + b.y - a.x;
+        }
+        s_base[threadIdx.x] = base;
+        s_len[threadIdx.x] = len;
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        s_off[0] = 0;
+        s_off[1] = s_len[0];
+        s_off[2] = s_len[0] + s_len[1];
+    }
+    g.total = s_len[0] + s_len[1] + s_len[2];
+    __syncthreads();
+    return true;
+}
+
+__device__ __forceinline__ int tile_strip(const int *s_off, int k) { return k < s_off[1] ? 0 : (k < s_off[2] ? 1 : 2); }
+
+__global__ void __launch_bounds__(kTileBlock) k_fluid_pair_tiled(sphnj_params p, DevState d, int tile_h, int cap) {
+    extern __shared__ __align__(16) unsigned char smem[];
+    __shared__ int s_base[3], s_off[3];
+    TileGeom g;
+    if (!tile_setup(p, d, tile_h, s_base, s_off, g)) return;
+    float2 *s_pos = reinterpret_cast<float2 *>(smem);
+    float2 *s_vel = s_pos + cap;
+    float2 *s_rp = s_vel + cap;
+    int *s_idx = reinterpret_cast<int *>(s_rp + cap);
+    uint8_t *s_fl = reinterpret_cast<uint8_t *>(s_idx + cap);
+    const bool staged = g.total <= cap;
+    if (staged) {
+        for (int k = threadIdx.x; k < g.total; k += blockDim.x) {
+            const int s = tile_strip(s_off, k);
+            const int j = __ldg(&d.lst_f[s_base[s] + k - s_off[s]]);
+            s_pos[k] = __ldg(&d.f_pos[j]);
+            s_vel[k] = __ldg(&d.f_vel[j]);
+            s_rp[k] = make_float2(__ldg(&d.f_rho[j]), __ldg(&d.f_p[j]));
+            s_idx[k] = j;
+            s_fl[k] = (uint8_t)(__ldg(&d.f_phase[j]) | (__ldg(&d.f_fbt[j]) << 1));
+        }
+    }
+    __syncthreads();
+    if (staged) {
+        const SrcTile src{s_pos, s_vel, s_rp, s_fl, s_idx, s_base, s_off};
+        for (int h = g.home_b + threadIdx.x; h < g.home_e; h += blockDim.x)
+            pair_particle_listed(p, d, src, d.lst_f[h], h, true);
+    } else {
+        const SrcGlobal src{&d};
+        for (int h = g.home_b + threadIdx.x; h < g.home_e; h += blockDim.x)
+            pair_particle_listed(p, d, src, d.lst_f[h], h, false);
+    }
+}
+
+__global__ void __launch_bounds__(kTileBlock) k_shift_gradient_tiled(sphnj_params p, DevState d, int tile_h,
+                                                                     int cap, int pass) {
+    extern __shared__ __align__(16) unsigned char smem[];
+    __shared__ int s_base[3], s_off[3];
+    TileGeom g;
+    if (!tile_setup(p, d, tile_h, s_base, s_off, g)) return;
+    float2 *s_pos = reinterpret_cast<float2 *>(smem);
+    const bool staged = g.total <= cap;
+    if (staged) {
+        for (int k = threadIdx.x; k < g.total; k += blockDim.x) {
+            const int s = tile_strip(s_off, k);
+            s_pos[k] = __ldg(&d.f_pos[__ldg(&d.lst_f[s_base[s] + k - s_off[s]])]);
+        }
+    }
+    __syncthreads();
+    const bool use_list = lists_valid(p, d, pass);
+    if (staged) {
+        const SrcTile src{s_pos, nullptr, nullptr, nullptr, nullptr, s_base, s_off};
+        for (int h = g.home_b + threadIdx.x; h < g.home_e; h += blockDim.x)
+            shift_particle_listed(p, d, src, d.lst_f[h], h, use_list);
+    } else {
+        // a tile the pair pass could not stage has no lists either
+        const SrcGlobal src{&d};
+        for (int h = g.home_b + threadIdx.x; h < g.home_e; h += blockDim.x)
+            shift_particle_listed(p, d, src, d.lst_f[h], h, false);
+    }
+}
+
+// Per-particle forms: every particle (listed == null), or only the particles
+// that are in no cell list.
+__global__ void __launch_bounds__(kPairBlock) k_fluid_pair_each(sphnj_params p, DevState d, int only_unlisted) {
+    const int nf = p.fluid_number_total;
+    if (only_unlisted && *d.f_listed_total == nf) return;
+    const SrcGlobal src{&d};
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < nf; i += gridDim.x * blockDim.x)
+        if (!only_unlisted || d.f_listed[i] != d.stamp) pair_particle(p, d, src, i);
+}
+
+__global__ void __launch_bounds__(kPairBlock) k_shift_gradient_each(sphnj_params p, DevState d, int only_unlisted) {
+    const int nf = p.fluid_number_total;
+    if (only_unlisted && *d.f_listed_total == nf) return;
+    const SrcGlobal src{&d};
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < nf; i += gridDim.x * blockDim.x)
+        if (!only_unlisted || d.f_listed[i] != d.stamp) shift_particle(p, d, src, i);
+}
+
+// densityToPressure, fluid.cu:15-23
+__device__ __forceinline__ float density_to_pressure(const sphnj_params &p, float rho, int ph) {
+    float pr = (powf(rho * by_phase(p.reference_density_inverse, ph), by_phase(p.gamma, ph)) - 1.0f) *
+               by_phase(p.coefficient_rho2p, ph);
+    return fmaxf(pr, p.min_pressure);
+}
+
+__global__ void __launch_bounds__(kBlock) k_fluid_update(sphnj_params p, DevState d) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    unsigned int sp2 = 0u, moved2 = 0u;
+    if (i < p.fluid_number_total) {
+        const int ph = d.f_phase[i];
+        const float dt = p.dt;
+        float2 x = d.f_pos[i], v = d.f_vel[i], a = d.f_dudt[i];
+        const float2 x0 = x;
+        if (p.transient_type == SPHNJ_STEADY) {
+            a.x += -0.1f * v.x;
+            a.y += -0.1f * v.y;
+            d.f_dudt[i] = a;
+        }
+        x.x += v.x * dt;
+        x.y += v.y * dt;
+        v.x += (a.x + p.gravity[0]) * dt;
+        v.y += (a.y + p.gravity[1]) * dt;
+        float rho = d.f_rho[i] + d.f_drho[i] * dt;
+        rho = fmaxf(rho, by_phase(p.min_density, ph));
+        d.f_rho[i] = rho;
+        d.f_p[i] = density_to_pressure(p, rho, ph);
+        x.x = fminf(fmaxf(x.x, p.domain_xmin[0]), p.domain_xmax[0]);
+        x.y = fminf(fmaxf(x.y, p.domain_xmin[1]), p.domain_xmax[1]);
+        d.f_pos[i] = x;
+        d.f_vel[i] = v;
+        float s2 = __fadd_rn(__fmul_rn(v.x, v.x), __fmul_rn(v.y, v.y));
+        if (s2 == s2) sp2 = __float_as_uint(s2);  // NaN never wins, as on the host
+        moved2 = disp2(x0, x);
+    }
+    block_max_to<kBlock>(sp2, d.max_speed2_bits);
+    __syncthreads();
+    block_max_to<kBlock>(moved2, &d.disp2_bits[0]);
+}
+
 // (I - n n^T) d with n = normalize(g), zeroed below EPS_FOR_SUM
 // (fluid.cu:394-397)
 __device__ __forceinline__ float2 project(float2 g, float2 disp) {
@@ -266,9 +646,9 @@ __device__ __forceinline__ float2 project(float2 g, float2 disp) {
     return make_float2(m00 * disp.x + m01 * disp.y, m10 * disp.x + m11 * disp.y);
 }
 
-__global__ void __launch_bounds__(kBlock) k_shift_update(sphnj_params p, DevState d) {
-    const int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= p.fluid_number_total) return;
+// shiftDisplacementCalculate + correctionUpdate for particle i; returns the
+// squared displacement (float bits)
+__device__ __forceinline__ unsigned int shift_update_particle(const sphnj_params &p, const DevState &d, int i) {
     // getMaxSpeed's clamp, fluid.cu:438-439
     const float vmax = __fsqrt_rn(__uint_as_float(*d.max_speed2_bits));
     const float max_speed = fminf(vmax, __fmul_rn(0.1f, fminf(p.sound_speed[0], p.sound_speed[1])));
@@ -300,7 +680,8 @@ __global__ void __launch_bounds__(kBlock) k_shift_update(sphnj_params p, DevStat
     }
     d.f_fbt[i] = bt;
     const float2 sh = make_float2(max_speed * dd.x, max_speed * dd.y);
-    float2 x = d.f_pos[i];
+    const float2 x0 = d.f_pos[i];
+    float2 x = x0;
     x.x += sh.x;
     x.y += sh.y;
     d.f_pos[i] = x;
@@ -309,25 +690,61 @@ __global__ void __launch_bounds__(kBlock) k_shift_update(sphnj_params p, DevStat
     v.x += m.x * sh.x + m.z * sh.y;
     v.y += m.y * sh.x + m.w * sh.y;
     d.f_vel[i] = v;
+    return disp2(x0, x);
 }
+
+__global__ void __launch_bounds__(kBlock) k_shift_update(sphnj_params p, DevState d, int pass) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    unsigned int moved2 = 0u;
+    if (i < p.fluid_number_total) moved2 = shift_update_particle(p, d, i);
+    if (pass < kMaskShifts) block_max_to<kBlock>(moved2, &d.disp2_bits[1 + pass]);
+}
+
+inline int tile_cap(int tile_h) { return 3 * (tile_h + 2) * 24; }
+inline unsigned tile_blocks(const sphnj_params &p, int tile_h) {
+    return (unsigned)p.cell_number[0] * (unsigned)((p.cell_number[1] + tile_h - 1) / tile_h);
+}
+constexpr size_t kPairSmemPerEntry = 3 * sizeof(float2) + sizeof(int) + 1;
 
 }  // namespace
 
-void launch_fluid_pair(cudaStream_t st, const sphnj_params &p, const DevState &d) {
+void launch_fluid_pair(cudaStream_t st, const sphnj_params &p, const DevState &d, const TileConfig &tc) {
     const int n = p.fluid_number_total;
-    if (n > 0) k_fluid_pair<<<grid_for(n, kPairBlock), kPairBlock, 0, st>>>(p, d);
+    if (n <= 0) return;
+    if (!tc.tiled) {
+        k_fluid_pair_each<<<grid_for(n, kPairBlock), kPairBlock, 0, st>>>(p, d, 0);
+        return;
+    }
+    const int cap = tile_cap(tc.tile_h);
+    const size_t smem = cap * kPairSmemPerEntry;
+    static size_t opted = 48 * 1024;  // dynamic shared memory above 48 KB needs an opt-in
+    if (smem > opted) {
+        cudaFuncSetAttribute(k_fluid_pair_tiled, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+        opted = smem;
+    }
+    k_fluid_pair_tiled<<<tile_blocks(p, tc.tile_h), kTileBlock, smem, st>>>(p, d, tc.tile_h, cap);
+    k_fluid_pair_each<<<kFallbackBlocks, kPairBlock, 0, st>>>(p, d, 1);
 }
 void launch_fluid_update(cudaStream_t st, const sphnj_params &p, const DevState &d) {
     const int n = p.fluid_number_total;
     if (n > 0) k_fluid_update<<<grid_for(n, kBlock), kBlock, 0, st>>>(p, d);
 }
-void launch_shift_gradient(cudaStream_t st, const sphnj_params &p, const DevState &d) {
+void launch_shift_gradient(cudaStream_t st, const sphnj_params &p, const DevState &d, const TileConfig &tc,
+                           int pass) {
     const int n = p.fluid_number_total;
-    if (n > 0) k_shift_gradient<<<grid_for(n, kPairBlock), kPairBlock, 0, st>>>(p, d);
+    if (n <= 0) return;
+    if (!tc.tiled) {
+        k_shift_gradient_each<<<grid_for(n, kPairBlock), kPairBlock, 0, st>>>(p, d, 0);
+        return;
+    }
+    const int cap = tile_cap(tc.tile_h);
+    k_shift_gradient_tiled<<<tile_blocks(p, tc.tile_h), kTileBlock, cap * sizeof(float2), st>>>(p, d, tc.tile_h,
+                                                                                                  cap, pass);
+    k_shift_gradient_each<<<kFallbackBlocks, kPairBlock, 0, st>>>(p, d, 1);
 }
-void launch_shift_update(cudaStream_t st, const sphnj_params &p, const DevState &d) {
+void launch_shift_update(cudaStream_t st, const sphnj_params &p, const DevState &d, int pass) {
     const int n = p.fluid_number_total;
-    if (n > 0) k_shift_update<<<grid_for(n, kBlock), kBlock, 0, st>>>(p, d);
+    if (n > 0) k_shift_update<<<grid_for(n, kBlock), kBlock, 0, st>>>(p, d, pass);
 }
 
 }  // namespace sphnj
