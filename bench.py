@@ -51,6 +51,8 @@ def parse():
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--untiled", action="store_true", help="one thread per particle in the neighbour sweeps")
     ap.add_argument("--tile-h", type=int, default=16, help="cells per tile of the neighbour sweeps")
+    ap.add_argument("--no-graphs", action="store_true", help="issue every kernel of a step instead of replaying "
+                                                             "the step's captured CUDA graph")
     return ap.parse_args()
 
 
@@ -185,6 +187,7 @@ def run_ours(args):
     sim = S.Simulation(p)
     sim.set_stream(stream.cuda_stream)
     sim.set_tiling(not args.untiled, args.tile_h)
+    sim.set_graphs(not args.no_graphs)
     sim.upload(arr)
 
     def barrier():
@@ -295,7 +298,8 @@ def run_ours(args):
         "data": "synthetic (lattice gas-liquid dam break generated in-process, reference .dat layout)",
         "config": {"workload": f"gas-liquid dam break, 1.0x2.0 m water in a 4.0x3.0 m air-filled tank, dx={args.dx}",
                    "form": "plain (reference precision and cell-list order)",
-                   "sweeps": "per-particle" if args.untiled else f"tiled, {args.tile_h} cells per tile", "n_fluid": nf, "n_liquid": p.fluid_number[0],
+                   "sweeps": "per-particle" if args.untiled else f"tiled, {args.tile_h} cells per tile",
+                   "launch": "direct" if args.no_graphs else "one CUDA graph per kind of step", "n_fluid": nf, "n_liquid": p.fluid_number[0],
                    "n_solid": ns, "n_virt": nv, "cells": p.cell_number_total, "shift_per_step": p.shift_per_step,
                    "sort_every_step": p.sort_every_step, "dt": p.dt,
                    "l2": "inputs larger than L2 (fluid state ~0.3 GB > 129 MB)",

@@ -318,6 +318,13 @@ int  sphnj_debug_max_speed(sphnj_ctx *ctx, float *max_speed);
  * the speed differs.  Default: tiled, tile_h = 16. */
 int  sphnj_set_tiling(sphnj_ctx *ctx, int tiled, int tile_h);
 
+/* on != 0 (default): each kind of step (sort or rebuild step, list buffer,
+ * first sort of the virtual particles) is captured once into a CUDA graph and
+ * replayed, so a step costs one graph launch on the host; 0 launches every
+ * kernel individually.  Results are identical.  Per-stage profiling
+ * (sphnj_profile_enable) always launches individually. */
+int  sphnj_set_graphs(sphnj_ctx *ctx, int on);
+
 /* ---- measurement (the reference has only a host clock() around its loop,
  * calculation.cu:24-46) -------------------------------------------------- */
 

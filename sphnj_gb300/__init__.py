@@ -67,6 +67,8 @@ def lib() -> C.CDLL:
         L.sphnj_stat_launches.restype = C.c_int
         L.sphnj_set_tiling.argtypes = [C.c_void_p, C.c_int, C.c_int]
         L.sphnj_set_tiling.restype = C.c_int
+        L.sphnj_set_graphs.argtypes = [C.c_void_p, C.c_int]
+        L.sphnj_set_graphs.restype = C.c_int
         for f in ("sphnj_params_read_ini", "sphnj_params_read_counts", "sphnj_params_derive",
                   "sphnj_read_particles", "sphnj_abi_sizeof"):
             getattr(L, f).restype = C.c_int
@@ -167,8 +169,11 @@ class Simulation:
         s = state_struct(arrays)
         self._check(self._lib.sphnj_upload(self._h, C.byref(s)), "upload")
 
-    def set_tiling(self, tiled: bool = True, tile_h: int = 8):
+    def set_tiling(self, tiled: bool = True, tile_h: int = 16):
         self._check(self._lib.sphnj_set_tiling(self._h, 1 if tiled else 0, int(tile_h)), "set_tiling")
+
+    def set_graphs(self, on: bool = True):
+        self._check(self._lib.sphnj_set_graphs(self._h, 1 if on else 0), "set_graphs")
 
     def upload_fields(self, mask: int, arrays: dict):
         s = state_struct(arrays)

@@ -19,6 +19,7 @@
 #include <algorithm>
 #include <cstdio>
 #include <cstring>
+#include <map>
 #include <string>
 #include <vector>
 
@@ -92,6 +93,10 @@ struct ProfRec {
     int stage, kernels;
     cudaEvent_t a, b;
 };
+struct StepGraph {
+    cudaGraphExec_t exec;
+    int kernels;
+};
 }  // namespace
 
 struct sphnj_ctx {
@@ -119,8 +124,9 @@ struct sphnj_ctx {
     bool virt_cells_valid = false;  // virtual cell ids computed since the last upload
     bool uploaded = false;
     int *f_listed_total = nullptr;
-    int stamp = 0;  // increases every step (marks the listed fluid particles)
     TileConfig tiles;
+    bool use_graphs = true;  // replay each kind of step as a captured CUDA graph
+    std::map<int, StepGraph> graphs;
     std::string msg = "ok";
 };
 
@@ -160,6 +166,7 @@ size_t layout(sphnj_ctx *ctx, char *base) {
     d.f_nbr = a.take<uint4>((size_t)kNbrChunks * nf);
     d.f_nbr_cnt = a.take<uint8_t>(nf);
     d.disp2_bits = a.take<unsigned int>(1 + kMaskShifts);
+    d.stamp = a.take<int>(1);
     d.s_pos = a.take<double2>(ns); d.s_ref = a.take<double2>(ns);
     d.s_vel = a.take<double2>(ns); d.s_dudt = a.take<double2>(ns);
     d.s_F = a.take<dmat2>(ns); d.s_P = a.take<dmat2>(ns); d.s_L = a.take<dmat2>(ns);
@@ -305,6 +312,10 @@ int sphnj_create(const sphnj_params *p, int form, sphnj_ctx **out) {
         sphnj_destroy(ctx);
         return SPHNJ_ERR_CUDA;
     }
+    if (configure_sweeps(ctx->tiles) != cudaSuccess) {
+        sphnj_destroy(ctx);
+        return SPHNJ_ERR_CUDA;
+    }
     bind_lists(ctx);
     *out = ctx;
     return SPHNJ_OK;
@@ -319,6 +330,7 @@ void sphnj_destroy(sphnj_ctx *ctx) {
         cudaEventDestroy(r.b);
     }
     for (auto e : ctx->pool) cudaEventDestroy(e);
+    for (auto &g : ctx->graphs) cudaGraphExecDestroy(g.second.exec);
     if (ctx->arena) cudaFree(ctx->arena);
     if (ctx->h_err) cudaFreeHost(ctx->h_err);
     if (ctx->own) cudaStreamDestroy(ctx->own);
@@ -403,16 +415,26 @@ int sphnj_upload(sphnj_ctx *ctx, const sphnj_host_state *s) {
     return SPHNJ_OK;
 }
 
-int sphnj_step(sphnj_ctx *ctx, int n) {
-    if (!ctx || n < 0) return SPHNJ_ERR_ARG;
-    if (!ctx->uploaded) return fail(ctx, SPHNJ_ERR_ARG, "sphnj_step before sphnj_upload");
-    cudaSetDevice(ctx->device);
+namespace {
+
+// What distinguishes the launch sequence of one step from another.
+struct StepKind {
+    bool is_sort, bin_virt, sort_virt;
+    int parity;  // list buffer that this step writes and reads
+    int key() const { return (is_sort ? 1 : 0) | (bin_virt ? 2 : 0) | (sort_virt ? 4 : 0) | (parity << 3); }
+};
+
+// Issues the launches of one step on the context stream; returns the number
+// of kernels launched.  Reads no host-side state that changes from step to
+// step except through `k`, so the sequence can be captured into a graph.
+int issue_step(sphnj_ctx *ctx, const StepKind &k) {
     const sphnj_params &p = ctx->p;
     const int nf = p.fluid_number_total, ns = p.solid_number, nv = p.virt_number;
     cudaStream_t st = ctx->st;
-    DevState &d = ctx->d;
-    // kernels each launcher issues (kernels_*.cu)
-    constexpr int kSortKernels = 7, kRebuildKernels = 4;
+    const DevState &d = ctx->d;
+    constexpr int kSortKernels = 7, kRebuildKernels = 4;  // kernels each launcher issues (kernels_cells.cu)
+    const int sweep_kernels = ctx->tiles.tiled ? 2 : 1;   // tiled sweep + fallback for unlisted particles
+    int launched = 0;
     auto stage = [&](int s, int kernels, auto &&fn) {
         ProfRec r{s, kernels, nullptr, nullptr};
         if (ctx->prof) {
@@ -425,70 +447,116 @@ int sphnj_step(sphnj_ctx *ctx, int n) {
             cudaEventRecord(r.b, st);
             ctx->pending.push_back(r);
         }
-        ctx->launches += (uint64_t)kernels;
+        launched += kernels;
     };
-    const int sweep_kernels = ctx->tiles.tiled ? 2 : 1;  // tiled sweep + fallback for unlisted particles
-    for (int it = 0; it < n; ++it) {
-        ctx->step++;
-        d.stamp = ++ctx->stamp;
-        const Listing lgf{d.f_listed, ctx->stamp, ctx->f_listed_total};
-        const bool is_sort = ((ctx->step - 1) % p.sort_every_step) == 0;  // SimTime::isSort
-        // virtual particles are binned until their first sort (and once after
-        // an upload); afterwards their ids never change
-        const bool bin_virt = !ctx->virt_sorted || !ctx->virt_cells_valid;
-        stage(ST_BIN, 1, [&] { launch_bin(st, p, d, bin_virt); });
-        ctx->virt_cells_valid = true;
-        if (is_sort) {
-            if (nf > 0)
-                stage(ST_SORT, kSortKernels,
-                      [&] {
-                          launch_sort_kind(st, p, d, KF, nf, d.f_cell, ctx->sc, ctx->lf[ctx->parity], ctx->payload,
-                                           lgf);
-                      });
-            if (ns > 0)
-                stage(ST_SORT, kSortKernels,
-                      [&] { launch_sort_kind(st, p, d, KS, ns, d.s_cell, ctx->sc, ctx->ls[ctx->parity], ctx->payload); });
-            if (nv > 0 && !ctx->virt_sorted) {
-                // virtual particles never move: after this first sort their
-                // order, cell ids and lists stay as they are (a stable sort of
-                // sorted keys is the identity)
-                stage(ST_SORT, kSortKernels,
-                      [&] { launch_sort_kind(st, p, d, KV, nv, d.v_cell, ctx->sc, ctx->lv, ctx->payload); });
-                ctx->virt_sorted = true;
-            }
-        } else {
-            ctx->parity ^= 1;
-            const int cur = ctx->parity, prev = cur ^ 1;
-            if (nf > 0)
-                stage(ST_REBUILD, kRebuildKernels,
-                      [&] {
-                          launch_rebuild_kind(st, p, nf, d.f_cell, ctx->lf[prev], ctx->lf[cur], ctx->sc, d.err, lgf);
-                      });
-            if (ns > 0)
-                stage(ST_REBUILD, kRebuildKernels,
-                      [&] { launch_rebuild_kind(st, p, ns, d.s_cell, ctx->ls[prev], ctx->ls[cur], ctx->sc, d.err); });
-        }
-        bind_lists(ctx);
-        stage(ST_CAPACITY, 1, [&] { launch_capacity_check(st, p, d); });
-        if (nf > 0 && ns > 0) stage(ST_SOLID_COUPLE, 1, [&] { launch_solid_couple(st, p, d); });
-        if (nv > 0) stage(ST_VIRT_DATA, 1, [&] { launch_virt_data(st, p, d); });
-        if (nf > 0) {
-            stage(ST_FLUID_PAIR, sweep_kernels, [&] { launch_fluid_pair(st, p, d, ctx->tiles); });
-            stage(ST_FLUID_UPDATE, 1, [&] { launch_fluid_update(st, p, d); });
-        }
-        if (ns > 0)
-            for (int k = 0; k < p.solid_sub_step; ++k) {
-                stage(ST_SOLID_DEFORM, 1, [&] { launch_solid_deformation(st, p, d); });
-                stage(ST_SOLID_FORCE, 1, [&] { launch_solid_force(st, p, d); });
-                stage(ST_SOLID_UPDATE, 1, [&] { launch_solid_update(st, p, d); });
-            }
+    const Listing lgf{d.f_listed, d.stamp, ctx->f_listed_total};
+    stage(ST_BIN, 1, [&] { launch_bin(st, p, d, k.bin_virt); });
+    if (k.is_sort) {
         if (nf > 0)
-            for (int k = 0; k < p.shift_per_step; ++k) {
-                stage(ST_SHIFT_GRADIENT, sweep_kernels, [&] { launch_shift_gradient(st, p, d, ctx->tiles, k); });
-                stage(ST_SHIFT_UPDATE, 1, [&] { launch_shift_update(st, p, d, k); });
+            stage(ST_SORT, kSortKernels, [&] {
+                launch_sort_kind(st, p, d, KF, nf, d.f_cell, ctx->sc, ctx->lf[k.parity], ctx->payload, lgf);
+            });
+        if (ns > 0)
+            stage(ST_SORT, kSortKernels,
+                  [&] { launch_sort_kind(st, p, d, KS, ns, d.s_cell, ctx->sc, ctx->ls[k.parity], ctx->payload); });
+        if (k.sort_virt)
+            stage(ST_SORT, kSortKernels,
+                  [&] { launch_sort_kind(st, p, d, KV, nv, d.v_cell, ctx->sc, ctx->lv, ctx->payload); });
+    } else {
+        const int cur = k.parity, prev = cur ^ 1;
+        if (nf > 0)
+            stage(ST_REBUILD, kRebuildKernels, [&] {
+                launch_rebuild_kind(st, p, nf, d.f_cell, ctx->lf[prev], ctx->lf[cur], ctx->sc, d.err, lgf);
+            });
+        if (ns > 0)
+            stage(ST_REBUILD, kRebuildKernels,
+                  [&] { launch_rebuild_kind(st, p, ns, d.s_cell, ctx->ls[prev], ctx->ls[cur], ctx->sc, d.err); });
+    }
+    stage(ST_CAPACITY, 1, [&] { launch_capacity_check(st, p, d); });
+    if (nf > 0 && ns > 0) stage(ST_SOLID_COUPLE, 1, [&] { launch_solid_couple(st, p, d); });
+    if (nv > 0) stage(ST_VIRT_DATA, 1, [&] { launch_virt_data(st, p, d); });
+    if (nf > 0) {
+        stage(ST_FLUID_PAIR, sweep_kernels, [&] { launch_fluid_pair(st, p, d, ctx->tiles); });
+        stage(ST_FLUID_UPDATE, 1, [&] { launch_fluid_update(st, p, d); });
+    }
+    if (ns > 0)
+        for (int s = 0; s < p.solid_sub_step; ++s) {
+            stage(ST_SOLID_DEFORM, 1, [&] { launch_solid_deformation(st, p, d); });
+            stage(ST_SOLID_FORCE, 1, [&] { launch_solid_force(st, p, d); });
+            stage(ST_SOLID_UPDATE, 1, [&] { launch_solid_update(st, p, d); });
+        }
+    if (nf > 0)
+        for (int s = 0; s < p.shift_per_step; ++s) {
+            stage(ST_SHIFT_GRADIENT, sweep_kernels, [&] { launch_shift_gradient(st, p, d, ctx->tiles, s); });
+            stage(ST_SHIFT_UPDATE, 1, [&] { launch_shift_update(st, p, d, s); });
+        }
+    return launched;
+}
+
+void drop_graphs(sphnj_ctx *ctx) {
+    for (auto &g : ctx->graphs) cudaGraphExecDestroy(g.second.exec);
+    ctx->graphs.clear();
+}
+
+// Advances the host-side step state of ctx by one step and returns the kind
+// of launch sequence that step needs.
+StepKind advance(sphnj_ctx *ctx) {
+    const sphnj_params &p = ctx->p;
+    ctx->step++;
+    StepKind k;
+    k.is_sort = ((ctx->step - 1) % p.sort_every_step) == 0;  // SimTime::isSort
+    // virtual particles are binned until their first sort (and once after an
+    // upload); afterwards their ids never change.  After their first sort
+    // their order and lists stay as they are (a stable sort of sorted keys is
+    // the identity), so they are sorted once.
+    k.bin_virt = !ctx->virt_sorted || !ctx->virt_cells_valid;
+    k.sort_virt = k.is_sort && p.virt_number > 0 && !ctx->virt_sorted;
+    if (!k.is_sort) ctx->parity ^= 1;
+    k.parity = ctx->parity;
+    ctx->virt_cells_valid = true;
+    if (k.sort_virt) ctx->virt_sorted = true;
+    bind_lists(ctx);
+    return k;
+}
+
+}  // namespace
+
+extern "C" int sphnj_step(sphnj_ctx *ctx, int n) {
+    if (!ctx || n < 0) return SPHNJ_ERR_ARG;
+    if (!ctx->uploaded) return fail(ctx, SPHNJ_ERR_ARG, "sphnj_step before sphnj_upload");
+    cudaSetDevice(ctx->device);
+    cudaStream_t st = ctx->st;
+    for (int it = 0; it < n; ++it) {
+        const StepKind k = advance(ctx);
+        if (ctx->use_graphs && !ctx->prof) {
+            auto it_g = ctx->graphs.find(k.key());
+            if (it_g == ctx->graphs.end()) {
+                cudaGraph_t g = nullptr;
+                CK(cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal));
+                const int launched = issue_step(ctx, k);
+                cudaError_t e = cudaStreamEndCapture(st, &g);
+                cudaGraphExec_t exec = nullptr;
+                if (e == cudaSuccess) e = cudaGraphInstantiate(&exec, g, 0);
+                if (g) cudaGraphDestroy(g);
+                if (e != cudaSuccess) return cuda_fail(ctx, e, "step graph capture");
+                it_g = ctx->graphs.emplace(k.key(), StepGraph{exec, launched}).first;
             }
+            CK(cudaGraphLaunch(it_g->second.exec, st));
+            ctx->launches += (uint64_t)it_g->second.kernels;
+        } else {
+            ctx->launches += (uint64_t)issue_step(ctx, k);
+        }
         CK(cudaGetLastError());
     }
+    return SPHNJ_OK;
+}
+
+extern "C" int sphnj_set_graphs(sphnj_ctx *ctx, int on) {
+    if (!ctx) return SPHNJ_ERR_ARG;
+    cudaSetDevice(ctx->device);
+    CK(cudaStreamSynchronize(ctx->st));
+    ctx->use_graphs = on != 0;
+    drop_graphs(ctx);
     return SPHNJ_OK;
 }
 
@@ -553,8 +621,12 @@ int sphnj_upload_fields(sphnj_ctx *ctx, uint32_t mask, const sphnj_host_state *s
 
 int sphnj_set_tiling(sphnj_ctx *ctx, int tiled, int tile_h) {
     if (!ctx || tile_h < 1 || tile_h > 64) return SPHNJ_ERR_ARG;
+    cudaSetDevice(ctx->device);
+    CK(cudaStreamSynchronize(ctx->st));
     ctx->tiles.tiled = tiled != 0;
     ctx->tiles.tile_h = tile_h;
+    drop_graphs(ctx);
+    CK(configure_sweeps(ctx->tiles));
     return SPHNJ_OK;
 }
 

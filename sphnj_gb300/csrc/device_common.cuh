@@ -54,11 +54,12 @@ struct DevState {
     // current cell lists (CSR) used by the neighbour sweeps
     const int2 *rng_f, *rng_s, *rng_v;
     const int *lst_f, *lst_s, *lst_v;
-    // which fluid particles the current lists hold (listed[i] == stamp) and
-    // how many
+    // which fluid particles the current lists hold (listed[i] == *stamp) and
+    // how many; the stamp is advanced on the device at the start of every step
+    // (so that a captured step graph replays correctly)
     int *f_listed;
     const int *f_listed_total;
-    int stamp;
+    int *stamp;
     // neighbour lists of this step, indexed by the particle's position h in
     // the fluid CSR list: the tile slots (uint16) of the fluid entries that
     // were within the cutoff plus skin when the pair pass ran, in the

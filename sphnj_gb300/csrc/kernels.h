@@ -35,7 +35,7 @@ enum Kind { KF = 0, KS = 1, KV = 2 };
 // per-particle fallback kernels.  Null members: nothing recorded.
 struct Listing {
     int *listed = nullptr;
-    int stamp = 0;
+    const int *stamp = nullptr;  // device value of this step's stamp
     int *total = nullptr;
 };
 
@@ -62,6 +62,10 @@ struct TileConfig {
     bool tiled = true;
     int tile_h = 16;
 };
+
+// Function attributes the sweeps need for this configuration (dynamic shared
+// memory above 48 KB); called outside any stream capture.
+cudaError_t configure_sweeps(const TileConfig &tc);
 
 // fluid passes (fluid.cu)
 void launch_fluid_pair(cudaStream_t st, const sphnj_params &p, const DevState &d, const TileConfig &tc);

@@ -40,7 +40,10 @@ __global__ void k_bin(sphnj_params p, DevState d, int with_virt) {
     const int nf = p.fluid_number_total, ns = p.solid_number, nv = with_virt ? p.virt_number : 0;
     const int C = p.cell_number_total;
     long t = (long)blockIdx.x * blockDim.x + threadIdx.x;
-    if (t == 0) *d.max_speed2_bits = 0u;
+    if (t == 0) {
+        *d.max_speed2_bits = 0u;
+        *d.stamp += 1;  // this step's stamp (read by kernels launched after this one)
+    }
     if (t < 1 + kMaskShifts) d.disp2_bits[t] = 0u;  // grid has >= 256 threads
     int kind, i, c;
     if (t < nf) {
@@ -229,10 +232,10 @@ struct FluidPayload {
     int *cell;
 };
 __global__ void k_gather_fluid(int n, const int *sorted, DevState d, FluidPayload o, int *lst, int *listed,
-                               int stamp) {
+                               const int *stamp) {
     int k = blockIdx.x * blockDim.x + threadIdx.x;
     if (k >= n) return;
-    if (listed) listed[k] = stamp;
+    if (listed) listed[k] = *stamp;
     int s = sorted[k];
     o.pos[k] = d.f_pos[s];
     o.vel[k] = d.f_vel[s];
@@ -343,7 +346,7 @@ __global__ void k_rebuild_count(int C, int nx, int ny, const int2 *prng, const i
 
 __global__ void k_rebuild_write(int C, int nx, int ny, const int2 *prng, const int *plst, const int *cell,
                                 const int *cnt9, const int *local, const int *sums, int2 *crng, int *clst,
-                                int *listed, int stamp) {
+                                int *listed, const int *stamp) {
     int m = blockIdx.x * blockDim.x + threadIdx.x;
     if (m >= C) return;
     const int mi = m / ny, mj = m - mi * ny;
@@ -371,7 +374,7 @@ __global__ void k_rebuild_write(int C, int nx, int ny, const int2 *prng, const i
         for (int q = 0; q < 9; ++q)
             if (q == s) dst = base[q]++;
         clst[dst] = pidx;
-        if (listed) listed[pidx] = stamp;
+        if (listed) listed[pidx] = *stamp;
     }
 }
 

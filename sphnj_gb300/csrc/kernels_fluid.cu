@@ -583,17 +583,19 @@ __global__ void __launch_bounds__(kTileBlock) k_shift_gradient_tiled(sphnj_param
 __global__ void __launch_bounds__(kPairBlock) k_fluid_pair_each(sphnj_params p, DevState d, int only_unlisted) {
     const int nf = p.fluid_number_total;
     if (only_unlisted && *d.f_listed_total == nf) return;
+    const int stamp = *d.stamp;
     const SrcGlobal src{&d};
     for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < nf; i += gridDim.x * blockDim.x)
-        if (!only_unlisted || d.f_listed[i] != d.stamp) pair_particle(p, d, src, i);
+        if (!only_unlisted || d.f_listed[i] != stamp) pair_particle(p, d, src, i);
 }
 
 __global__ void __launch_bounds__(kPairBlock) k_shift_gradient_each(sphnj_params p, DevState d, int only_unlisted) {
     const int nf = p.fluid_number_total;
     if (only_unlisted && *d.f_listed_total == nf) return;
+    const int stamp = *d.stamp;
     const SrcGlobal src{&d};
     for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < nf; i += gridDim.x * blockDim.x)
-        if (!only_unlisted || d.f_listed[i] != d.stamp) shift_particle(p, d, src, i);
+        if (!only_unlisted || d.f_listed[i] != stamp) shift_particle(p, d, src, i);
 }
 
 // densityToPressure, fluid.cu:15-23
@@ -708,6 +710,12 @@ constexpr size_t kPairSmemPerEntry = 3 * sizeof(float2) + sizeof(int) + 1;
 
 }  // namespace
 
+cudaError_t configure_sweeps(const TileConfig &tc) {
+    const size_t smem = tile_cap(tc.tile_h) * kPairSmemPerEntry;  // above 48 KB needs an opt-in
+    if (smem <= 48 * 1024) return cudaSuccess;
+    return cudaFuncSetAttribute(k_fluid_pair_tiled, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+}
+
 void launch_fluid_pair(cudaStream_t st, const sphnj_params &p, const DevState &d, const TileConfig &tc) {
     const int n = p.fluid_number_total;
     if (n <= 0) return;
@@ -717,11 +725,6 @@ void launch_fluid_pair(cudaStream_t st, const sphnj_params &p, const DevState &d
     }
     const int cap = tile_cap(tc.tile_h);
     const size_t smem = cap * kPairSmemPerEntry;
-    static size_t opted = 48 * 1024;  // dynamic shared memory above 48 KB needs an opt-in
-    if (smem > opted) {
-        cudaFuncSetAttribute(k_fluid_pair_tiled, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-        opted = smem;
-    }
     k_fluid_pair_tiled<<<tile_blocks(p, tc.tile_h), kTileBlock, smem, st>>>(p, d, tc.tile_h, cap);
     k_fluid_pair_each<<<kFallbackBlocks, kPairBlock, 0, st>>>(p, d, 1);
 }
