@@ -381,6 +381,35 @@ int  sphnj_rebuild_cell_lists_noalloc(int nx, int ny, int n_particles, const int
 /* Message of the last error on this context (never NULL). */
 const char *sphnj_last_error(const sphnj_ctx *ctx);
 
+/* ---- batches of independent scenes -----------------------------------------
+ * The reference runs one case per process (main.cu:14-35).  A batch advances
+ * many independent scenes - contexts created and uploaded as usual, of any
+ * sizes and parameters - together: every stage of a step is one launch over
+ * all of them, and each kind of step is replayed as one CUDA graph.  The
+ * result for every scene is identical to stepping it alone.
+ *
+ * The scenes of a batch must share sort_every_step and be at the same step
+ * (same istart, stepped together), and stay alive until the batch is
+ * destroyed.  While in a batch a scene launches on the batch's stream, so its
+ * uploads and downloads are ordered with the batch's steps; it may belong to
+ * one batch at a time and must not be given another stream. */
+typedef struct sphnj_batch sphnj_batch;
+
+int  sphnj_batch_create(sphnj_ctx *const *scenes, int n, sphnj_batch **out);
+void sphnj_batch_destroy(sphnj_batch *b);
+int  sphnj_batch_set_stream(sphnj_batch *b, void *cuda_stream);
+/* As sphnj_set_tiling / sphnj_set_graphs, for every scene of the batch. */
+int  sphnj_batch_set_tiling(sphnj_batch *b, int tiled, int tile_h);
+int  sphnj_batch_set_graphs(sphnj_batch *b, int on);
+/* Advances every scene n fluid steps (asynchronous, as sphnj_step). */
+int  sphnj_batch_step(sphnj_batch *b, int n);
+/* Waits for the batch's stream; reports the first scene with a device error. */
+int  sphnj_batch_synchronize(sphnj_batch *b);
+int  sphnj_batch_profile_enable(sphnj_batch *b, int on);
+int  sphnj_batch_profile_read(sphnj_batch *b, double *ms, int64_t *calls, int64_t *kernels);
+int  sphnj_batch_stat_launches(const sphnj_batch *b, uint64_t *launches);
+const char *sphnj_batch_last_error(const sphnj_batch *b);
+
 #ifdef __cplusplus
 }
 #endif

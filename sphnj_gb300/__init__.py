@@ -243,5 +243,76 @@ class Simulation:
         return v.value
 
 
-__all__ = ["abi", "Params", "Simulation", "SphnjError", "build", "lib", "load_case", "read_ini", "derive",
+class Batch:
+    """Independent scenes advanced together: every stage of a step is one
+    launch over all of them (sphnj_batch_* in include/sphnj.h).  The scenes
+    are uploaded Simulations at the same step with the same sort_every_step;
+    they stay usable for download (and upload) and must outlive the batch."""
+
+    def __init__(self, sims):
+        self.sims = list(sims)
+        self._lib = lib()
+        handles = (C.c_void_p * len(self.sims))(*[s._h.value for s in self.sims])
+        h = C.c_void_p()
+        rc = self._lib.sphnj_batch_create(handles, len(self.sims), C.byref(h))
+        if rc:
+            raise SphnjError(rc, "sphnj_batch_create: scenes must be uploaded, at the same step, share "
+                                 "sort_every_step and belong to no other batch")
+        self._h = h
+
+    def _check(self, rc: int, what: str):
+        if rc:
+            raise SphnjError(rc, f"{what}: {self._lib.sphnj_batch_last_error(self._h).decode()}")
+
+    def close(self):
+        if getattr(self, "_h", None):
+            self._lib.sphnj_batch_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+    def set_stream(self, stream_handle: int | None):
+        self._check(self._lib.sphnj_batch_set_stream(self._h, C.c_void_p(stream_handle or 0)), "set_stream")
+
+    def set_tiling(self, tiled: bool = True, tile_h: int = 16):
+        self._check(self._lib.sphnj_batch_set_tiling(self._h, 1 if tiled else 0, int(tile_h)), "set_tiling")
+
+    def set_graphs(self, on: bool = True):
+        self._check(self._lib.sphnj_batch_set_graphs(self._h, 1 if on else 0), "set_graphs")
+
+    def step(self, n: int = 1):
+        self._check(self._lib.sphnj_batch_step(self._h, int(n)), "step")
+
+    def synchronize(self):
+        self._check(self._lib.sphnj_batch_synchronize(self._h), "synchronize")
+
+    def profile_enable(self, on: bool = True):
+        self._check(self._lib.sphnj_batch_profile_enable(self._h, 1 if on else 0), "profile_enable")
+
+    def profile_read(self) -> dict:
+        """{stage: (device ms, timed calls, kernels launched)} since enabling."""
+        n = self._lib.sphnj_profile_stage_count()
+        ms = (C.c_double * n)()
+        calls = (C.c_int64 * n)()
+        kern = (C.c_int64 * n)()
+        self._check(self._lib.sphnj_batch_profile_read(self._h, ms, calls, kern), "profile_read")
+        return {self._lib.sphnj_profile_stage_name(i).decode(): (ms[i], calls[i], kern[i]) for i in range(n)}
+
+    def launches(self) -> int:
+        v = C.c_uint64()
+        self._check(self._lib.sphnj_batch_stat_launches(self._h, C.byref(v)), "stat_launches")
+        return v.value
+
+
+__all__ = ["abi", "Params", "Simulation", "Batch", "SphnjError", "build", "lib", "load_case", "read_ini", "derive",
            "read_counts", "read_particles", "alloc_state", "state_struct"]

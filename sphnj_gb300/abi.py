@@ -203,6 +203,22 @@ def declare(lib: C.CDLL, prefix: str) -> None:
         g("last_error").restype = C.c_char_p
         g("synchronize").argtypes = [vp]
         g("synchronize").restype = C.c_int
+        g("batch_create").argtypes = [C.POINTER(vp), C.c_int, C.POINTER(vp)]
+        g("batch_destroy").argtypes = [vp]
+        g("batch_destroy").restype = None
+        g("batch_set_stream").argtypes = [vp, vp]
+        g("batch_set_tiling").argtypes = [vp, C.c_int, C.c_int]
+        g("batch_set_graphs").argtypes = [vp, C.c_int]
+        g("batch_step").argtypes = [vp, C.c_int]
+        g("batch_synchronize").argtypes = [vp]
+        g("batch_profile_enable").argtypes = [vp, C.c_int]
+        g("batch_profile_read").argtypes = [vp, C.POINTER(C.c_double), C.POINTER(C.c_int64), C.POINTER(C.c_int64)]
+        g("batch_stat_launches").argtypes = [vp, C.POINTER(C.c_uint64)]
+        for n in ("batch_create", "batch_set_stream", "batch_set_tiling", "batch_set_graphs", "batch_step",
+                  "batch_synchronize", "batch_profile_enable", "batch_profile_read", "batch_stat_launches"):
+            g(n).restype = C.c_int
+        g("batch_last_error").argtypes = [vp]
+        g("batch_last_error").restype = C.c_char_p
     else:
         g("create").argtypes = [C.POINTER(Params), C.c_int, C.c_int, C.POINTER(vp)]
         g("error").argtypes = [vp]

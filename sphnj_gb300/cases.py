@@ -358,6 +358,46 @@ def auxetic_block(dx=0.002, n=20, rate=1000.0, yield_stress=2.0e6, yield_strain=
                 solid_boundary_type=np.zeros(len(x), np.int32), notes=dict(dx=dx, cs=cs))
 
 
+SWEEP_SCENES = 256
+
+
+def sweep_scene(seed: int, iend: int = 2000) -> Case:
+    """Scene `seed` (0..255) of the batched sweep of independent scenes of
+    uneven size, drawn from a per-scene generator seeded with `seed`:
+      seeds 0..127    water-only dam breaks: a 1.0 m wide column of height
+                      H/W ~ U[0.5, 2.5] in a 4.0 x 3.0 m tank, particle count
+                      log-uniform in [2k, 60k] (dx = sqrt(W H / N)), 3 wall
+                      layers;
+      seeds 128..255  cantilever beams: length L ~ U[0.1, 0.3] m, thickness
+                      L/10, clamp 0.3 L, E log-uniform in [0.5, 20] MPa,
+                      nu ~ U[0.3, 0.45], rho = 1000, particle count
+                      log-uniform in [1k, 20k];
+    every lattice jittered by +-0.01 dx."""
+    if not 0 <= seed < SWEEP_SCENES:
+        raise ValueError(f"sweep scene seed {seed} outside 0..{SWEEP_SCENES - 1}")
+    rng = np.random.default_rng(seed)
+    if seed < SWEEP_SCENES // 2:
+        aspect = rng.uniform(0.5, 2.5)
+        n = math.exp(rng.uniform(math.log(2_000), math.log(60_000)))
+        col_w, col_h = 1.0, aspect
+        dx = math.sqrt(col_w * col_h / n)
+        case = tank(f"sweep{seed:03d}_dam", dx, 4.0, 3.0, col_w, col_h, layers=3, gas=False, iend=iend,
+                    jitter=0.01, seed=10_000 + seed)
+        case.notes.update(kind="dam_break", aspect=aspect, seed=seed)
+        return case
+    length = rng.uniform(0.1, 0.3)
+    E = math.exp(rng.uniform(math.log(0.5e6), math.log(20e6)))
+    nu = rng.uniform(0.3, 0.45)
+    n = math.exp(rng.uniform(math.log(1_000), math.log(20_000)))
+    thick, clamp = 0.1 * length, 0.3 * length
+    dx = math.sqrt((length + clamp) * thick / n)
+    case = beam(dx=dx, length=length, thick=thick, clamp=clamp, E=E, nu=nu, rho=1000.0, iend=iend,
+                jitter=0.01, seed=10_000 + seed)
+    case.name = f"sweep{seed:03d}_beam"
+    case.notes.update(kind="beam", E=E, nu=nu, seed=seed)
+    return case
+
+
 def by_name(name: str, **kw) -> Case:
     return {"dam_break_water": dam_break_water, "dam_break_gas": dam_break_gas, "beam": beam,
             "gate": gate, "auxetic_block": auxetic_block}[name](**kw)

@@ -1,0 +1,295 @@
+// Batched stepping: many independent scenes (each an ordinary context with
+// its own arena, uploaded and downloaded on its own) advanced together.
+//
+// Every stage of a step is ONE launch over all scenes of the batch: a block
+// finds its scene in a per-launch block table (scene k owns blocks first[k]
+// .. first[k+1]-1, in proportion to its own particle / cell / tile counts)
+// and reads the scene's record - parameters, state pointers, cell lists and
+// scratch - from device memory.  So a batch of 256 small scenes costs the
+// same ~30 launches per step as one large scene, every launch fills the GPU,
+// and scenes of uneven size share it in proportion to their work.  Each kind
+// of step is captured once as a CUDA graph and replayed.
+//
+// The scenes of a batch step in lockstep: they must share sort_every_step
+// and sit at the same step index with the same list buffer.  Scenes may
+// differ in everything else (sizes, grids, materials, time steps, shifting
+// passes and solid sub-steps per step: a scene with fewer passes owns no
+// block of the later ones).
+#include "context.h"
+
+#include <algorithm>
+#include <cstdio>
+#include <set>
+
+using namespace sphnj;
+
+struct sphnj_batch {
+    std::vector<sphnj_ctx *> scenes;
+    int device = 0;
+    cudaStream_t own = nullptr, st = nullptr;
+    GroupMany g;
+    std::vector<Scene> recs[2];        // host records, list buffer 0 / 1 bound
+    Scene *d_recs[2] = {nullptr, nullptr};
+    TileConfig tiles;
+    bool use_graphs = true;
+    std::map<int, StepGraph> graphs;
+    std::set<int> planned;             // step kinds whose block tables exist
+    Profiler prof;
+    uint64_t launches = 0;
+    std::string msg = "ok";
+};
+
+namespace {
+
+int bfail(sphnj_batch *b, int code, const std::string &m) {
+    if (b) b->msg = m;
+    return code;
+}
+
+int bcuda(sphnj_batch *b, cudaError_t e, const char *where) {
+    return bfail(b, SPHNJ_ERR_CUDA, std::string(where) + ": " + cudaGetErrorString(e));
+}
+
+#define BCK(call)                                                  \
+    do {                                                           \
+        cudaError_t e_ = (call);                                   \
+        if (e_ != cudaSuccess) return bcuda(b, e_, #call);         \
+    } while (0)
+
+void drop_graphs(sphnj_batch *b) {
+    for (auto &g : b->graphs) cudaGraphExecDestroy(g.second.exec);
+    b->graphs.clear();
+}
+
+// Builds the block tables of one kind of step (no launch).
+int plan(sphnj_batch *b, const StepKind &k) {
+    if (b->planned.count(k.key())) return SPHNJ_OK;
+    b->g.planning = true;
+    issue_step(b->g, k, b->st, b->tiles, nullptr);
+    b->g.planning = false;
+    if (b->g.error != cudaSuccess) {
+        cudaError_t e = b->g.error;
+        b->g.error = cudaSuccess;
+        return bcuda(b, e, "batch launch planning");
+    }
+    b->planned.insert(k.key());
+    return SPHNJ_OK;
+}
+
+void set_scene_streams(sphnj_batch *b, cudaStream_t st) {
+    for (sphnj_ctx *c : b->scenes) c->st = st;
+}
+
+}  // namespace
+
+extern "C" {
+
+int sphnj_batch_create(sphnj_ctx *const *scenes, int n, sphnj_batch **out) {
+    if (!scenes || n < 1 || !out) return SPHNJ_ERR_ARG;
+    *out = nullptr;
+    const sphnj_ctx *c0 = scenes[0];
+    if (!c0) return SPHNJ_ERR_ARG;
+    for (int i = 0; i < n; ++i) {
+        const sphnj_ctx *c = scenes[i];
+        if (!c || !c->uploaded || c->batch) return SPHNJ_ERR_ARG;
+        for (int j = 0; j < i; ++j)
+            if (scenes[j] == c) return SPHNJ_ERR_ARG;  // a scene appears once
+        if (c->device != c0->device || c->form != c0->form || c->p.sort_every_step != c0->p.sort_every_step ||
+            c->step != c0->step || c->parity != c0->parity)
+            return SPHNJ_ERR_ARG;
+    }
+    sphnj_batch *b = new sphnj_batch;
+    b->device = c0->device;
+    cudaSetDevice(b->device);
+    b->scenes.assign(scenes, scenes + n);
+    for (sphnj_ctx *c : b->scenes)
+        if (cudaStreamSynchronize(c->st) != cudaSuccess) {
+            cudaGetLastError();
+            delete b;
+            return SPHNJ_ERR_CUDA;
+        }
+    if (cudaStreamCreateWithFlags(&b->own, cudaStreamNonBlocking) != cudaSuccess) {
+        cudaGetLastError();
+        delete b;
+        return SPHNJ_ERR_CUDA;
+    }
+    b->st = b->own;
+    for (int par = 0; par < 2; ++par) {
+        b->recs[par].reserve(n);
+        for (sphnj_ctx *c : b->scenes) b->recs[par].push_back(scene_of(c, par));
+        cudaError_t e = cudaMalloc(&b->d_recs[par], sizeof(Scene) * n);
+        if (e == cudaSuccess)
+            e = cudaMemcpy(b->d_recs[par], b->recs[par].data(), sizeof(Scene) * n, cudaMemcpyHostToDevice);
+        if (e != cudaSuccess) {
+            cudaGetLastError();
+            for (Scene *r : b->d_recs)
+                if (r) cudaFree(r);
+            cudaStreamDestroy(b->own);
+            delete b;
+            return SPHNJ_ERR_CUDA;
+        }
+    }
+    b->g.n = n;
+    if (configure_sweeps(b->tiles) != cudaSuccess) {
+        cudaGetLastError();
+        for (Scene *r : b->d_recs) cudaFree(r);
+        cudaStreamDestroy(b->own);
+        delete b;
+        return SPHNJ_ERR_CUDA;
+    }
+    for (sphnj_ctx *c : b->scenes) c->batch = b;
+    set_scene_streams(b, b->st);
+    *out = b;
+    return SPHNJ_OK;
+}
+
+void sphnj_batch_destroy(sphnj_batch *b) {
+    if (!b) return;
+    cudaSetDevice(b->device);
+    if (b->st) cudaStreamSynchronize(b->st);
+    drop_graphs(b);
+    b->g.free_tables();
+    b->prof.release();
+    for (Scene *r : b->d_recs)
+        if (r) cudaFree(r);
+    for (sphnj_ctx *c : b->scenes) {
+        c->st = c->own;
+        c->batch = nullptr;
+    }
+    if (b->own) cudaStreamDestroy(b->own);
+    delete b;
+}
+
+int sphnj_batch_set_stream(sphnj_batch *b, void *stream) {
+    if (!b) return SPHNJ_ERR_ARG;
+    cudaSetDevice(b->device);
+    BCK(cudaStreamSynchronize(b->st));
+    b->st = stream ? static_cast<cudaStream_t>(stream) : b->own;
+    set_scene_streams(b, b->st);
+    return SPHNJ_OK;
+}
+
+int sphnj_batch_set_tiling(sphnj_batch *b, int tiled, int tile_h) {
+    if (!b || tile_h < 1 || tile_h > 64) return SPHNJ_ERR_ARG;
+    cudaSetDevice(b->device);
+    BCK(cudaStreamSynchronize(b->st));
+    b->tiles.tiled = tiled != 0;
+    b->tiles.tile_h = tile_h;
+    drop_graphs(b);
+    b->planned.clear();  // tiled launches have their own tables
+    BCK(configure_sweeps(b->tiles));
+    return SPHNJ_OK;
+}
+
+int sphnj_batch_set_graphs(sphnj_batch *b, int on) {
+    if (!b) return SPHNJ_ERR_ARG;
+    cudaSetDevice(b->device);
+    BCK(cudaStreamSynchronize(b->st));
+    b->use_graphs = on != 0;
+    drop_graphs(b);
+    return SPHNJ_OK;
+}
+
+int sphnj_batch_step(sphnj_batch *b, int n) {
+    if (!b || n < 0) return SPHNJ_ERR_ARG;
+    cudaSetDevice(b->device);
+    cudaStream_t st = b->st;
+    for (int it = 0; it < n; ++it) {
+        const sphnj_ctx *c0 = b->scenes[0];
+        for (const sphnj_ctx *c : b->scenes)
+            if (!c->uploaded || c->step != c0->step || c->parity != c0->parity)
+                return bfail(b, SPHNJ_ERR_ARG, "batch scenes are not at the same step");
+        StepKind k{};
+        for (size_t i = 0; i < b->scenes.size(); ++i) {
+            const StepKind ki = advance(b->scenes[i]);
+            if (i == 0) {
+                k = ki;
+            } else {
+                // re-binning or re-sorting virtual particles that are already
+                // binned and sorted changes nothing, so these are OR-ed
+                k.bin_virt = k.bin_virt || ki.bin_virt;
+                k.sort_virt = k.sort_virt || ki.sort_virt;
+            }
+        }
+        GroupMany &g = b->g;
+        g.h_scenes = b->recs[k.parity].data();
+        g.d_scenes = b->d_recs[k.parity];
+        int rc = plan(b, k);
+        if (rc) return rc;
+        if (b->use_graphs && !b->prof.on) {
+            auto it_g = b->graphs.find(k.key());
+            if (it_g == b->graphs.end()) {
+                cudaGraph_t graph = nullptr;
+                BCK(cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal));
+                const int launched = issue_step(g, k, st, b->tiles, nullptr);
+                cudaError_t e = cudaStreamEndCapture(st, &graph);
+                cudaGraphExec_t exec = nullptr;
+                if (e == cudaSuccess) e = g.error;
+                if (e == cudaSuccess) e = cudaGraphInstantiate(&exec, graph, 0);
+                if (graph) cudaGraphDestroy(graph);
+                g.error = cudaSuccess;
+                if (e != cudaSuccess) return bcuda(b, e, "batch step graph capture");
+                it_g = b->graphs.emplace(k.key(), StepGraph{exec, launched}).first;
+            }
+            BCK(cudaGraphLaunch(it_g->second.exec, st));
+            b->launches += (uint64_t)it_g->second.kernels;
+        } else {
+            b->launches += (uint64_t)issue_step(g, k, st, b->tiles, b->prof.on ? &b->prof : nullptr);
+            if (g.error != cudaSuccess) {
+                cudaError_t e = g.error;
+                g.error = cudaSuccess;
+                return bcuda(b, e, "batch step");
+            }
+        }
+        BCK(cudaGetLastError());
+    }
+    return SPHNJ_OK;
+}
+
+int sphnj_batch_synchronize(sphnj_batch *b) {
+    if (!b) return SPHNJ_ERR_ARG;
+    cudaSetDevice(b->device);
+    for (sphnj_ctx *c : b->scenes)
+        BCK(cudaMemcpyAsync(c->h_err, c->d.err, sizeof(DevErr), cudaMemcpyDeviceToHost, b->st));
+    BCK(cudaStreamSynchronize(b->st));
+    for (size_t i = 0; i < b->scenes.size(); ++i) {
+        const int rc = device_error_status(b->scenes[i]);
+        if (rc) {
+            char buf[48];
+            snprintf(buf, sizeof buf, "scene %d: ", (int)i);
+            return bfail(b, rc, buf + b->scenes[i]->msg);
+        }
+    }
+    return SPHNJ_OK;
+}
+
+int sphnj_batch_profile_enable(sphnj_batch *b, int on) {
+    if (!b) return SPHNJ_ERR_ARG;
+    cudaSetDevice(b->device);
+    BCK(cudaStreamSynchronize(b->st));
+    b->prof.enable(on != 0);
+    return SPHNJ_OK;
+}
+
+int sphnj_batch_profile_read(sphnj_batch *b, double *ms, int64_t *calls, int64_t *kernels) {
+    if (!b) return SPHNJ_ERR_ARG;
+    cudaSetDevice(b->device);
+    BCK(cudaStreamSynchronize(b->st));
+    BCK(b->prof.collect());
+    for (int s = 0; s < ST_COUNT; ++s) {
+        if (ms) ms[s] = b->prof.ms[s];
+        if (calls) calls[s] = b->prof.calls[s];
+        if (kernels) kernels[s] = b->prof.kernels[s];
+    }
+    return SPHNJ_OK;
+}
+
+int sphnj_batch_stat_launches(const sphnj_batch *b, uint64_t *launches) {
+    if (!b || !launches) return SPHNJ_ERR_ARG;
+    *launches = b->launches;
+    return SPHNJ_OK;
+}
+
+const char *sphnj_batch_last_error(const sphnj_batch *b) { return b ? b->msg.c_str() : "null batch"; }
+
+}  // extern "C"

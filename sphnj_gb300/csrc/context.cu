@@ -14,14 +14,11 @@
 // Nothing in a step reads device data on the host: the reference's per-step
 // device-to-host copy of all fluid velocities (getMaxSpeed) is a device
 // reduction here, and every launch is asynchronous on the context stream.
-#include "kernels.h"
+#include "context.h"
 
 #include <algorithm>
 #include <cstdio>
 #include <cstring>
-#include <map>
-#include <string>
-#include <vector>
 
 using namespace sphnj;
 
@@ -81,54 +78,59 @@ void launch_fill_f32(cudaStream_t st, float *dst, float v, int n) {
 }
 }  // namespace sphnj
 
-namespace {
-enum Stage {
-    ST_BIN, ST_SORT, ST_REBUILD, ST_CAPACITY, ST_SOLID_COUPLE, ST_VIRT_DATA, ST_FLUID_PAIR, ST_FLUID_UPDATE,
-    ST_SOLID_DEFORM, ST_SOLID_FORCE, ST_SOLID_UPDATE, ST_SHIFT_GRADIENT, ST_SHIFT_UPDATE, ST_COUNT
-};
-const char *kStageNames[ST_COUNT] = {"bin", "sort", "rebuild", "capacity", "solid_couple", "virt_data",
-                                     "fluid_pair", "fluid_update", "solid_deformation", "solid_force",
-                                     "solid_update", "shift_gradient", "shift_update"};
-struct ProfRec {
-    int stage, kernels;
-    cudaEvent_t a, b;
-};
-struct StepGraph {
-    cudaGraphExec_t exec;
-    int kernels;
-};
-}  // namespace
+namespace sphnj {
 
-struct sphnj_ctx {
-    sphnj_params p;
-    // measurement
-    bool prof = false;
-    std::vector<ProfRec> pending;
-    std::vector<cudaEvent_t> pool;
-    double prof_ms[ST_COUNT] = {};
-    int64_t prof_calls[ST_COUNT] = {}, prof_kernels[ST_COUNT] = {};
-    uint64_t launches = 0;
-    int form = SPHNJ_FORM_PLAIN;
-    int device = 0;
-    cudaStream_t own = nullptr, st = nullptr;
-    char *arena = nullptr;
-    size_t arena_bytes = 0;
-    DevState d{};
-    CellList lf[2]{}, ls[2]{}, lv{};
-    ListScratch sc{};
-    void *payload = nullptr;
-    DevErr *h_err = nullptr;  // pinned
-    int step = 0;
-    int parity = 0;
-    bool virt_sorted = false;
-    bool virt_cells_valid = false;  // virtual cell ids computed since the last upload
-    bool uploaded = false;
-    int *f_listed_total = nullptr;
-    TileConfig tiles;
-    bool use_graphs = true;  // replay each kind of step as a captured CUDA graph
-    std::map<int, StepGraph> graphs;
-    std::string msg = "ok";
-};
+const char *const kStageNames[ST_COUNT] = {"bin", "sort", "rebuild", "capacity", "solid_couple", "virt_data",
+                                           "fluid_pair", "fluid_update", "solid_deformation", "solid_force",
+                                           "solid_update", "shift_gradient", "shift_update"};
+
+cudaEvent_t Profiler::take() {
+    if (!pool.empty()) {
+        cudaEvent_t e = pool.back();
+        pool.pop_back();
+        return e;
+    }
+    cudaEvent_t e = nullptr;
+    cudaEventCreate(&e);
+    return e;
+}
+
+void Profiler::enable(bool v) {
+    for (auto &r : pending) {
+        pool.push_back(r.a);
+        pool.push_back(r.b);
+    }
+    pending.clear();
+    on = v;
+    for (int s = 0; s < ST_COUNT; ++s) ms[s] = 0.0, calls[s] = kernels[s] = 0;
+}
+
+cudaError_t Profiler::collect() {
+    for (auto &r : pending) {
+        float t = 0.0f;
+        cudaError_t e = cudaEventElapsedTime(&t, r.a, r.b);
+        if (e != cudaSuccess) return e;
+        ms[r.stage] += t;
+        calls[r.stage] += 1;
+        kernels[r.stage] += r.kernels;
+        pool.push_back(r.a);
+        pool.push_back(r.b);
+    }
+    pending.clear();
+    return cudaSuccess;
+}
+
+void Profiler::release() {
+    for (auto &r : pending) {
+        cudaEventDestroy(r.a);
+        cudaEventDestroy(r.b);
+    }
+    pending.clear();
+    for (auto e : pool) cudaEventDestroy(e);
+    pool.clear();
+}
+
+}  // namespace sphnj
 
 namespace {
 
@@ -195,29 +197,43 @@ size_t layout(sphnj_ctx *ctx, char *base) {
     return a.off;
 }
 
-void bind_lists(sphnj_ctx *ctx) {
-    ctx->d.rng_f = ctx->lf[ctx->parity].rng;
-    ctx->d.lst_f = ctx->lf[ctx->parity].lst;
-    ctx->d.rng_s = ctx->ls[ctx->parity].rng;
-    ctx->d.lst_s = ctx->ls[ctx->parity].lst;
-    ctx->d.rng_v = ctx->lv.rng;
-    ctx->d.lst_v = ctx->lv.lst;
+void bind_lists(const sphnj_ctx *ctx, DevState &d, int parity) {
+    d.rng_f = ctx->lf[parity].rng;
+    d.lst_f = ctx->lf[parity].lst;
+    d.rng_s = ctx->ls[parity].rng;
+    d.lst_s = ctx->ls[parity].lst;
+    d.rng_v = ctx->lv.rng;
+    d.lst_v = ctx->lv.lst;
 }
+void bind_lists(sphnj_ctx *ctx) { bind_lists(ctx, ctx->d, ctx->parity); }
 
-cudaEvent_t take_event(sphnj_ctx *ctx) {
-    if (!ctx->pool.empty()) {
-        cudaEvent_t e = ctx->pool.back();
-        ctx->pool.pop_back();
-        return e;
+}  // namespace
+
+namespace sphnj {
+
+Scene scene_of(const sphnj_ctx *ctx, int parity) {
+    Scene s{};
+    s.p = ctx->p;
+    s.d = ctx->d;
+    bind_lists(ctx, s.d, parity);
+    for (int k = 0; k < 2; ++k) {
+        s.lf[k] = ctx->lf[k];
+        s.ls[k] = ctx->ls[k];
     }
-    cudaEvent_t e = nullptr;
-    cudaEventCreate(&e);
-    return e;
+    s.lv = ctx->lv;
+    s.sc = ctx->sc;
+    s.payload = static_cast<char *>(ctx->payload);
+    s.f_listed_total = ctx->f_listed_total;
+    return s;
 }
 
 int check_device_error(sphnj_ctx *ctx) {
     CK(cudaMemcpyAsync(ctx->h_err, ctx->d.err, sizeof(DevErr), cudaMemcpyDeviceToHost, ctx->st));
     CK(cudaStreamSynchronize(ctx->st));
+    return device_error_status(ctx);
+}
+
+int device_error_status(sphnj_ctx *ctx) {
     const DevErr &e = *ctx->h_err;
     if (e.code == 0) return SPHNJ_OK;
     char buf[256];
@@ -235,6 +251,10 @@ int check_device_error(sphnj_ctx *ctx) {
     }
     return fail(ctx, e.code, buf);
 }
+
+}  // namespace sphnj
+
+namespace {
 
 template <class T> int h2d(sphnj_ctx *ctx, T *dst, const void *src, size_t n) {
     if (n == 0) return SPHNJ_OK;
@@ -325,11 +345,7 @@ void sphnj_destroy(sphnj_ctx *ctx) {
     if (!ctx) return;
     cudaSetDevice(ctx->device);
     if (ctx->st) cudaStreamSynchronize(ctx->st);
-    for (auto &r : ctx->pending) {
-        cudaEventDestroy(r.a);
-        cudaEventDestroy(r.b);
-    }
-    for (auto e : ctx->pool) cudaEventDestroy(e);
+    ctx->prof.release();
     for (auto &g : ctx->graphs) cudaGraphExecDestroy(g.second.exec);
     if (ctx->arena) cudaFree(ctx->arena);
     if (ctx->h_err) cudaFreeHost(ctx->h_err);
@@ -339,6 +355,7 @@ void sphnj_destroy(sphnj_ctx *ctx) {
 
 int sphnj_set_stream(sphnj_ctx *ctx, void *stream) {
     if (!ctx) return SPHNJ_ERR_ARG;
+    if (ctx->batch) return fail(ctx, SPHNJ_ERR_ARG, "the scene is in a batch: set the batch's stream");
     cudaSetDevice(ctx->device);
     CK(cudaStreamSynchronize(ctx->st));
     ctx->st = stream ? static_cast<cudaStream_t>(stream) : ctx->own;
@@ -408,98 +425,78 @@ int sphnj_upload(sphnj_ctx *ctx, const sphnj_host_state *s) {
     bind_lists(ctx);
     // wall normals once before the loop (virtNormalCalculation, calculation.cu:28)
     if (s->virt_normal) RET(h2d(ctx, d.v_normal, s->virt_normal, nv));
-    else launch_virt_normal(st, p, d);
+    else {
+        GroupOne g{scene_of(ctx, ctx->parity)};
+        launch_virt_normal(st, g);
+    }
     CK(cudaGetLastError());
     CK(cudaStreamSynchronize(st));
     ctx->uploaded = true;
     return SPHNJ_OK;
 }
 
-namespace {
+}  // extern "C"
 
-// What distinguishes the launch sequence of one step from another.
-struct StepKind {
-    bool is_sort, bin_virt, sort_virt;
-    int parity;  // list buffer that this step writes and reads
-    int key() const { return (is_sort ? 1 : 0) | (bin_virt ? 2 : 0) | (sort_virt ? 4 : 0) | (parity << 3); }
-};
+namespace sphnj {
 
-// Issues the launches of one step on the context stream; returns the number
-// of kernels launched.  Reads no host-side state that changes from step to
-// step except through `k`, so the sequence can be captured into a graph.
-int issue_step(sphnj_ctx *ctx, const StepKind &k) {
-    const sphnj_params &p = ctx->p;
-    const int nf = p.fluid_number_total, ns = p.solid_number, nv = p.virt_number;
-    cudaStream_t st = ctx->st;
-    const DevState &d = ctx->d;
-    constexpr int kSortKernels = 7, kRebuildKernels = 4;  // kernels each launcher issues (kernels_cells.cu)
-    const int sweep_kernels = ctx->tiles.tiled ? 2 : 1;   // tiled sweep + fallback for unlisted particles
+template <class G> int issue_step(G &g, const StepKind &k, cudaStream_t st, const TileConfig &tc, Profiler *prof) {
     int launched = 0;
-    auto stage = [&](int s, int kernels, auto &&fn) {
-        ProfRec r{s, kernels, nullptr, nullptr};
-        if (ctx->prof) {
-            r.a = take_event(ctx);
-            r.b = take_event(ctx);
+    auto stage = [&](int s, auto &&fn) {
+        Profiler::Rec r{s, 0, nullptr, nullptr};
+        if (prof) {
+            r.a = prof->take();
+            r.b = prof->take();
             cudaEventRecord(r.a, st);
         }
-        fn();
-        if (ctx->prof) {
+        r.kernels = fn();
+        if (prof) {
             cudaEventRecord(r.b, st);
-            ctx->pending.push_back(r);
+            prof->pending.push_back(r);
         }
-        launched += kernels;
+        launched += r.kernels;
     };
-    const Listing lgf{d.f_listed, d.stamp, ctx->f_listed_total};
-    stage(ST_BIN, 1, [&] { launch_bin(st, p, d, k.bin_virt); });
+    auto fluid = [](const sphnj_params &p) { return p.fluid_number_total > 0; };
+    auto solid = [](const sphnj_params &p) { return p.solid_number > 0; };
+    auto virt = [](const sphnj_params &p) { return p.virt_number > 0; };
+    const bool any_fluid = g.any(fluid), any_solid = g.any(solid);
+    stage(ST_BIN, [&] { return launch_bin(st, g, k.bin_virt); });
     if (k.is_sort) {
-        if (nf > 0)
-            stage(ST_SORT, kSortKernels, [&] {
-                launch_sort_kind(st, p, d, KF, nf, d.f_cell, ctx->sc, ctx->lf[k.parity], ctx->payload, lgf);
-            });
-        if (ns > 0)
-            stage(ST_SORT, kSortKernels,
-                  [&] { launch_sort_kind(st, p, d, KS, ns, d.s_cell, ctx->sc, ctx->ls[k.parity], ctx->payload); });
-        if (k.sort_virt)
-            stage(ST_SORT, kSortKernels,
-                  [&] { launch_sort_kind(st, p, d, KV, nv, d.v_cell, ctx->sc, ctx->lv, ctx->payload); });
+        if (any_fluid) stage(ST_SORT, [&] { return launch_sort_kind(st, g, KF, k.parity); });
+        if (any_solid) stage(ST_SORT, [&] { return launch_sort_kind(st, g, KS, k.parity); });
+        if (k.sort_virt) stage(ST_SORT, [&] { return launch_sort_kind(st, g, KV, k.parity); });
     } else {
-        const int cur = k.parity, prev = cur ^ 1;
-        if (nf > 0)
-            stage(ST_REBUILD, kRebuildKernels, [&] {
-                launch_rebuild_kind(st, p, nf, d.f_cell, ctx->lf[prev], ctx->lf[cur], ctx->sc, d.err, lgf);
-            });
-        if (ns > 0)
-            stage(ST_REBUILD, kRebuildKernels,
-                  [&] { launch_rebuild_kind(st, p, ns, d.s_cell, ctx->ls[prev], ctx->ls[cur], ctx->sc, d.err); });
+        if (any_fluid) stage(ST_REBUILD, [&] { return launch_rebuild_kind(st, g, KF, k.parity); });
+        if (any_solid) stage(ST_REBUILD, [&] { return launch_rebuild_kind(st, g, KS, k.parity); });
     }
-    stage(ST_CAPACITY, 1, [&] { launch_capacity_check(st, p, d); });
-    if (nf > 0 && ns > 0) stage(ST_SOLID_COUPLE, 1, [&] { launch_solid_couple(st, p, d); });
-    if (nv > 0) stage(ST_VIRT_DATA, 1, [&] { launch_virt_data(st, p, d); });
-    if (nf > 0) {
-        stage(ST_FLUID_PAIR, sweep_kernels, [&] { launch_fluid_pair(st, p, d, ctx->tiles); });
-        stage(ST_FLUID_UPDATE, 1, [&] { launch_fluid_update(st, p, d); });
+    stage(ST_CAPACITY, [&] { return launch_capacity_check(st, g); });
+    if (g.any([](const sphnj_params &p) { return p.fluid_number_total > 0 && p.solid_number > 0; }))
+        stage(ST_SOLID_COUPLE, [&] { return launch_solid_couple(st, g); });
+    if (g.any(virt)) stage(ST_VIRT_DATA, [&] { return launch_virt_data(st, g); });
+    if (any_fluid) {
+        stage(ST_FLUID_PAIR, [&] { return launch_fluid_pair(st, g, tc); });
+        stage(ST_FLUID_UPDATE, [&] { return launch_fluid_update(st, g); });
     }
-    if (ns > 0)
-        for (int s = 0; s < p.solid_sub_step; ++s) {
-            stage(ST_SOLID_DEFORM, 1, [&] { launch_solid_deformation(st, p, d); });
-            stage(ST_SOLID_FORCE, 1, [&] { launch_solid_force(st, p, d); });
-            stage(ST_SOLID_UPDATE, 1, [&] { launch_solid_update(st, p, d); });
-        }
-    if (nf > 0)
-        for (int s = 0; s < p.shift_per_step; ++s) {
-            stage(ST_SHIFT_GRADIENT, sweep_kernels, [&] { launch_shift_gradient(st, p, d, ctx->tiles, s); });
-            stage(ST_SHIFT_UPDATE, 1, [&] { launch_shift_update(st, p, d, s); });
-        }
+    int subs = 0, shifts = 0;
+    g.any([&](const sphnj_params &p) {
+        if (p.solid_number > 0) subs = std::max(subs, p.solid_sub_step);
+        if (p.fluid_number_total > 0) shifts = std::max(shifts, p.shift_per_step);
+        return false;
+    });
+    for (int s = 0; s < subs; ++s) {
+        stage(ST_SOLID_DEFORM, [&] { return launch_solid_deformation(st, g, s); });
+        stage(ST_SOLID_FORCE, [&] { return launch_solid_force(st, g, s); });
+        stage(ST_SOLID_UPDATE, [&] { return launch_solid_update(st, g, s); });
+    }
+    for (int s = 0; s < shifts; ++s) {
+        stage(ST_SHIFT_GRADIENT, [&] { return launch_shift_gradient(st, g, tc, s); });
+        stage(ST_SHIFT_UPDATE, [&] { return launch_shift_update(st, g, s); });
+    }
     return launched;
 }
 
-void drop_graphs(sphnj_ctx *ctx) {
-    for (auto &g : ctx->graphs) cudaGraphExecDestroy(g.second.exec);
-    ctx->graphs.clear();
-}
+template int issue_step<GroupOne>(GroupOne &, const StepKind &, cudaStream_t, const TileConfig &, Profiler *);
+template int issue_step<GroupMany>(GroupMany &, const StepKind &, cudaStream_t, const TileConfig &, Profiler *);
 
-// Advances the host-side step state of ctx by one step and returns the kind
-// of launch sequence that step needs.
 StepKind advance(sphnj_ctx *ctx) {
     const sphnj_params &p = ctx->p;
     ctx->step++;
@@ -519,6 +516,15 @@ StepKind advance(sphnj_ctx *ctx) {
     return k;
 }
 
+}  // namespace sphnj
+
+namespace {
+
+void drop_graphs(sphnj_ctx *ctx) {
+    for (auto &g : ctx->graphs) cudaGraphExecDestroy(g.second.exec);
+    ctx->graphs.clear();
+}
+
 }  // namespace
 
 extern "C" int sphnj_step(sphnj_ctx *ctx, int n) {
@@ -528,30 +534,33 @@ extern "C" int sphnj_step(sphnj_ctx *ctx, int n) {
     cudaStream_t st = ctx->st;
     for (int it = 0; it < n; ++it) {
         const StepKind k = advance(ctx);
-        if (ctx->use_graphs && !ctx->prof) {
+        GroupOne g{scene_of(ctx, k.parity)};
+        if (ctx->use_graphs && !ctx->prof.on) {
             auto it_g = ctx->graphs.find(k.key());
             if (it_g == ctx->graphs.end()) {
-                cudaGraph_t g = nullptr;
+                cudaGraph_t graph = nullptr;
                 CK(cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal));
-                const int launched = issue_step(ctx, k);
-                cudaError_t e = cudaStreamEndCapture(st, &g);
+                const int launched = issue_step(g, k, st, ctx->tiles, nullptr);
+                cudaError_t e = cudaStreamEndCapture(st, &graph);
                 cudaGraphExec_t exec = nullptr;
-                if (e == cudaSuccess) e = cudaGraphInstantiate(&exec, g, 0);
-                if (g) cudaGraphDestroy(g);
+                if (e == cudaSuccess) e = cudaGraphInstantiate(&exec, graph, 0);
+                if (graph) cudaGraphDestroy(graph);
                 if (e != cudaSuccess) return cuda_fail(ctx, e, "step graph capture");
                 it_g = ctx->graphs.emplace(k.key(), StepGraph{exec, launched}).first;
             }
             CK(cudaGraphLaunch(it_g->second.exec, st));
             ctx->launches += (uint64_t)it_g->second.kernels;
         } else {
-            ctx->launches += (uint64_t)issue_step(ctx, k);
+            ctx->launches += (uint64_t)issue_step(g, k, st, ctx->tiles, ctx->prof.on ? &ctx->prof : nullptr);
         }
         CK(cudaGetLastError());
     }
     return SPHNJ_OK;
 }
 
-extern "C" int sphnj_set_graphs(sphnj_ctx *ctx, int on) {
+extern "C" {
+
+int sphnj_set_graphs(sphnj_ctx *ctx, int on) {
     if (!ctx) return SPHNJ_ERR_ARG;
     cudaSetDevice(ctx->device);
     CK(cudaStreamSynchronize(ctx->st));
@@ -637,13 +646,7 @@ int sphnj_profile_enable(sphnj_ctx *ctx, int on) {
     if (!ctx) return SPHNJ_ERR_ARG;
     cudaSetDevice(ctx->device);
     CK(cudaStreamSynchronize(ctx->st));
-    for (auto &r : ctx->pending) {
-        ctx->pool.push_back(r.a);
-        ctx->pool.push_back(r.b);
-    }
-    ctx->pending.clear();
-    ctx->prof = on != 0;
-    for (int s = 0; s < ST_COUNT; ++s) ctx->prof_ms[s] = 0.0, ctx->prof_calls[s] = ctx->prof_kernels[s] = 0;
+    ctx->prof.enable(on != 0);
     return SPHNJ_OK;
 }
 
@@ -651,20 +654,11 @@ int sphnj_profile_read(sphnj_ctx *ctx, double *ms, int64_t *calls, int64_t *kern
     if (!ctx) return SPHNJ_ERR_ARG;
     cudaSetDevice(ctx->device);
     CK(cudaStreamSynchronize(ctx->st));
-    for (auto &r : ctx->pending) {
-        float t = 0.0f;
-        CK(cudaEventElapsedTime(&t, r.a, r.b));
-        ctx->prof_ms[r.stage] += t;
-        ctx->prof_calls[r.stage] += 1;
-        ctx->prof_kernels[r.stage] += r.kernels;
-        ctx->pool.push_back(r.a);
-        ctx->pool.push_back(r.b);
-    }
-    ctx->pending.clear();
+    CK(ctx->prof.collect());
     for (int s = 0; s < ST_COUNT; ++s) {
-        if (ms) ms[s] = ctx->prof_ms[s];
-        if (calls) calls[s] = ctx->prof_calls[s];
-        if (kernels) kernels[s] = ctx->prof_kernels[s];
+        if (ms) ms[s] = ctx->prof.ms[s];
+        if (calls) calls[s] = ctx->prof.calls[s];
+        if (kernels) kernels[s] = ctx->prof.kernels[s];
     }
     return SPHNJ_OK;
 }

@@ -1,0 +1,97 @@
+// Internal state of a libsphnj context (one scene) and the pieces of the step
+// sequencer that a batch of scenes shares with it.
+#pragma once
+
+#include <cstdint>
+#include <map>
+#include <string>
+#include <vector>
+
+#include "kernels.h"
+
+namespace sphnj {
+
+enum Stage {
+    ST_BIN, ST_SORT, ST_REBUILD, ST_CAPACITY, ST_SOLID_COUPLE, ST_VIRT_DATA, ST_FLUID_PAIR, ST_FLUID_UPDATE,
+    ST_SOLID_DEFORM, ST_SOLID_FORCE, ST_SOLID_UPDATE, ST_SHIFT_GRADIENT, ST_SHIFT_UPDATE, ST_COUNT
+};
+extern const char *const kStageNames[ST_COUNT];
+
+// Per-stage device times from CUDA events recorded around each stage on the
+// launching stream (steps are issued directly, not as graphs, while on).
+struct Profiler {
+    struct Rec {
+        int stage, kernels;
+        cudaEvent_t a, b;
+    };
+    bool on = false;
+    std::vector<Rec> pending;
+    std::vector<cudaEvent_t> pool;
+    double ms[ST_COUNT] = {};
+    int64_t calls[ST_COUNT] = {}, kernels[ST_COUNT] = {};
+    cudaEvent_t take();
+    void enable(bool v);                  // stream synchronised by the caller
+    cudaError_t collect();                // stream synchronised by the caller
+    void release();
+};
+
+struct StepGraph {
+    cudaGraphExec_t exec;
+    int kernels;
+};
+
+// What distinguishes the launch sequence of one step from another.
+struct StepKind {
+    bool is_sort, bin_virt, sort_virt;
+    int parity;  // list buffer that this step writes and reads
+    int key() const { return (is_sort ? 1 : 0) | (bin_virt ? 2 : 0) | (sort_virt ? 4 : 0) | (parity << 3); }
+};
+
+// Issues the launches of one step of every scene of g on stream st; returns
+// the number of kernels launched.  Reads no host state that changes from
+// step to step except through `k`, so the sequence can be captured.
+template <class G> int issue_step(G &g, const StepKind &k, cudaStream_t st, const TileConfig &tc, Profiler *prof);
+
+}  // namespace sphnj
+
+struct sphnj_ctx {
+    sphnj_params p;
+    sphnj::Profiler prof;
+    uint64_t launches = 0;
+    int form = SPHNJ_FORM_PLAIN;
+    int device = 0;
+    cudaStream_t own = nullptr, st = nullptr;
+    char *arena = nullptr;
+    size_t arena_bytes = 0;
+    sphnj::DevState d{};
+    sphnj::CellList lf[2]{}, ls[2]{}, lv{};
+    sphnj::ListScratch sc{};
+    void *payload = nullptr;
+    sphnj::DevErr *h_err = nullptr;  // pinned
+    int step = 0;
+    int parity = 0;
+    bool virt_sorted = false;
+    bool virt_cells_valid = false;  // virtual cell ids computed since the last upload
+    bool uploaded = false;
+    int *f_listed_total = nullptr;
+    sphnj::TileConfig tiles;
+    bool use_graphs = true;  // replay each kind of step as a captured CUDA graph
+    std::map<int, sphnj::StepGraph> graphs;
+    sphnj_batch *batch = nullptr;  // the batch this scene belongs to, if any
+    std::string msg = "ok";
+};
+
+namespace sphnj {
+
+// The scene record of ctx with the cell lists of buffer `parity` bound.
+Scene scene_of(const sphnj_ctx *ctx, int parity);
+// Advances the host-side step state of ctx by one step and returns the kind
+// of launch sequence that step needs.
+StepKind advance(sphnj_ctx *ctx);
+// Copies the device error record of ctx to the host (synchronising its
+// stream) and turns it into a status and message.
+int check_device_error(sphnj_ctx *ctx);
+// The status and message of the device error record last copied to the host.
+int device_error_status(sphnj_ctx *ctx);
+
+}  // namespace sphnj

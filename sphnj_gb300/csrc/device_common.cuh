@@ -161,4 +161,83 @@ constexpr int SCAN_MAX_TILES = 4096;  // => up to 4M cells per scene
 
 inline unsigned grid_for(long n, int block) { return (unsigned)((n + block - 1) / block); }
 
+// CSR cell list of one particle kind
+struct CellList {
+    int2 *rng;  // [C] {start, count}
+    int *lst;   // [N] particle indices, cell by cell
+};
+
+// Scratch for sorting / list rebuilding of one particle kind
+struct ListScratch {
+    int *cnt9;    // [9*C] per (destination cell, neighbour slot) counts
+    int *cnt;     // [C]
+    int *local;   // [C] tile-local exclusive prefix
+    int *sums;    // [SCAN_MAX_TILES] tile sums (scanned in place)
+    int *cursor;  // [C]
+    int *bucket;  // [N]
+    int *sorted;  // [N]
+};
+
+// kinds
+enum Kind { KF = 0, KS = 1, KV = 2 };
+
+// Everything a kernel reads about one scene: its parameters, its state (with
+// the current cell lists bound in `d`), both list buffers of each kind, and
+// its sort / rebuild scratch.
+struct Scene {
+    sphnj_params p;
+    DevState d;
+    CellList lf[2], ls[2], lv;
+    ListScratch sc;
+    char *payload;        // sort payload staging
+    int *f_listed_total;  // fluid particles in the current lists (written by the list scans)
+};
+
+// Where a block finds its scene.  Every kernel of the step is a template over
+// one of the two, and starts with SPHNJ_SCENE(g), which defines
+//   blk, nblk  the block's index among its scene's blocks, and their number
+//   S, p, d    the scene record, its parameters and its state.
+//
+// One: a launch over one scene, the record a __grid_constant__ kernel
+// parameter (read in place from parameter space).
+struct One {
+    Scene s;
+    __device__ __forceinline__ const Scene *locate(int &blk, int &nblk) const {
+        blk = blockIdx.x;
+        nblk = gridDim.x;
+        return &s;
+    }
+};
+
+// Many: one launch over many scenes.  Scene k owns the blocks
+// first[k] <= b < first[k + 1]; first[n] is the grid size, and a scene with
+// no work for this launch owns no block.
+struct Many {
+    const Scene *scenes;
+    const int *first;  // [n + 1]
+    int n;
+    __device__ __forceinline__ const Scene *locate(int &blk, int &nblk) const {
+        const int b = blockIdx.x;
+        int lo = 0, hi = n;  // first[lo] <= b < first[hi]
+        while (hi - lo > 1) {
+            const int mid = (lo + hi) >> 1;
+            if (__ldg(&first[mid]) <= b) lo = mid;
+            else hi = mid;
+        }
+        const int f0 = __ldg(&first[lo]);
+        blk = b - f0;
+        nblk = __ldg(&first[lo + 1]) - f0;
+        return scenes + lo;
+    }
+};
+
+#define SPHNJ_SCENE(g)                                   \
+    int blk, nblk;                                       \
+    const ::sphnj::Scene &S = *(g).locate(blk, nblk);    \
+    const sphnj_params &p = S.p;                         \
+    const ::sphnj::DevState &d = S.d;                    \
+    (void)nblk;                                          \
+    (void)p;                                             \
+    (void)d
+
 }  // namespace sphnj

@@ -1,59 +1,25 @@
 // Host-side launchers for the sm_103a kernels of libsphnj.  Each wraps one
-// or more kernel launches on the given stream; none synchronises.
+// or more kernel launches on the given stream, returns how many kernels it
+// launched, and never synchronises.
+//
+// Every launcher is a template over the group of scenes it advances:
+//   GroupOne   one scene; its record travels as a kernel parameter.
+//   GroupMany  a batch of independent scenes advanced by the same launches:
+//              the records live in device memory and each launch gets a
+//              per-scene block table (scene k owns blocks first[k] ..
+//              first[k+1]-1), so one launch covers every scene and a scene
+//              with no work for it owns no block.
 #pragma once
 
 #include <cuda_runtime.h>
 
+#include <map>
+#include <utility>
+#include <vector>
+
 #include "device_common.cuh"
 
 namespace sphnj {
-
-// CSR cell list of one particle kind
-struct CellList {
-    int2 *rng;  // [C] {start, count}
-    int *lst;   // [N] particle indices, cell by cell
-};
-
-// Scratch for sorting / list rebuilding of one particle kind
-struct ListScratch {
-    int *cnt9;    // [9*C] per (destination cell, neighbour slot) counts
-    int *cnt;     // [C]
-    int *local;   // [C] tile-local exclusive prefix
-    int *sums;    // [SCAN_MAX_TILES] tile sums (scanned in place)
-    int *cursor;  // [C]
-    int *bucket;  // [N]
-    int *sorted;  // [N]
-};
-
-// kinds
-enum Kind { KF = 0, KS = 1, KV = 2 };
-
-// Which particles a list build placed in some cell list: listed[i] = stamp
-// for each of them, and *total = their number.  The tiled neighbour sweeps
-// process listed particles cell by cell; particles that dropped out of every
-// list (a jump of more than one cell between sorts) are processed by the
-// per-particle fallback kernels.  Null members: nothing recorded.
-struct Listing {
-    int *listed = nullptr;
-    const int *stamp = nullptr;  // device value of this step's stamp
-    int *total = nullptr;
-};
-
-// cells: cell ids of every particle (pair.cu:20-64); also resets the
-// per-step max-speed accumulator.
-void launch_bin(cudaStream_t st, const sphnj_params &p, const DevState &d, bool with_virt);
-
-// stable sort of one kind by cell id + identity cell lists (sort.cu:10-137)
-void launch_sort_kind(cudaStream_t st, const sphnj_params &p, const DevState &d, Kind k, int n, int *cell,
-                      ListScratch sc, CellList cur, void *payload_scratch, Listing lg = Listing());
-
-// incremental cell-list rebuild of one kind from its previous lists
-// (pair.cu:66-181)
-void launch_rebuild_kind(cudaStream_t st, const sphnj_params &p, int n, const int *cell, CellList prev,
-                         CellList cur, ListScratch sc, DevErr *err, Listing lg = Listing());
-
-// per-cell capacity check against the reference's 64 slots
-void launch_capacity_check(cudaStream_t st, const sphnj_params &p, const DevState &d);
 
 // How the fluid neighbour sweeps are launched: tiled (a block per column
 // segment of tile_h cells, neighbours staged in shared memory) or one thread
@@ -63,27 +29,141 @@ struct TileConfig {
     int tile_h = 16;
 };
 
+// Launch sites: a batch keeps one block table per (site, argument).
+enum Site : int {
+    SITE_BIN, SITE_SORT_CLEAR, SITE_SORT_N, SITE_SORT_TILES, SITE_SORT_ONE, SITE_SORT_CELLS32,
+    SITE_REBUILD_CELLS, SITE_REBUILD_TILES, SITE_REBUILD_ONE, SITE_CAPACITY, SITE_COUPLE, SITE_VIRT_NORMAL,
+    SITE_VIRT_DATA, SITE_PAIR_TILED, SITE_PAIR_EACH, SITE_PAIR_FALLBACK, SITE_FLUID_UPDATE, SITE_SOLID_DEFORM,
+    SITE_SOLID_FORCE, SITE_SOLID_UPDATE, SITE_SHIFT_TILED, SITE_SHIFT_EACH, SITE_SHIFT_FALLBACK,
+    SITE_SHIFT_UPDATE
+};
+inline long long site_key(int site, int arg = 0) { return ((long long)site << 32) | (unsigned)arg; }
+
+struct GroupOne {
+    using Dev = One;
+    Scene s;
+    template <class F> bool prepare(long long, F &&blocks_of, unsigned &blocks, Dev &dev) {
+        blocks = blocks_of(s);
+        dev.s = s;
+        return blocks > 0;
+    }
+    template <class Pred> bool any(Pred &&pr) const { return pr(s.p); }
+};
+
+struct GroupMany {
+    using Dev = Many;
+    const Scene *h_scenes = nullptr;  // host copies of the records in d_scenes
+    int n = 0;
+    const Scene *d_scenes = nullptr;  // device records of the current parity
+    // With `planning` set, prepare() builds the block table of each launch
+    // (synchronous allocation and copy) and launches nothing; a launch
+    // sequence is planned once before it is captured into a graph.
+    bool planning = false;
+    struct Table {
+        int *first;
+        unsigned total;
+    };
+    std::map<long long, Table> tables;
+    cudaError_t error = cudaSuccess;
+    template <class F> bool prepare(long long key, F &&blocks_of, unsigned &blocks, Dev &dev) {
+        auto it = tables.find(key);
+        if (it == tables.end()) {
+            if (!planning) {
+                if (error == cudaSuccess) error = cudaErrorNotReady;  // launch not planned
+                return false;
+            }
+            std::vector<int> first((size_t)n + 1, 0);
+            long long acc = 0;
+            for (int k = 0; k < n; ++k) {
+                first[k] = (int)acc;
+                acc += blocks_of(h_scenes[k]);
+            }
+            first[n] = (int)acc;
+            Table t{nullptr, (unsigned)acc};
+            if (acc > 0x7fffffffLL) {
+                error = cudaErrorInvalidValue;
+                return false;
+            }
+            cudaError_t e = cudaMalloc(&t.first, sizeof(int) * first.size());
+            if (e == cudaSuccess) e = cudaMemcpy(t.first, first.data(), sizeof(int) * first.size(),
+                                                 cudaMemcpyHostToDevice);
+            if (e != cudaSuccess) {
+                if (t.first) cudaFree(t.first);
+                error = e;
+                return false;
+            }
+            it = tables.emplace(key, t).first;
+        }
+        if (planning) return false;
+        blocks = it->second.total;
+        dev.scenes = d_scenes;
+        dev.first = it->second.first;
+        dev.n = n;
+        return blocks > 0;
+    }
+    template <class Pred> bool any(Pred &&pr) const {
+        for (int k = 0; k < n; ++k)
+            if (pr(h_scenes[k].p)) return true;
+        return false;
+    }
+    void free_tables() {
+        for (auto &t : tables) cudaFree(t.second.first);
+        tables.clear();
+    }
+};
+
+// Launches `kern` over the blocks that blocks_of(scene) gives each scene of
+// the group; returns 1 when something was launched.
+template <class G, class F, class... P, class... A>
+int launch(G &g, long long key, F &&blocks_of, void (*kern)(typename G::Dev, P...), int threads, size_t smem,
+           cudaStream_t st, A &&...a) {
+    unsigned blocks = 0;
+    typename G::Dev dev;
+    if (!g.prepare(key, blocks_of, blocks, dev)) return 0;
+    kern<<<blocks, threads, smem, st>>>(dev, std::forward<A>(a)...);
+    return 1;
+}
+
+__host__ __device__ inline int count_of(const sphnj_params &p, Kind k) {
+    return k == KF ? p.fluid_number_total : k == KS ? p.solid_number : p.virt_number;
+}
+
+// cells: cell ids of every particle (pair.cu:20-64); also resets the
+// per-step accumulators and advances the list stamp.
+template <class G> int launch_bin(cudaStream_t st, G &g, bool with_virt);
+
+// stable sort of one kind by cell id + identity cell lists written to list
+// buffer `parity` (sort.cu:10-137)
+template <class G> int launch_sort_kind(cudaStream_t st, G &g, Kind k, int parity);
+
+// incremental cell-list rebuild of one kind from list buffer parity ^ 1 into
+// list buffer `parity` (pair.cu:66-181)
+template <class G> int launch_rebuild_kind(cudaStream_t st, G &g, Kind k, int parity);
+
+// per-cell capacity check against the reference's 64 slots
+template <class G> int launch_capacity_check(cudaStream_t st, G &g);
+
 // Function attributes the sweeps need for this configuration (dynamic shared
 // memory above 48 KB); called outside any stream capture.
 cudaError_t configure_sweeps(const TileConfig &tc);
 
 // fluid passes (fluid.cu)
-void launch_fluid_pair(cudaStream_t st, const sphnj_params &p, const DevState &d, const TileConfig &tc);
-void launch_fluid_update(cudaStream_t st, const sphnj_params &p, const DevState &d);
-// pass = index of the shifting pass within the step (0..shift_per_step-1)
-void launch_shift_gradient(cudaStream_t st, const sphnj_params &p, const DevState &d, const TileConfig &tc,
-                           int pass);
-void launch_shift_update(cudaStream_t st, const sphnj_params &p, const DevState &d, int pass);
+template <class G> int launch_fluid_pair(cudaStream_t st, G &g, const TileConfig &tc);
+template <class G> int launch_fluid_update(cudaStream_t st, G &g);
+// pass = index of the shifting pass within the step; scenes with fewer
+// shifting passes per step own no block of it
+template <class G> int launch_shift_gradient(cudaStream_t st, G &g, const TileConfig &tc, int pass);
+template <class G> int launch_shift_update(cudaStream_t st, G &g, int pass);
 
 // virtual particles (virt.cu)
-void launch_virt_normal(cudaStream_t st, const sphnj_params &p, const DevState &d);
-void launch_virt_data(cudaStream_t st, const sphnj_params &p, const DevState &d);
+template <class G> int launch_virt_normal(cudaStream_t st, G &g);
+template <class G> int launch_virt_data(cudaStream_t st, G &g);
 
-// solid (solid.cu)
-void launch_solid_couple(cudaStream_t st, const sphnj_params &p, const DevState &d);
-void launch_solid_deformation(cudaStream_t st, const sphnj_params &p, const DevState &d);
-void launch_solid_force(cudaStream_t st, const sphnj_params &p, const DevState &d);
-void launch_solid_update(cudaStream_t st, const sphnj_params &p, const DevState &d);
+// solid (solid.cu); sub = index of the solid sub-step within the fluid step
+template <class G> int launch_solid_couple(cudaStream_t st, G &g);
+template <class G> int launch_solid_deformation(cudaStream_t st, G &g, int sub);
+template <class G> int launch_solid_force(cudaStream_t st, G &g, int sub);
+template <class G> int launch_solid_update(cudaStream_t st, G &g, int sub);
 
 // state conversion helpers (upload / download of 32-bit enums)
 void launch_u8_from_i32(cudaStream_t st, uint8_t *dst, const int32_t *src, int n);
@@ -91,5 +171,9 @@ void launch_i32_from_u8(cudaStream_t st, int32_t *dst, const uint8_t *src, int n
 void launch_fill_u8(cudaStream_t st, uint8_t *dst, uint8_t v, int n);
 void launch_fill_dmat2(cudaStream_t st, dmat2 *dst, dmat2 v, int n);
 void launch_fill_f32(cudaStream_t st, float *dst, float v, int n);
+
+#define SPHNJ_INSTANTIATE_GROUPS(fn, ...)                 \
+    template int fn<GroupOne>(cudaStream_t, GroupOne &, ##__VA_ARGS__); \
+    template int fn<GroupMany>(cudaStream_t, GroupMany &, ##__VA_ARGS__)
 
 }  // namespace sphnj

@@ -26,6 +26,9 @@
 //     cnt9[c][slot] (every (c,slot) pair has exactly one writer, so no
 //     atomics and no zeroing), a tiled scan gives the new cell starts, and
 //     m writes its particles to their destinations in previous-list order.
+//   - every kernel runs over one scene or a batch of scenes (SPHNJ_SCENE):
+//     each scene's scan, sort and rebuild use that scene's own scratch, so
+//     the scenes of a batch share launches but no data.
 #include "kernels.h"
 
 #include <climits>
@@ -36,15 +39,23 @@ namespace {
 
 constexpr int kBlock = 256;
 
-__global__ void k_bin(sphnj_params p, DevState d, int with_virt) {
+__device__ __forceinline__ int *cells_of(const DevState &d, int k) {
+    return k == KF ? d.f_cell : k == KS ? d.s_cell : d.v_cell;
+}
+__device__ __forceinline__ const CellList &list_of(const Scene &S, int k, int parity) {
+    return k == KF ? S.lf[parity] : k == KS ? S.ls[parity] : S.lv;
+}
+
+template <class G> __global__ void k_bin(const __grid_constant__ G g, int with_virt) {
+    SPHNJ_SCENE(g);
     const int nf = p.fluid_number_total, ns = p.solid_number, nv = with_virt ? p.virt_number : 0;
     const int C = p.cell_number_total;
-    long t = (long)blockIdx.x * blockDim.x + threadIdx.x;
+    long t = (long)blk * blockDim.x + threadIdx.x;
     if (t == 0) {
         *d.max_speed2_bits = 0u;
         *d.stamp += 1;  // this step's stamp (read by kernels launched after this one)
     }
-    if (t < 1 + kMaskShifts) d.disp2_bits[t] = 0u;  // grid has >= 256 threads
+    if (t < 1 + kMaskShifts) d.disp2_bits[t] = 0u;  // every scene has >= 256 threads
     int kind, i, c;
     if (t < nf) {
         kind = 0;
@@ -108,53 +119,61 @@ __device__ __forceinline__ bool slot_valid(int ci, int cj, int s, int nx, int ny
 }
 
 // Tile scan: tile = 1024 cells, 4 per thread.  Source is either per-cell
-// counts (cnt) or the per-(cell,slot) counts of a rebuild (cnt9).
-template <bool kFromCnt9>
-__global__ void __launch_bounds__(kBlock) k_scan_tile(int C, int nx, int ny, const int *cnt, const int *cnt9,
-                                                      int2 *rng, int *local, int *sums) {
-    const int c0 = blockIdx.x * SCAN_TILE + threadIdx.x * 4;
+// counts (sort) or the per-(cell,slot) counts of a rebuild, whose per-cell
+// totals also become the counts of list buffer `parity` of kind k.
+template <class G, bool kFromCnt9>
+__global__ void __launch_bounds__(kBlock) k_scan_tile(const __grid_constant__ G g, int k, int parity) {
+    SPHNJ_SCENE(g);
+    const int C = p.cell_number_total, nx = p.cell_number[0], ny = p.cell_number[1];
+    const ListScratch &sc = S.sc;
+    int2 *rng = list_of(S, k, parity).rng;
+    const int c0 = blk * SCAN_TILE + threadIdx.x * 4;
     int v[4];
     int tsum = 0;
 #pragma unroll
-    for (int k = 0; k < 4; ++k) {
-        int c = c0 + k;
+    for (int q = 0; q < 4; ++q) {
+        int c = c0 + q;
         int x = 0;
         if (c < C) {
             if (kFromCnt9) {
                 int ci = c / ny, cj = c - ci * ny;
 #pragma unroll
                 for (int s = 0; s < 9; ++s)
-                    if (slot_valid(ci, cj, s, nx, ny)) x += cnt9[(long)c * 9 + s];
+                    if (slot_valid(ci, cj, s, nx, ny)) x += sc.cnt9[(long)c * 9 + s];
                 rng[c].y = x;
             } else {
-                x = cnt[c];
+                x = sc.cnt[c];
             }
         }
-        v[k] = x;
+        v[q] = x;
         tsum += x;
     }
     int total;
     int ex = block_excl_scan(tsum, &total);
 #pragma unroll
-    for (int k = 0; k < 4; ++k) {
-        int c = c0 + k;
-        if (c < C) local[c] = ex;
-        ex += v[k];
+    for (int q = 0; q < 4; ++q) {
+        int c = c0 + q;
+        if (c < C) sc.local[c] = ex;
+        ex += v[q];
     }
-    if (threadIdx.x == 0) sums[blockIdx.x] = total;
+    if (threadIdx.x == 0) sc.sums[blk] = total;
 }
 
 // In-place exclusive scan of the tile sums (<= SCAN_MAX_TILES) by one block;
-// the grand total goes to *total when given.
-__global__ void __launch_bounds__(1024) k_scan_sums(int ntiles, int *sums, int *total = nullptr) {
+// with want_total the grand total goes to the scene's listed-particle count.
+template <class G> __global__ void __launch_bounds__(1024) k_scan_sums(const __grid_constant__ G g, int want_total) {
+    SPHNJ_SCENE(g);
     __shared__ int ws[33];
+    const int ntiles = (p.cell_number_total + SCAN_TILE - 1) / SCAN_TILE;
+    int *sums = S.sc.sums;
+    int *total = want_total ? S.f_listed_total : nullptr;
     const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
     int v[4], tsum = 0;
 #pragma unroll
-    for (int k = 0; k < 4; ++k) {
-        int t = threadIdx.x * 4 + k;
-        v[k] = t < ntiles ? sums[t] : 0;
-        tsum += v[k];
+    for (int q = 0; q < 4; ++q) {
+        int t = threadIdx.x * 4 + q;
+        v[q] = t < ntiles ? sums[t] : 0;
+        tsum += v[q];
     }
     int inc = tsum;
 #pragma unroll
@@ -176,11 +195,11 @@ __global__ void __launch_bounds__(1024) k_scan_sums(int ntiles, int *sums, int *
     __syncthreads();
     int ex = inc - tsum + ws[w];
 #pragma unroll
-    for (int k = 0; k < 4; ++k) {
-        int t = threadIdx.x * 4 + k;
+    for (int q = 0; q < 4; ++q) {
+        int t = threadIdx.x * 4 + q;
         if (t < ntiles) sums[t] = ex;
-        if (total && t == ntiles - 1) *total = ex + v[k];
-        ex += v[k];
+        if (total && t == ntiles - 1) *total = ex + v[q];
+        ex += v[q];
     }
 }
 
@@ -189,54 +208,81 @@ __device__ __forceinline__ int cell_start(const int *local, const int *sums, int
 }
 
 // ---- sort ------------------------------------------------------------------
-__global__ void k_hist(int n, const int *cell, int *cnt) {
-    int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i < n) atomicAdd(&cnt[cell[i]], 1);
+template <class G> __global__ void k_sort_clear(const __grid_constant__ G g) {
+    SPHNJ_SCENE(g);
+    const int c = blk * blockDim.x + threadIdx.x;
+    if (c >= p.cell_number_total) return;
+    S.sc.cnt[c] = 0;
+    S.sc.cursor[c] = 0;
 }
 
-__global__ void k_bucket(int n, const int *cell, const int *local, const int *sums, int *cursor, int *bucket) {
-    int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= n) return;
-    int c = cell[i];
-    int slot = atomicAdd(&cursor[c], 1);
-    bucket[cell_start(local, sums, c) + slot] = i;
+template <class G> __global__ void k_hist(const __grid_constant__ G g, int k) {
+    SPHNJ_SCENE(g);
+    const int i = blk * blockDim.x + threadIdx.x;
+    if (i < count_of(p, (Kind)k)) atomicAdd(&S.sc.cnt[cells_of(d, k)[i]], 1);
+}
+
+template <class G> __global__ void k_bucket(const __grid_constant__ G g, int k) {
+    SPHNJ_SCENE(g);
+    const int i = blk * blockDim.x + threadIdx.x;
+    if (i >= count_of(p, (Kind)k)) return;
+    const ListScratch &sc = S.sc;
+    const int c = cells_of(d, k)[i];
+    const int slot = atomicAdd(&sc.cursor[c], 1);
+    sc.bucket[cell_start(sc.local, sc.sums, c) + slot] = i;
 }
 
 // One warp per cell: rank sort of the cell's bucket by particle index.
-__global__ void k_cellsort(int C, const int *cnt, const int *local, const int *sums, const int *bucket,
-                           int *sorted, int2 *rng) {
+template <class G> __global__ void k_cellsort(const __grid_constant__ G g, int k, int parity) {
+    SPHNJ_SCENE(g);
+    const ListScratch &sc = S.sc;
     const int lane = threadIdx.x & 31;
-    const long c = ((long)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
-    if (c >= C) return;
-    const int n = cnt[c];
-    const int base = cell_start(local, sums, (int)c);
-    if (lane == 0) rng[c] = make_int2(base, n);
+    const long c = ((long)blk * blockDim.x + threadIdx.x) >> 5;
+    if (c >= p.cell_number_total) return;
+    const int n = sc.cnt[c];
+    const int base = cell_start(sc.local, sc.sums, (int)c);
+    if (lane == 0) list_of(S, k, parity).rng[c] = make_int2(base, n);
     for (int k0 = 0; k0 < n; k0 += 32) {
-        int k = k0 + lane;
-        int v = k < n ? bucket[base + k] : INT_MAX;
+        int q = k0 + lane;
+        int v = q < n ? sc.bucket[base + q] : INT_MAX;
         int rank = 0;
         for (int q0 = 0; q0 < n; q0 += 32) {
-            int w = q0 + lane < n ? bucket[base + q0 + lane] : INT_MAX;
+            int w = q0 + lane < n ? sc.bucket[base + q0 + lane] : INT_MAX;
 #pragma unroll 8
             for (int t = 0; t < 32; ++t) rank += (__shfl_sync(0xffffffffu, w, t) < v) ? 1 : 0;
         }
-        if (k < n) sorted[base + rank] = v;
+        if (q < n) sc.sorted[base + rank] = v;
     }
 }
 
 // Payload gathers (sort.cu:10-45): new[k] = old[sorted[k]], lists = identity.
+__device__ __forceinline__ size_t align256_d(size_t x) { return (x + 255) & ~size_t(255); }
+template <class T> __device__ __forceinline__ T *carve(char *&q, size_t n) {
+    T *r = reinterpret_cast<T *>(q);
+    q += align256_d(n * sizeof(T));
+    return r;
+}
+
 struct FluidPayload {
     float2 *pos, *vel;
     float *rho, *p;
     uint8_t *phase, *fbt;
     int *cell;
+    __device__ FluidPayload(char *q, int n) {
+        pos = carve<float2>(q, n); vel = carve<float2>(q, n);
+        rho = carve<float>(q, n); p = carve<float>(q, n);
+        phase = carve<uint8_t>(q, n); fbt = carve<uint8_t>(q, n);
+        cell = carve<int>(q, n);
+    }
 };
-__global__ void k_gather_fluid(int n, const int *sorted, DevState d, FluidPayload o, int *lst, int *listed,
-                               const int *stamp) {
-    int k = blockIdx.x * blockDim.x + threadIdx.x;
+template <class G> __global__ void k_gather_fluid(const __grid_constant__ G g, int parity) {
+    SPHNJ_SCENE(g);
+    const int n = p.fluid_number_total;
+    const int k = blk * blockDim.x + threadIdx.x;
     if (k >= n) return;
-    if (listed) listed[k] = *stamp;
-    int s = sorted[k];
+    const FluidPayload o(S.payload, n);
+    if (d.f_listed) d.f_listed[k] = *d.stamp;
+    const int s = S.sc.sorted[k];
     o.pos[k] = d.f_pos[s];
     o.vel[k] = d.f_vel[s];
     o.rho[k] = d.f_rho[s];
@@ -244,11 +290,14 @@ __global__ void k_gather_fluid(int n, const int *sorted, DevState d, FluidPayloa
     o.phase[k] = d.f_phase[s];
     o.fbt[k] = d.f_fbt[s];
     o.cell[k] = d.f_cell[s];
-    lst[k] = k;
+    S.lf[parity].lst[k] = k;
 }
-__global__ void k_scatter_back_fluid(int n, DevState d, FluidPayload o) {
-    int k = blockIdx.x * blockDim.x + threadIdx.x;
+template <class G> __global__ void k_scatter_back_fluid(const __grid_constant__ G g) {
+    SPHNJ_SCENE(g);
+    const int n = p.fluid_number_total;
+    const int k = blk * blockDim.x + threadIdx.x;
     if (k >= n) return;
+    const FluidPayload o(S.payload, n);
     d.f_pos[k] = o.pos[k];
     d.f_vel[k] = o.vel[k];
     d.f_rho[k] = o.rho[k];
@@ -263,11 +312,20 @@ struct SolidPayload {
     dmat2 *maxstrain;
     uint8_t *mat, *bt;
     int *cell;
+    __device__ SolidPayload(char *q, int n) {
+        ref = carve<double2>(q, n); pos = carve<double2>(q, n); vel = carve<double2>(q, n);
+        maxstrain = carve<dmat2>(q, n);
+        mat = carve<uint8_t>(q, n); bt = carve<uint8_t>(q, n);
+        cell = carve<int>(q, n);
+    }
 };
-__global__ void k_gather_solid(int n, const int *sorted, DevState d, SolidPayload o, int *lst) {
-    int k = blockIdx.x * blockDim.x + threadIdx.x;
+template <class G> __global__ void k_gather_solid(const __grid_constant__ G g, int parity) {
+    SPHNJ_SCENE(g);
+    const int n = p.solid_number;
+    const int k = blk * blockDim.x + threadIdx.x;
     if (k >= n) return;
-    int s = sorted[k];
+    const SolidPayload o(S.payload, n);
+    const int s = S.sc.sorted[k];
     o.ref[k] = d.s_ref[s];
     o.pos[k] = d.s_pos[s];
     o.vel[k] = d.s_vel[s];
@@ -275,11 +333,14 @@ __global__ void k_gather_solid(int n, const int *sorted, DevState d, SolidPayloa
     o.mat[k] = d.s_mat[s];
     o.bt[k] = d.s_bt[s];
     o.cell[k] = d.s_cell[s];
-    lst[k] = k;
+    S.ls[parity].lst[k] = k;
 }
-__global__ void k_scatter_back_solid(int n, DevState d, SolidPayload o) {
-    int k = blockIdx.x * blockDim.x + threadIdx.x;
+template <class G> __global__ void k_scatter_back_solid(const __grid_constant__ G g) {
+    SPHNJ_SCENE(g);
+    const int n = p.solid_number;
+    const int k = blk * blockDim.x + threadIdx.x;
     if (k >= n) return;
+    const SolidPayload o(S.payload, n);
     d.s_ref[k] = o.ref[k];
     d.s_pos[k] = o.pos[k];
     d.s_vel[k] = o.vel[k];
@@ -293,20 +354,31 @@ struct VirtPayload {
     float2 *pos, *normal;
     uint8_t *bt;
     int *cell;
+    __device__ VirtPayload(char *q, int n) {
+        pos = carve<float2>(q, n); normal = carve<float2>(q, n);
+        bt = carve<uint8_t>(q, n);
+        cell = carve<int>(q, n);
+    }
 };
-__global__ void k_gather_virt(int n, const int *sorted, DevState d, VirtPayload o, int *lst) {
-    int k = blockIdx.x * blockDim.x + threadIdx.x;
+template <class G> __global__ void k_gather_virt(const __grid_constant__ G g) {
+    SPHNJ_SCENE(g);
+    const int n = p.virt_number;
+    const int k = blk * blockDim.x + threadIdx.x;
     if (k >= n) return;
-    int s = sorted[k];
+    const VirtPayload o(S.payload, n);
+    const int s = S.sc.sorted[k];
     o.pos[k] = d.v_pos[s];
     o.normal[k] = d.v_normal[s];
     o.bt[k] = d.v_bt[s];
     o.cell[k] = d.v_cell[s];
-    lst[k] = k;
+    S.lv.lst[k] = k;
 }
-__global__ void k_scatter_back_virt(int n, DevState d, VirtPayload o) {
-    int k = blockIdx.x * blockDim.x + threadIdx.x;
+template <class G> __global__ void k_scatter_back_virt(const __grid_constant__ G g) {
+    SPHNJ_SCENE(g);
+    const int n = p.virt_number;
+    const int k = blk * blockDim.x + threadIdx.x;
     if (k >= n) return;
+    const VirtPayload o(S.payload, n);
     d.v_pos[k] = o.pos[k];
     d.v_normal[k] = o.normal[k];
     d.v_bt[k] = o.bt[k];
@@ -323,19 +395,23 @@ __device__ __forceinline__ int slot_from(int mi, int mj, int c, int ny) {
     return 3 * (di + 1) + (dj + 1);
 }
 
-__global__ void k_rebuild_count(int C, int nx, int ny, const int2 *prng, const int *plst, const int *cell,
-                                int *cnt9) {
-    int m = blockIdx.x * blockDim.x + threadIdx.x;
+template <class G> __global__ void k_rebuild_count(const __grid_constant__ G g, int k, int parity) {
+    SPHNJ_SCENE(g);
+    const int C = p.cell_number_total, nx = p.cell_number[0], ny = p.cell_number[1];
+    const int m = blk * blockDim.x + threadIdx.x;
     if (m >= C) return;
+    const CellList &prev = list_of(S, k, parity ^ 1);
+    const int *cell = cells_of(d, k);
+    int *cnt9 = S.sc.cnt9;
     const int mi = m / ny, mj = m - mi * ny;
-    const int2 r = prng[m];
+    const int2 r = prev.rng[m];
     int run[9];
 #pragma unroll
     for (int s = 0; s < 9; ++s) run[s] = 0;
-    for (int k = r.x; k < r.x + r.y; ++k) {
-        int s = slot_from(mi, mj, __ldg(&cell[__ldg(&plst[k])]), ny);
+    for (int q = r.x; q < r.x + r.y; ++q) {
+        int s = slot_from(mi, mj, __ldg(&cell[__ldg(&prev.lst[q])]), ny);
 #pragma unroll
-        for (int q = 0; q < 9; ++q) run[q] += (s == q);
+        for (int t = 0; t < 9; ++t) run[t] += (s == t);
     }
 #pragma unroll
     for (int s = 0; s < 9; ++s) {
@@ -344,13 +420,17 @@ __global__ void k_rebuild_count(int C, int nx, int ny, const int2 *prng, const i
     }
 }
 
-__global__ void k_rebuild_write(int C, int nx, int ny, const int2 *prng, const int *plst, const int *cell,
-                                const int *cnt9, const int *local, const int *sums, int2 *crng, int *clst,
-                                int *listed, const int *stamp) {
-    int m = blockIdx.x * blockDim.x + threadIdx.x;
+template <class G> __global__ void k_rebuild_write(const __grid_constant__ G g, int k, int parity) {
+    SPHNJ_SCENE(g);
+    const int C = p.cell_number_total, nx = p.cell_number[0], ny = p.cell_number[1];
+    const int m = blk * blockDim.x + threadIdx.x;
     if (m >= C) return;
+    const CellList &prev = list_of(S, k, parity ^ 1), &cur = list_of(S, k, parity);
+    const int *cell = cells_of(d, k);
+    const ListScratch &sc = S.sc;
+    int *listed = k == KF ? d.f_listed : nullptr;
     const int mi = m / ny, mj = m - mi * ny;
-    crng[m].x = cell_start(local, sums, m);
+    cur.rng[m].x = cell_start(sc.local, sc.sums, m);
     int base[9];
 #pragma unroll
     for (int s = 0; s < 9; ++s) {
@@ -358,107 +438,100 @@ __global__ void k_rebuild_write(int C, int nx, int ny, const int2 *prng, const i
         int b = 0;
         if (ci >= 0 && ci < nx && cj >= 0 && cj < ny) {
             int c = ci * ny + cj;
-            b = cell_start(local, sums, c);
+            b = cell_start(sc.local, sc.sums, c);
             for (int q = 0; q < s; ++q)
-                if (slot_valid(ci, cj, q, nx, ny)) b += cnt9[(long)c * 9 + q];
+                if (slot_valid(ci, cj, q, nx, ny)) b += sc.cnt9[(long)c * 9 + q];
         }
         base[s] = b;
     }
-    const int2 r = prng[m];
-    for (int k = r.x; k < r.x + r.y; ++k) {
-        int pidx = __ldg(&plst[k]);
+    const int stamp = listed ? *d.stamp : 0;
+    const int2 r = prev.rng[m];
+    for (int q = r.x; q < r.x + r.y; ++q) {
+        int pidx = __ldg(&prev.lst[q]);
         int s = slot_from(mi, mj, __ldg(&cell[pidx]), ny);
         if (s < 0) continue;
         int dst = 0;
 #pragma unroll
-        for (int q = 0; q < 9; ++q)
-            if (q == s) dst = base[q]++;
-        clst[dst] = pidx;
-        if (listed) listed[pidx] = *stamp;
+        for (int t = 0; t < 9; ++t)
+            if (t == s) dst = base[t]++;
+        cur.lst[dst] = pidx;
+        if (listed) listed[pidx] = stamp;
     }
 }
 
-__global__ void k_capacity(int C, const int2 *rf, const int2 *rs, const int2 *rv, DevErr *err) {
-    int c = blockIdx.x * blockDim.x + threadIdx.x;
-    if (c >= C) return;
-    int t = rf[c].y + rs[c].y + rv[c].y;
-    if (t > SPHNJ_CELL_SIZE) raise_error(err, SPHNJ_ERR_CELL_OVERFLOW, c, t, 0);
-}
-
-inline size_t align256(size_t x) { return (x + 255) & ~size_t(255); }
-template <class T> T *carve(char *&p, size_t n) {
-    T *r = reinterpret_cast<T *>(p);
-    p += align256(n * sizeof(T));
-    return r;
+template <class G> __global__ void k_capacity(const __grid_constant__ G g) {
+    SPHNJ_SCENE(g);
+    const int c = blk * blockDim.x + threadIdx.x;
+    if (c >= p.cell_number_total) return;
+    const int t = d.rng_f[c].y + d.rng_s[c].y + d.rng_v[c].y;
+    if (t > SPHNJ_CELL_SIZE) raise_error(d.err, SPHNJ_ERR_CELL_OVERFLOW, c, t, 0);
 }
 
 }  // namespace
 
-void launch_bin(cudaStream_t st, const sphnj_params &p, const DevState &d, bool with_virt) {
-    long n = (long)p.fluid_number_total + p.solid_number + (with_virt ? p.virt_number : 0);
-    k_bin<<<grid_for(n > 0 ? n : 1, kBlock), kBlock, 0, st>>>(p, d, with_virt ? 1 : 0);
+template <class G> int launch_bin(cudaStream_t st, G &g, bool with_virt) {
+    return launch(
+        g, site_key(SITE_BIN, with_virt ? 1 : 0),
+        [&](const Scene &s) {
+            long n = (long)s.p.fluid_number_total + s.p.solid_number + (with_virt ? s.p.virt_number : 0);
+            return grid_for(n > 0 ? n : 1, kBlock);
+        },
+        k_bin<typename G::Dev>, kBlock, 0, st, with_virt ? 1 : 0);
 }
 
-static void scan_counts(cudaStream_t st, int C, const int *cnt, int *local, int *sums, int *total) {
-    int tiles = (C + SCAN_TILE - 1) / SCAN_TILE;
-    k_scan_tile<false><<<tiles, kBlock, 0, st>>>(C, 0, 1, cnt, nullptr, nullptr, local, sums);
-    k_scan_sums<<<1, 1024, 0, st>>>(tiles, sums, total);
-}
-
-void launch_sort_kind(cudaStream_t st, const sphnj_params &p, const DevState &d, Kind k, int n, int *cell,
-                      ListScratch sc, CellList cur, void *payload_scratch, Listing lg) {
-    const int C = p.cell_number_total;
-    cudaMemsetAsync(sc.cnt, 0, sizeof(int) * C, st);
-    cudaMemsetAsync(sc.cursor, 0, sizeof(int) * C, st);
-    if (n > 0) k_hist<<<grid_for(n, kBlock), kBlock, 0, st>>>(n, cell, sc.cnt);
-    scan_counts(st, C, sc.cnt, sc.local, sc.sums, lg.total);
-    if (n > 0) k_bucket<<<grid_for(n, kBlock), kBlock, 0, st>>>(n, cell, sc.local, sc.sums, sc.cursor, sc.bucket);
-    k_cellsort<<<grid_for((long)C * 32, kBlock), kBlock, 0, st>>>(C, sc.cnt, sc.local, sc.sums, sc.bucket,
-                                                                    sc.sorted, cur.rng);
-    if (n <= 0) return;
-    char *q = static_cast<char *>(payload_scratch);
+template <class G> int launch_sort_kind(cudaStream_t st, G &g, Kind k, int parity) {
+    using D = typename G::Dev;
+    auto has = [k](const Scene &s) { return count_of(s.p, k) > 0; };
+    auto cells = [&](const Scene &s) { return has(s) ? grid_for(s.p.cell_number_total, kBlock) : 0u; };
+    auto parts = [&](const Scene &s) { return has(s) ? grid_for(count_of(s.p, k), kBlock) : 0u; };
+    auto tiles = [&](const Scene &s) { return has(s) ? grid_for(s.p.cell_number_total, SCAN_TILE) : 0u; };
+    auto one = [&](const Scene &s) { return has(s) ? 1u : 0u; };
+    auto warps = [&](const Scene &s) { return has(s) ? grid_for((long)s.p.cell_number_total * 32, kBlock) : 0u; };
+    const int ki = (int)k;
+    int n = 0;
+    n += launch(g, site_key(SITE_SORT_CLEAR, ki), cells, k_sort_clear<D>, kBlock, 0, st);
+    n += launch(g, site_key(SITE_SORT_N, ki), parts, k_hist<D>, kBlock, 0, st, ki);
+    n += launch(g, site_key(SITE_SORT_TILES, ki), tiles, k_scan_tile<D, false>, kBlock, 0, st, ki, parity);
+    n += launch(g, site_key(SITE_SORT_ONE, ki), one, k_scan_sums<D>, 1024, 0, st, k == KF ? 1 : 0);
+    n += launch(g, site_key(SITE_SORT_N, ki), parts, k_bucket<D>, kBlock, 0, st, ki);
+    n += launch(g, site_key(SITE_SORT_CELLS32, ki), warps, k_cellsort<D>, kBlock, 0, st, ki, parity);
     if (k == KF) {
-        FluidPayload o;
-        o.pos = carve<float2>(q, n); o.vel = carve<float2>(q, n);
-        o.rho = carve<float>(q, n); o.p = carve<float>(q, n);
-        o.phase = carve<uint8_t>(q, n); o.fbt = carve<uint8_t>(q, n);
-        o.cell = carve<int>(q, n);
-        k_gather_fluid<<<grid_for(n, kBlock), kBlock, 0, st>>>(n, sc.sorted, d, o, cur.lst, lg.listed, lg.stamp);
-        k_scatter_back_fluid<<<grid_for(n, kBlock), kBlock, 0, st>>>(n, d, o);
+        n += launch(g, site_key(SITE_SORT_N, ki), parts, k_gather_fluid<D>, kBlock, 0, st, parity);
+        n += launch(g, site_key(SITE_SORT_N, ki), parts, k_scatter_back_fluid<D>, kBlock, 0, st);
     } else if (k == KS) {
-        SolidPayload o;
-        o.ref = carve<double2>(q, n); o.pos = carve<double2>(q, n); o.vel = carve<double2>(q, n);
-        o.maxstrain = carve<dmat2>(q, n);
-        o.mat = carve<uint8_t>(q, n); o.bt = carve<uint8_t>(q, n);
-        o.cell = carve<int>(q, n);
-        k_gather_solid<<<grid_for(n, kBlock), kBlock, 0, st>>>(n, sc.sorted, d, o, cur.lst);
-        k_scatter_back_solid<<<grid_for(n, kBlock), kBlock, 0, st>>>(n, d, o);
+        n += launch(g, site_key(SITE_SORT_N, ki), parts, k_gather_solid<D>, kBlock, 0, st, parity);
+        n += launch(g, site_key(SITE_SORT_N, ki), parts, k_scatter_back_solid<D>, kBlock, 0, st);
     } else {
-        VirtPayload o;
-        o.pos = carve<float2>(q, n); o.normal = carve<float2>(q, n);
-        o.bt = carve<uint8_t>(q, n);
-        o.cell = carve<int>(q, n);
-        k_gather_virt<<<grid_for(n, kBlock), kBlock, 0, st>>>(n, sc.sorted, d, o, cur.lst);
-        k_scatter_back_virt<<<grid_for(n, kBlock), kBlock, 0, st>>>(n, d, o);
+        n += launch(g, site_key(SITE_SORT_N, ki), parts, k_gather_virt<D>, kBlock, 0, st);
+        n += launch(g, site_key(SITE_SORT_N, ki), parts, k_scatter_back_virt<D>, kBlock, 0, st);
     }
+    return n;
 }
 
-void launch_rebuild_kind(cudaStream_t st, const sphnj_params &p, int n, const int *cell, CellList prev,
-                         CellList cur, ListScratch sc, DevErr *err, Listing lg) {
-    (void)n;
-    (void)err;
-    const int C = p.cell_number_total, nx = p.cell_number[0], ny = p.cell_number[1];
-    const int tiles = (C + SCAN_TILE - 1) / SCAN_TILE;
-    k_rebuild_count<<<grid_for(C, kBlock), kBlock, 0, st>>>(C, nx, ny, prev.rng, prev.lst, cell, sc.cnt9);
-    k_scan_tile<true><<<tiles, kBlock, 0, st>>>(C, nx, ny, nullptr, sc.cnt9, cur.rng, sc.local, sc.sums);
-    k_scan_sums<<<1, 1024, 0, st>>>(tiles, sc.sums, lg.total);
-    k_rebuild_write<<<grid_for(C, kBlock), kBlock, 0, st>>>(C, nx, ny, prev.rng, prev.lst, cell, sc.cnt9, sc.local,
-                                                            sc.sums, cur.rng, cur.lst, lg.listed, lg.stamp);
+template <class G> int launch_rebuild_kind(cudaStream_t st, G &g, Kind k, int parity) {
+    using D = typename G::Dev;
+    auto has = [k](const Scene &s) { return count_of(s.p, k) > 0; };
+    auto cells = [&](const Scene &s) { return has(s) ? grid_for(s.p.cell_number_total, kBlock) : 0u; };
+    auto tiles = [&](const Scene &s) { return has(s) ? grid_for(s.p.cell_number_total, SCAN_TILE) : 0u; };
+    auto one = [&](const Scene &s) { return has(s) ? 1u : 0u; };
+    const int ki = (int)k;
+    int n = 0;
+    n += launch(g, site_key(SITE_REBUILD_CELLS, ki), cells, k_rebuild_count<D>, kBlock, 0, st, ki, parity);
+    n += launch(g, site_key(SITE_REBUILD_TILES, ki), tiles, k_scan_tile<D, true>, kBlock, 0, st, ki, parity);
+    n += launch(g, site_key(SITE_REBUILD_ONE, ki), one, k_scan_sums<D>, 1024, 0, st, k == KF ? 1 : 0);
+    n += launch(g, site_key(SITE_REBUILD_CELLS, ki), cells, k_rebuild_write<D>, kBlock, 0, st, ki, parity);
+    return n;
 }
 
-void launch_capacity_check(cudaStream_t st, const sphnj_params &p, const DevState &d) {
-    const int C = p.cell_number_total;
-    k_capacity<<<grid_for(C, kBlock), kBlock, 0, st>>>(C, d.rng_f, d.rng_s, d.rng_v, d.err);
+template <class G> int launch_capacity_check(cudaStream_t st, G &g) {
+    return launch(
+        g, site_key(SITE_CAPACITY), [](const Scene &s) { return grid_for(s.p.cell_number_total, kBlock); },
+        k_capacity<typename G::Dev>, kBlock, 0, st);
 }
+
+SPHNJ_INSTANTIATE_GROUPS(launch_bin, bool);
+SPHNJ_INSTANTIATE_GROUPS(launch_sort_kind, Kind, int);
+SPHNJ_INSTANTIATE_GROUPS(launch_rebuild_kind, Kind, int);
+SPHNJ_INSTANTIATE_GROUPS(launch_capacity_check);
 
 }  // namespace sphnj

@@ -34,6 +34,8 @@
 // loses ~1e-4 relative pressure accuracy near the reference density.
 #include "kernels.h"
 
+#include <algorithm>
+
 namespace sphnj {
 
 namespace {
@@ -480,11 +482,11 @@ struct TileGeom {
     int home_b, home_e, total;
 };
 
-__device__ __forceinline__ bool tile_setup(const sphnj_params &p, const DevState &d, int tile_h, int *s_base,
-                                           int *s_off, TileGeom &g) {
+__device__ __forceinline__ bool tile_setup(const sphnj_params &p, const DevState &d, int blk, int tile_h,
+                                           int *s_base, int *s_off, TileGeom &g) {
     const int nx = p.cell_number[0], ny = p.cell_number[1];
     const int tiles_y = (ny + tile_h - 1) / tile_h;
-    const int ci = blockIdx.x / tiles_y, cj0 = (blockIdx.x - ci * tiles_y) * tile_h;
+    const int ci = blk / tiles_y, cj0 = (blk - ci * tiles_y) * tile_h;
     const int cj1 = min(cj0 + tile_h, ny);
     const int2 h0 = __ldg(&d.rng_f[ci * ny + cj0]), h1 = __ldg(&d.rng_f[ci * ny + cj1 - 1]);
     g.home_b = h0.x;
@@ -516,11 +518,13 @@ __device__ __forceinline__ bool tile_setup(const sphnj_params &p, const DevState
 
 __device__ __forceinline__ int tile_strip(const int *s_off, int k) { return k < s_off[1] ? 0 : (k < s_off[2] ? 1 : 2); }
 
-__global__ void __launch_bounds__(kTileBlock) k_fluid_pair_tiled(sphnj_params p, DevState d, int tile_h, int cap) {
+template <class G>
+__global__ void __launch_bounds__(kTileBlock) k_fluid_pair_tiled(const __grid_constant__ G gs, int tile_h, int cap) {
+    SPHNJ_SCENE(gs);
     extern __shared__ __align__(16) unsigned char smem[];
     __shared__ int s_base[3], s_off[3];
     TileGeom g;
-    if (!tile_setup(p, d, tile_h, s_base, s_off, g)) return;
+    if (!tile_setup(p, d, blk, tile_h, s_base, s_off, g)) return;
     float2 *s_pos = reinterpret_cast<float2 *>(smem);
     float2 *s_vel = s_pos + cap;
     float2 *s_rp = s_vel + cap;
@@ -550,12 +554,14 @@ __global__ void __launch_bounds__(kTileBlock) k_fluid_pair_tiled(sphnj_params p,
     }
 }
 
-__global__ void __launch_bounds__(kTileBlock) k_shift_gradient_tiled(sphnj_params p, DevState d, int tile_h,
-                                                                     int cap, int pass) {
+template <class G>
+__global__ void __launch_bounds__(kTileBlock) k_shift_gradient_tiled(const __grid_constant__ G gs, int tile_h, int cap,
+                                                                     int pass) {
+    SPHNJ_SCENE(gs);
     extern __shared__ __align__(16) unsigned char smem[];
     __shared__ int s_base[3], s_off[3];
     TileGeom g;
-    if (!tile_setup(p, d, tile_h, s_base, s_off, g)) return;
+    if (!tile_setup(p, d, blk, tile_h, s_base, s_off, g)) return;
     float2 *s_pos = reinterpret_cast<float2 *>(smem);
     const bool staged = g.total <= cap;
     if (staged) {
@@ -580,21 +586,25 @@ __global__ void __launch_bounds__(kTileBlock) k_shift_gradient_tiled(sphnj_param
 
 // Per-particle forms: every particle (listed == null), or only the particles
 // that are in no cell list.
-__global__ void __launch_bounds__(kPairBlock) k_fluid_pair_each(sphnj_params p, DevState d, int only_unlisted) {
+template <class G>
+__global__ void __launch_bounds__(kPairBlock) k_fluid_pair_each(const __grid_constant__ G g, int only_unlisted) {
+    SPHNJ_SCENE(g);
     const int nf = p.fluid_number_total;
     if (only_unlisted && *d.f_listed_total == nf) return;
     const int stamp = *d.stamp;
     const SrcGlobal src{&d};
-    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < nf; i += gridDim.x * blockDim.x)
+    for (int i = blk * blockDim.x + threadIdx.x; i < nf; i += nblk * blockDim.x)
         if (!only_unlisted || d.f_listed[i] != stamp) pair_particle(p, d, src, i);
 }
 
-__global__ void __launch_bounds__(kPairBlock) k_shift_gradient_each(sphnj_params p, DevState d, int only_unlisted) {
+template <class G>
+__global__ void __launch_bounds__(kPairBlock) k_shift_gradient_each(const __grid_constant__ G g, int only_unlisted) {
+    SPHNJ_SCENE(g);
     const int nf = p.fluid_number_total;
     if (only_unlisted && *d.f_listed_total == nf) return;
     const int stamp = *d.stamp;
     const SrcGlobal src{&d};
-    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < nf; i += gridDim.x * blockDim.x)
+    for (int i = blk * blockDim.x + threadIdx.x; i < nf; i += nblk * blockDim.x)
         if (!only_unlisted || d.f_listed[i] != stamp) shift_particle(p, d, src, i);
 }
 
@@ -605,8 +615,9 @@ __device__ __forceinline__ float density_to_pressure(const sphnj_params &p, floa
     return fmaxf(pr, p.min_pressure);
 }
 
-__global__ void __launch_bounds__(kBlock) k_fluid_update(sphnj_params p, DevState d) {
-    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+template <class G> __global__ void __launch_bounds__(kBlock) k_fluid_update(const __grid_constant__ G g) {
+    SPHNJ_SCENE(g);
+    const int i = blk * blockDim.x + threadIdx.x;
     unsigned int sp2 = 0u, moved2 = 0u;
     if (i < p.fluid_number_total) {
         const int ph = d.f_phase[i];
@@ -695,8 +706,9 @@ __device__ __forceinline__ unsigned int shift_update_particle(const sphnj_params
     return disp2(x0, x);
 }
 
-__global__ void __launch_bounds__(kBlock) k_shift_update(sphnj_params p, DevState d, int pass) {
-    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+template <class G> __global__ void __launch_bounds__(kBlock) k_shift_update(const __grid_constant__ G g, int pass) {
+    SPHNJ_SCENE(g);
+    const int i = blk * blockDim.x + threadIdx.x;
     unsigned int moved2 = 0u;
     if (i < p.fluid_number_total) moved2 = shift_update_particle(p, d, i);
     if (pass < kMaskShifts) block_max_to<kBlock>(moved2, &d.disp2_bits[1 + pass]);
@@ -713,41 +725,69 @@ constexpr size_t kPairSmemPerEntry = 3 * sizeof(float2) + sizeof(int) + 1;
 cudaError_t configure_sweeps(const TileConfig &tc) {
     const size_t smem = tile_cap(tc.tile_h) * kPairSmemPerEntry;  // above 48 KB needs an opt-in
     if (smem <= 48 * 1024) return cudaSuccess;
-    return cudaFuncSetAttribute(k_fluid_pair_tiled, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    cudaError_t e = cudaFuncSetAttribute(k_fluid_pair_tiled<One>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (e == cudaSuccess)
+        e = cudaFuncSetAttribute(k_fluid_pair_tiled<Many>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    return e;
 }
 
-void launch_fluid_pair(cudaStream_t st, const sphnj_params &p, const DevState &d, const TileConfig &tc) {
-    const int n = p.fluid_number_total;
-    if (n <= 0) return;
-    if (!tc.tiled) {
-        k_fluid_pair_each<<<grid_for(n, kPairBlock), kPairBlock, 0, st>>>(p, d, 0);
-        return;
-    }
+// Per-particle fallback grid of one scene: grid-stride, at most 2 blocks per SM.
+inline unsigned fallback_blocks(int n) { return n > 0 ? (unsigned)std::min<long>(kFallbackBlocks, grid_for(n, kPairBlock)) : 0u; }
+
+template <class G> int launch_fluid_pair(cudaStream_t st, G &g, const TileConfig &tc) {
+    using D = typename G::Dev;
+    if (!tc.tiled)
+        return launch(
+            g, site_key(SITE_PAIR_EACH), [](const Scene &s) { return grid_for(s.p.fluid_number_total, kPairBlock); },
+            k_fluid_pair_each<D>, kPairBlock, 0, st, 0);
     const int cap = tile_cap(tc.tile_h);
     const size_t smem = cap * kPairSmemPerEntry;
-    k_fluid_pair_tiled<<<tile_blocks(p, tc.tile_h), kTileBlock, smem, st>>>(p, d, tc.tile_h, cap);
-    k_fluid_pair_each<<<kFallbackBlocks, kPairBlock, 0, st>>>(p, d, 1);
+    int n = launch(
+        g, site_key(SITE_PAIR_TILED, tc.tile_h),
+        [&](const Scene &s) { return s.p.fluid_number_total > 0 ? tile_blocks(s.p, tc.tile_h) : 0u; },
+        k_fluid_pair_tiled<D>, kTileBlock, smem, st, tc.tile_h, cap);
+    n += launch(
+        g, site_key(SITE_PAIR_FALLBACK), [](const Scene &s) { return fallback_blocks(s.p.fluid_number_total); },
+        k_fluid_pair_each<D>, kPairBlock, 0, st, 1);
+    return n;
 }
-void launch_fluid_update(cudaStream_t st, const sphnj_params &p, const DevState &d) {
-    const int n = p.fluid_number_total;
-    if (n > 0) k_fluid_update<<<grid_for(n, kBlock), kBlock, 0, st>>>(p, d);
+
+template <class G> int launch_fluid_update(cudaStream_t st, G &g) {
+    return launch(
+        g, site_key(SITE_FLUID_UPDATE), [](const Scene &s) { return grid_for(s.p.fluid_number_total, kBlock); },
+        k_fluid_update<typename G::Dev>, kBlock, 0, st);
 }
-void launch_shift_gradient(cudaStream_t st, const sphnj_params &p, const DevState &d, const TileConfig &tc,
-                           int pass) {
-    const int n = p.fluid_number_total;
-    if (n <= 0) return;
-    if (!tc.tiled) {
-        k_shift_gradient_each<<<grid_for(n, kPairBlock), kPairBlock, 0, st>>>(p, d, 0);
-        return;
-    }
+
+template <class G> int launch_shift_gradient(cudaStream_t st, G &g, const TileConfig &tc, int pass) {
+    using D = typename G::Dev;
+    auto active = [pass](const Scene &s) { return s.p.fluid_number_total > 0 && pass < s.p.shift_per_step; };
+    if (!tc.tiled)
+        return launch(
+            g, site_key(SITE_SHIFT_EACH, pass),
+            [&](const Scene &s) { return active(s) ? grid_for(s.p.fluid_number_total, kPairBlock) : 0u; },
+            k_shift_gradient_each<D>, kPairBlock, 0, st, 0);
     const int cap = tile_cap(tc.tile_h);
-    k_shift_gradient_tiled<<<tile_blocks(p, tc.tile_h), kTileBlock, cap * sizeof(float2), st>>>(p, d, tc.tile_h,
-                                                                                                  cap, pass);
-    k_shift_gradient_each<<<kFallbackBlocks, kPairBlock, 0, st>>>(p, d, 1);
+    int n = launch(
+        g, site_key(SITE_SHIFT_TILED, (tc.tile_h << 8) | pass),
+        [&](const Scene &s) { return active(s) ? tile_blocks(s.p, tc.tile_h) : 0u; }, k_shift_gradient_tiled<D>,
+        kTileBlock, cap * sizeof(float2), st, tc.tile_h, cap, pass);
+    n += launch(
+        g, site_key(SITE_SHIFT_FALLBACK, pass),
+        [&](const Scene &s) { return active(s) ? fallback_blocks(s.p.fluid_number_total) : 0u; },
+        k_shift_gradient_each<D>, kPairBlock, 0, st, 1);
+    return n;
 }
-void launch_shift_update(cudaStream_t st, const sphnj_params &p, const DevState &d, int pass) {
-    const int n = p.fluid_number_total;
-    if (n > 0) k_shift_update<<<grid_for(n, kBlock), kBlock, 0, st>>>(p, d, pass);
+
+template <class G> int launch_shift_update(cudaStream_t st, G &g, int pass) {
+    return launch(
+        g, site_key(SITE_SHIFT_UPDATE, pass),
+        [pass](const Scene &s) { return pass < s.p.shift_per_step ? grid_for(s.p.fluid_number_total, kBlock) : 0u; },
+        k_shift_update<typename G::Dev>, kBlock, 0, st, pass);
 }
+
+SPHNJ_INSTANTIATE_GROUPS(launch_fluid_pair, const TileConfig &);
+SPHNJ_INSTANTIATE_GROUPS(launch_fluid_update);
+SPHNJ_INSTANTIATE_GROUPS(launch_shift_gradient, const TileConfig &, int);
+SPHNJ_INSTANTIATE_GROUPS(launch_shift_update, int);
 
 }  // namespace sphnj

@@ -28,10 +28,11 @@ __device__ __forceinline__ float sw(const sphnj_params &p, float q2) {
 }
 __device__ __forceinline__ float by_phase(const float (&a)[2], int ph) { return ph ? a[1] : a[0]; }
 
-__global__ void __launch_bounds__(256) k_virt_normal(sphnj_params p, DevState d) {
+template <class G> __global__ void __launch_bounds__(256) k_virt_normal(const __grid_constant__ G g) {
+    SPHNJ_SCENE(g);
     __shared__ float2 tile[256];
     const int nv = p.virt_number;
-    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    const int i = blk * blockDim.x + threadIdx.x;
     const float R2 = p.impact_distance_square, hinv2 = p.smoothing_length_inverse_square;
     const float2 x_i = i < nv ? d.v_pos[i] : make_float2(0.f, 0.f);
     float2 nrm = make_float2(0.f, 0.f);
@@ -53,8 +54,9 @@ __global__ void __launch_bounds__(256) k_virt_normal(sphnj_params p, DevState d)
     if (i < nv) d.v_normal[i] = sqrtf(sqn(nrm)) < EPS_FOR_SUM ? make_float2(0.f, 0.f) : normalized(nrm);
 }
 
-__global__ void __launch_bounds__(kBlock) k_virt_data(sphnj_params p, DevState d) {
-    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+template <class G> __global__ void __launch_bounds__(kBlock) k_virt_data(const __grid_constant__ G g) {
+    SPHNJ_SCENE(g);
+    const int i = blk * blockDim.x + threadIdx.x;
     if (i >= p.virt_number) return;
     const int nx = p.cell_number[0], ny = p.cell_number[1];
     const float R2 = p.impact_distance_square, hinv2 = p.smoothing_length_inverse_square;
@@ -111,8 +113,9 @@ __global__ void __launch_bounds__(kBlock) k_virt_data(sphnj_params p, DevState d
                  powf(pv * by_phase(p.coefficient_p2rho, phase) + 1.0f, by_phase(p.gamma_inv, phase));
 }
 
-__global__ void __launch_bounds__(kBlock) k_solid_couple(sphnj_params p, DevState d) {
-    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+template <class G> __global__ void __launch_bounds__(kBlock) k_solid_couple(const __grid_constant__ G g) {
+    SPHNJ_SCENE(g);
+    const int i = blk * blockDim.x + threadIdx.x;
     if (i >= p.solid_number) return;
     const int nx = p.cell_number[0], ny = p.cell_number[1];
     const float R2 = p.impact_distance_square, hinv2 = p.smoothing_length_inverse_square;
@@ -199,8 +202,9 @@ __device__ __forceinline__ bool ref_within(const sphnj_params &p, double2 dref) 
     return __double2float_rn(dref.x * dref.x + dref.y * dref.y) < p.impact_distance_square;
 }
 
-__global__ void __launch_bounds__(kBlock) k_solid_deform(sphnj_params p, DevState d) {
-    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+template <class G> __global__ void __launch_bounds__(kBlock) k_solid_deform(const __grid_constant__ G g) {
+    SPHNJ_SCENE(g);
+    const int i = blk * blockDim.x + threadIdx.x;
     if (i >= p.solid_number) return;
     const int nx = p.cell_number[0], ny = p.cell_number[1];
     dmat2 L = {0, 0, 0, 0}, Ft = {0, 0, 0, 0};
@@ -245,8 +249,9 @@ __global__ void __launch_bounds__(kBlock) k_solid_deform(sphnj_params p, DevStat
     d.s_L[i] = L;
 }
 
-__global__ void __launch_bounds__(kBlock) k_solid_force(sphnj_params p, DevState d) {
-    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+template <class G> __global__ void __launch_bounds__(kBlock) k_solid_force(const __grid_constant__ G g) {
+    SPHNJ_SCENE(g);
+    const int i = blk * blockDim.x + threadIdx.x;
     if (i >= p.solid_number) return;
     const int nx = p.cell_number[0], ny = p.cell_number[1];
     const float R2 = p.impact_distance_square, hinv2 = p.smoothing_length_inverse_square;
@@ -315,8 +320,9 @@ __global__ void __launch_bounds__(kBlock) k_solid_force(sphnj_params p, DevState
     d.s_dudt[i] = make_double2(acc.x + (double)couple.x, acc.y + (double)couple.y);
 }
 
-__global__ void __launch_bounds__(256) k_solid_update(sphnj_params p, DevState d) {
-    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+template <class G> __global__ void __launch_bounds__(256) k_solid_update(const __grid_constant__ G g) {
+    SPHNJ_SCENE(g);
+    const int i = blk * blockDim.x + threadIdx.x;
     if (i >= p.solid_number) return;
     const double dt = (double)(p.dt / (float)p.solid_sub_step);
     const int bt = d.s_bt[i];
@@ -344,23 +350,47 @@ __global__ void __launch_bounds__(256) k_solid_update(sphnj_params p, DevState d
 
 }  // namespace
 
-void launch_virt_normal(cudaStream_t st, const sphnj_params &p, const DevState &d) {
-    if (p.virt_number > 0) k_virt_normal<<<grid_for(p.virt_number, 256), 256, 0, st>>>(p, d);
+template <class G> int launch_virt_normal(cudaStream_t st, G &g) {
+    return launch(
+        g, site_key(SITE_VIRT_NORMAL), [](const Scene &s) { return grid_for(s.p.virt_number, 256); },
+        k_virt_normal<typename G::Dev>, 256, 0, st);
 }
-void launch_virt_data(cudaStream_t st, const sphnj_params &p, const DevState &d) {
-    if (p.virt_number > 0) k_virt_data<<<grid_for(p.virt_number, kBlock), kBlock, 0, st>>>(p, d);
+template <class G> int launch_virt_data(cudaStream_t st, G &g) {
+    return launch(
+        g, site_key(SITE_VIRT_DATA), [](const Scene &s) { return grid_for(s.p.virt_number, kBlock); },
+        k_virt_data<typename G::Dev>, kBlock, 0, st);
 }
-void launch_solid_couple(cudaStream_t st, const sphnj_params &p, const DevState &d) {
-    if (p.solid_number > 0) k_solid_couple<<<grid_for(p.solid_number, kBlock), kBlock, 0, st>>>(p, d);
+template <class G> int launch_solid_couple(cudaStream_t st, G &g) {
+    return launch(
+        g, site_key(SITE_COUPLE),
+        [](const Scene &s) { return s.p.fluid_number_total > 0 ? grid_for(s.p.solid_number, kBlock) : 0u; },
+        k_solid_couple<typename G::Dev>, kBlock, 0, st);
 }
-void launch_solid_deformation(cudaStream_t st, const sphnj_params &p, const DevState &d) {
-    if (p.solid_number > 0) k_solid_deform<<<grid_for(p.solid_number, kBlock), kBlock, 0, st>>>(p, d);
+// scenes with fewer solid sub-steps per fluid step own no block of sub-step `sub`
+inline unsigned solid_blocks(const sphnj_params &p, int sub, int block) {
+    return sub < p.solid_sub_step ? grid_for(p.solid_number, block) : 0u;
 }
-void launch_solid_force(cudaStream_t st, const sphnj_params &p, const DevState &d) {
-    if (p.solid_number > 0) k_solid_force<<<grid_for(p.solid_number, kBlock), kBlock, 0, st>>>(p, d);
+template <class G> int launch_solid_deformation(cudaStream_t st, G &g, int sub) {
+    return launch(
+        g, site_key(SITE_SOLID_DEFORM, sub), [sub](const Scene &s) { return solid_blocks(s.p, sub, kBlock); },
+        k_solid_deform<typename G::Dev>, kBlock, 0, st);
 }
-void launch_solid_update(cudaStream_t st, const sphnj_params &p, const DevState &d) {
-    if (p.solid_number > 0) k_solid_update<<<grid_for(p.solid_number, 256), 256, 0, st>>>(p, d);
+template <class G> int launch_solid_force(cudaStream_t st, G &g, int sub) {
+    return launch(
+        g, site_key(SITE_SOLID_FORCE, sub), [sub](const Scene &s) { return solid_blocks(s.p, sub, kBlock); },
+        k_solid_force<typename G::Dev>, kBlock, 0, st);
 }
+template <class G> int launch_solid_update(cudaStream_t st, G &g, int sub) {
+    return launch(
+        g, site_key(SITE_SOLID_UPDATE, sub), [sub](const Scene &s) { return solid_blocks(s.p, sub, 256); },
+        k_solid_update<typename G::Dev>, 256, 0, st);
+}
+
+SPHNJ_INSTANTIATE_GROUPS(launch_virt_normal);
+SPHNJ_INSTANTIATE_GROUPS(launch_virt_data);
+SPHNJ_INSTANTIATE_GROUPS(launch_solid_couple);
+SPHNJ_INSTANTIATE_GROUPS(launch_solid_deformation, int);
+SPHNJ_INSTANTIATE_GROUPS(launch_solid_force, int);
+SPHNJ_INSTANTIATE_GROUPS(launch_solid_update, int);
 
 }  // namespace sphnj

@@ -69,18 +69,28 @@ extern "C" int sphnj_rebuild_cell_lists_noalloc(int nx, int ny, int n_particles,
     int rc = scratch_for_current_device(&scratch);
     if (rc) return rc;
     const int C = nx * ny;
-    sphnj_params p{};
-    p.cell_number[0] = nx;
-    p.cell_number[1] = ny;
-    p.cell_number_total = C;
-    sphnj::ListScratch sc{};
-    sc.cnt9 = scratch;
-    sc.local = scratch + (size_t)9 * kMaxCells;
-    sc.sums = scratch + (size_t)10 * kMaxCells;
-    sphnj::CellList prev{reinterpret_cast<int2 *>(const_cast<int32_t *>(prev_range)), const_cast<int32_t *>(prev_list)};
-    sphnj::CellList cur{reinterpret_cast<int2 *>(range_out), list_out};
     cudaStream_t st = static_cast<cudaStream_t>(stream);
-    sphnj::launch_rebuild_kind(st, p, n_particles, cell_id, prev, cur, sc, nullptr);
+    if (n_particles == 0) {
+        // no particles: every cell starts at 0 and holds none
+        cudaError_t e = cudaMemsetAsync(range_out, 0, sizeof(int32_t) * 2 * (size_t)C, st);
+        return e == cudaSuccess ? SPHNJ_OK : SPHNJ_ERR_CUDA;
+    }
+    // A scene record holding only what the rebuild reads: the grid, the
+    // particles' cell ids (as fluid, with no listing), the two list buffers
+    // (previous = 0, output = 1) and the static scratch.
+    sphnj::GroupOne g{};
+    sphnj::Scene &s = g.s;
+    s.p.cell_number[0] = nx;
+    s.p.cell_number[1] = ny;
+    s.p.cell_number_total = C;
+    s.p.fluid_number_total = n_particles;
+    s.d.f_cell = const_cast<int32_t *>(cell_id);
+    s.sc.cnt9 = scratch;
+    s.sc.local = scratch + (size_t)9 * kMaxCells;
+    s.sc.sums = scratch + (size_t)10 * kMaxCells;
+    s.lf[0] = {reinterpret_cast<int2 *>(const_cast<int32_t *>(prev_range)), const_cast<int32_t *>(prev_list)};
+    s.lf[1] = {reinterpret_cast<int2 *>(range_out), list_out};
+    sphnj::launch_rebuild_kind(st, g, sphnj::KF, 1);
     cudaError_t e = cudaGetLastError();
     return e == cudaSuccess ? SPHNJ_OK : SPHNJ_ERR_CUDA;
 }
