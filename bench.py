@@ -53,6 +53,8 @@ def parse():
     ap.add_argument("--tile-h", type=int, default=16, help="cells per tile of the neighbour sweeps")
     ap.add_argument("--no-graphs", action="store_true", help="issue every kernel of a step instead of replaying "
                                                              "the step's captured CUDA graph")
+    ap.add_argument("--form", default="plain", choices=["plain", "mixed"],
+                    help="plain: the reference's precision; mixed: the mixed-precision form")
     ap.add_argument("--no-sweep", action="store_true", help="skip the 256-scene batched sweep")
     ap.add_argument("--sweep-steps", type=int, default=20, help="timed steps of the 256-scene sweep")
     return ap.parse_args()
@@ -177,18 +179,12 @@ def run_sweep(args, stream):
     import torch
 
     import sphnj_gb300 as S
-    from sphnj_gb300 import cases
+    from sphnj_gb300 import abi, cases
 
     t0 = time.perf_counter()
     scenes = [cases.sweep_scene(s) for s in range(cases.SWEEP_SCENES)]
     params = [c.params() for c in scenes]
-    sims = []
-    for c, p in zip(scenes, params):
-        sim = S.Simulation(p)
-        sim.set_stream(stream.cuda_stream)
-        sim.set_tiling(True, args.tile_h)
-        sim.upload(c.arrays())
-        sims.append(sim)
+    arrays = [c.arrays() for c in scenes]
     setup_s = time.perf_counter() - t0
     units = sum(p.fluid_number_total + p.solid_number for p in params)
     K = args.sweep_steps
@@ -202,6 +198,21 @@ def run_sweep(args, stream):
         torch.cuda.synchronize()
         return e0.elapsed_time(e1)
 
+    def make(form):
+        sims = []
+        for p, a in zip(params, arrays):
+            sim = S.Simulation(p, form)
+            sim.set_stream(stream.cuda_stream)
+            sim.set_tiling(True, args.tile_h)
+            sim.upload(a)
+            sims.append(sim)
+        return sims
+
+    def rate(ms):
+        return {"value": units * K / (ms / 1e3), "ms_per_step": ms / K}
+
+    # plain form, scene by scene
+    sims = make(abi.FORM_PLAIN)
     for sim in sims:
         sim.step(args.warmup)
     lp0 = sum(sim.launches() for sim in sims)
@@ -209,35 +220,41 @@ def run_sweep(args, stream):
     launches_plain = sum(sim.launches() for sim in sims) - lp0
     for sim in sims:
         sim.synchronize()
-    b = S.Batch(sims)
-    b.set_stream(stream.cuda_stream)
-    b.set_tiling(True, args.tile_h)
-    b.step(args.warmup)
-    l0 = b.launches()
-    ms_batch = timed(lambda: b.step(K))
-    launches_batch = b.launches() - l0
-    b.synchronize()
-    b.profile_enable(True)
-    b.step(K)
-    prof = b.profile_read()
-    b.profile_enable(False)
-    b.close()
-    for sim in sims:
         sim.close()
-    total = sum(v[0] for v in prof.values())
+
+    # batched, each form
+    out = {}
+    for name, form in (("batched", abi.FORM_PLAIN), ("batched_mixed", abi.FORM_MIXED)):
+        sims = make(form)
+        b = S.Batch(sims)
+        b.set_stream(stream.cuda_stream)
+        b.set_tiling(True, args.tile_h)
+        b.step(args.warmup)
+        l0 = b.launches()
+        ms = timed(lambda: b.step(K))
+        launches = b.launches() - l0
+        b.synchronize()
+        b.profile_enable(True)
+        b.step(K)
+        prof = b.profile_read()
+        b.profile_enable(False)
+        b.close()
+        for sim in sims:
+            sim.close()
+        total = sum(v[0] for v in prof.values())
+        out[name] = dict(rate(ms), launches_per_step=launches / K,
+                         stage_share={k: round(v[0] / total, 4) for k, v in prof.items() if v[1]})
+        out[name + "_over_plain"] = ms_plain / ms
     return {
         "workload": "256 independent scenes (seeds 0..255): 128 water dam breaks of 2k-60k particles "
                     "(H/W in [0.5, 2.5]), 128 cantilever beams of 1k-20k particles (E 0.5-20 MPa, "
                     "nu 0.3-0.45, L 0.1-0.3 m), +-0.01 dx jitter",
-        "scenes": len(sims), "particles": units, "steps": K, "warmup": args.warmup,
-        "plain_scene_by_scene": {"value": units * K / (ms_plain / 1e3), "ms_per_step": ms_plain / K,
-                                 "launches_per_step": launches_plain / K},
-        "batched": {"value": units * K / (ms_batch / 1e3), "ms_per_step": ms_batch / K,
-                    "launches_per_step": launches_batch / K},
-        "batched_over_plain": ms_plain / ms_batch,
-        "batched_stage_share": {k: round(v[0] / total, 4) for k, v in prof.items() if v[1]},
+        "scenes": len(params), "particles": units, "steps": K, "warmup": args.warmup,
+        "plain_scene_by_scene": dict(rate(ms_plain), launches_per_step=launches_plain / K),
+        **out,
         "setup_s": setup_s,
-        "form": "plain precision in both (the batched form changes only how launches cover scenes)",
+        "forms": "plain: reference precision; mixed: FP32 pair loops, cell + offset positions with Kahan "
+                 "integration, FP64 correction inverse and F/PK1 step",
     }
 
 
@@ -260,7 +277,8 @@ def run_ours(args):
     nf, ns, nv = p.fluid_number_total, p.solid_number, p.virt_number
     units = nf + ns
     stream = torch.cuda.Stream()
-    sim = S.Simulation(p)
+    form = abi.FORM_MIXED if args.form == "mixed" else abi.FORM_PLAIN
+    sim = S.Simulation(p, form)
     sim.set_stream(stream.cuda_stream)
     sim.set_tiling(not args.untiled, args.tile_h)
     sim.set_graphs(not args.no_graphs)
@@ -377,7 +395,8 @@ def run_ours(args):
         "vs_baseline": None, "dtype": "f32",
         "data": "synthetic (lattice gas-liquid dam break generated in-process, reference .dat layout)",
         "config": {"workload": f"gas-liquid dam break, 1.0x2.0 m water in a 4.0x3.0 m air-filled tank, dx={args.dx}",
-                   "form": "plain (reference precision and cell-list order)",
+                   "form": "plain (reference precision and cell-list order)" if form == abi.FORM_PLAIN else
+                           "mixed (FP32 pair loops, cell + offset positions with Kahan integration)",
                    "sweeps": "per-particle" if args.untiled else f"tiled, {args.tile_h} cells per tile",
                    "launch": "direct" if args.no_graphs else "one CUDA graph per kind of step", "n_fluid": nf, "n_liquid": p.fluid_number[0],
                    "n_solid": ns, "n_virt": nv, "cells": p.cell_number_total, "shift_per_step": p.shift_per_step,

@@ -212,6 +212,18 @@ typedef struct sphnj_host_state {
 /* ---- forms ---------------------------------------------------------------- */
 #define SPHNJ_FORM_PLAIN  0   /* reference precision (fluid FP32, solid FP64),
                                  reference cell-list order and stage order    */
+#define SPHNJ_FORM_MIXED  1   /* mixed precision: FP32 in every pair loop;
+                                 positions as integer cell + FP32 offset,
+                                 integrated with Kahan compensation (fluid
+                                 position and velocity; solid displacement
+                                 and velocity); solids in total-Lagrangian
+                                 displacement form with FP64 only for the 2x2
+                                 correction-matrix inverse and the deformation
+                                 gradient / PK1 stress step.  Same stages,
+                                 lists and order as the plain form; results
+                                 differ from it in rounding only.  The host
+                                 state in and out is the plain layout (upload
+                                 splits positions, download joins them). */
 
 /* ---- host-side parameter and case I/O (no GPU needed) --------------------- */
 

@@ -32,6 +32,7 @@ TRANSIENT, STEADY = 0, 1
 
 CELL_SIZE = 64
 FORM_PLAIN = 0
+FORM_MIXED = 1
 
 F_FLUID_KINEMATICS = 1 << 0
 F_FLUID_THERMO = 1 << 1

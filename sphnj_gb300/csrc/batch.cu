@@ -130,6 +130,7 @@ int sphnj_batch_create(sphnj_ctx *const *scenes, int n, sphnj_batch **out) {
         }
     }
     b->g.n = n;
+    b->g.form = c0->form;
     if (configure_sweeps(b->tiles) != cudaSuccess) {
         cudaGetLastError();
         for (Scene *r : b->d_recs) cudaFree(r);

@@ -183,6 +183,16 @@ size_t layout(sphnj_ctx *ctx, char *base) {
         ctx->ls[k].rng = a.take<int2>(C); ctx->ls[k].lst = a.take<int>(ns);
     }
     ctx->lv.rng = a.take<int2>(C); ctx->lv.lst = a.take<int>(nv);
+    const bool mixed = ctx->form == SPHNJ_FORM_MIXED;
+    if (mixed) {
+        d.f_off = a.take<float2>(nf); d.f_offc = a.take<float2>(nf); d.f_velc = a.take<float2>(nf);
+        d.s_rc = a.take<int2>(ns);
+        d.s_roff = a.take<float2>(ns); d.s_u = a.take<float2>(ns); d.s_uc = a.take<float2>(ns);
+        d.s_v = a.take<float2>(ns); d.s_vc = a.take<float2>(ns); d.s_off = a.take<float2>(ns);
+        d.s_acc = a.take<float2>(ns);
+        d.s_PL = a.take<float4>(ns); d.s_FL = a.take<float4>(ns);
+        d.v_off = a.take<float2>(nv);
+    }
     ctx->sc.cnt9 = a.take<int>((size_t)9 * C);
     ctx->sc.cnt = a.take<int>(C);
     ctx->sc.local = a.take<int>(C);
@@ -190,7 +200,9 @@ size_t layout(sphnj_ctx *ctx, char *base) {
     ctx->sc.cursor = a.take<int>(C);
     ctx->sc.bucket = a.take<int>(nmax);
     ctx->sc.sorted = a.take<int>(nmax);
-    size_t pay = std::max((size_t)nf * 30, std::max((size_t)ns * 86, (size_t)nv * 21)) + 8 * 256;
+    // sort payload staging: the per-kind column sets of kernels_cells.cu
+    const size_t pf = mixed ? 54 : 30, ps = mixed ? 142 : 86, pv = mixed ? 29 : 21;
+    size_t pay = std::max((size_t)nf * pf, std::max((size_t)ns * ps, (size_t)nv * pv)) + 16 * 256;
     ctx->payload = a.take<char>(pay);
     d.max_speed2_bits = a.take<unsigned int>(1);
     d.err = a.take<DevErr>(1);
@@ -296,7 +308,7 @@ extern "C" {
 int sphnj_create(const sphnj_params *p, int form, sphnj_ctx **out) {
     if (!p || !out) return SPHNJ_ERR_ARG;
     *out = nullptr;
-    if (form != SPHNJ_FORM_PLAIN) return SPHNJ_ERR_UNSUPPORTED;
+    if (form != SPHNJ_FORM_PLAIN && form != SPHNJ_FORM_MIXED) return SPHNJ_ERR_UNSUPPORTED;
     if (p->fluid_number_total < 0 || p->solid_number < 0 || p->virt_number < 0) return SPHNJ_ERR_ARG;
     if (p->cell_number[0] < 3 || p->cell_number[1] < 3 ||
         (long)p->cell_number[0] * p->cell_number[1] != p->cell_number_total)
@@ -424,11 +436,11 @@ int sphnj_upload(sphnj_ctx *ctx, const sphnj_host_state *s) {
     ctx->step = p.istart;
     bind_lists(ctx);
     // wall normals once before the loop (virtNormalCalculation, calculation.cu:28)
+    GroupOne g{scene_of(ctx, ctx->parity), ctx->form};
     if (s->virt_normal) RET(h2d(ctx, d.v_normal, s->virt_normal, nv));
-    else {
-        GroupOne g{scene_of(ctx, ctx->parity)};
-        launch_virt_normal(st, g);
-    }
+    else launch_virt_normal(st, g);
+    // mixed form: cells + offsets, displacements and compensations
+    if (ctx->form == SPHNJ_FORM_MIXED) launch_mixed_split(st, g, 7);
     CK(cudaGetLastError());
     CK(cudaStreamSynchronize(st));
     ctx->uploaded = true;
@@ -534,7 +546,7 @@ extern "C" int sphnj_step(sphnj_ctx *ctx, int n) {
     cudaStream_t st = ctx->st;
     for (int it = 0; it < n; ++it) {
         const StepKind k = advance(ctx);
-        GroupOne g{scene_of(ctx, k.parity)};
+        GroupOne g{scene_of(ctx, k.parity), ctx->form};
         if (ctx->use_graphs && !ctx->prof.on) {
             auto it_g = ctx->graphs.find(k.key());
             if (it_g == ctx->graphs.end()) {
@@ -576,6 +588,21 @@ int sphnj_upload_fields(sphnj_ctx *ctx, uint32_t mask, const sphnj_host_state *s
     const sphnj_params &p = ctx->p;
     const int nf = p.fluid_number_total, ns = p.solid_number, nv = p.virt_number;
     DevState &d = ctx->d;
+    // Mixed form: the host-layout mirrors are refreshed from the state first,
+    // so that a kind whose positions are re-split keeps its other fields; only
+    // kinds whose positions are given are re-split (a round trip through an
+    // absolute FP32 position would lose the offset's precision).
+    const bool mixed = ctx->form == SPHNJ_FORM_MIXED;
+    int resplit = 0;
+    if (mixed) {
+        if ((mask & SPHNJ_F_FLUID_KINEMATICS) && s->fluid_position) resplit |= 1;
+        if ((mask & SPHNJ_F_SOLID_KINEMATICS) &&
+            (s->solid_position || s->solid_reference_position || s->solid_velocity))
+            resplit |= 2;
+        launch_mixed_join(ctx->st, GroupOne{scene_of(ctx, ctx->parity), ctx->form});
+        if ((mask & SPHNJ_F_FLUID_KINEMATICS) && s->fluid_velocity && !s->fluid_position)
+            CK(cudaMemsetAsync(d.f_velc, 0, sizeof(float2) * (size_t)nf, ctx->st));
+    }
     if (mask & SPHNJ_F_FLUID_KINEMATICS) {
         if (s->fluid_position) RET(h2d(ctx, d.f_pos, s->fluid_position, nf));
         if (s->fluid_velocity) RET(h2d(ctx, d.f_vel, s->fluid_velocity, nf));
@@ -623,6 +650,7 @@ int sphnj_upload_fields(sphnj_ctx *ctx, uint32_t mask, const sphnj_host_state *s
         if (s->virt_density) RET(h2d(ctx, d.v_rho, s->virt_density, nv));
         if (s->virt_phase) RET(enum_h2d(ctx, d.v_phase, s->virt_phase, nv));
     }
+    if (resplit) launch_mixed_split(ctx->st, GroupOne{scene_of(ctx, ctx->parity), ctx->form}, resplit);
     CK(cudaGetLastError());
     CK(cudaStreamSynchronize(ctx->st));
     return SPHNJ_OK;
@@ -681,6 +709,10 @@ int sphnj_download(sphnj_ctx *ctx, uint32_t mask, sphnj_host_state *s) {
     const sphnj_params &p = ctx->p;
     const int nf = p.fluid_number_total, ns = p.solid_number, nv = p.virt_number;
     const DevState &d = ctx->d;
+    // mixed form: absolute positions and FP64 solid kinematics from the state
+    if (ctx->form == SPHNJ_FORM_MIXED && (mask & (SPHNJ_F_FLUID_KINEMATICS | SPHNJ_F_SOLID_KINEMATICS |
+                                                  SPHNJ_F_SOLID_DERIVED)))
+        launch_mixed_join(ctx->st, GroupOne{scene_of(ctx, ctx->parity), ctx->form});
     if (mask & SPHNJ_F_FLUID_KINEMATICS) {
         RET(d2h(ctx, s->fluid_position, d.f_pos, nf));
         RET(d2h(ctx, s->fluid_velocity, d.f_vel, nf));

@@ -75,6 +75,18 @@ struct DevState {
     // scalars
     unsigned int *max_speed2_bits;  // max over fluid of |v|^2 (float bits)
     DevErr *err;
+    // ---- mixed-precision form only (null in the plain form) ----------------
+    // Positions are an integer cell (f_cell, s_cell, v_cell: the cell the
+    // particle is listed in) plus an FP32 offset from that cell's lower-left
+    // corner; fluid positions and velocities carry Kahan compensations.
+    float2 *f_off, *f_offc, *f_velc;
+    // Solids: reference position = reference cell (x, y) + FP32 offset;
+    // current position = reference position + FP32 displacement u (Kahan);
+    // s_off is the current offset from the corner of s_cell (set by binning).
+    int2 *s_rc;
+    float2 *s_roff, *s_u, *s_uc, *s_v, *s_vc, *s_off, *s_acc;
+    float4 *s_PL, *s_FL;  // P L and F L of the last deformation pass (FP32, column-major)
+    float2 *v_off;
 };
 
 __device__ __forceinline__ void raise_error(DevErr *e, int code, int a = 0, int b = 0, int c = 0) {

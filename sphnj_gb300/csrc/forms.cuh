@@ -1,0 +1,112 @@
+// The two forms of the method, as the neighbour loops see them.
+//
+// FormPlain  the reference's precision (include/types.h): fluid and virtual
+//            positions absolute FP32, solid state FP64.  Pair vectors are
+//            differences of absolute positions, exactly as the reference
+//            forms them.
+// FormMixed  positions are an integer cell plus an FP32 offset from the
+//            cell's lower-left corner.  A neighbour loop works in the frame
+//            of one cell (the home particle's own cell, or the origin of a
+//            tile): a particle listed in cell m sits at
+//                (m - frame) * cell width + its offset,
+//            which keeps ~eps * (a few cell widths) of absolute precision
+//            anywhere in the domain instead of eps * |x|.
+#pragma once
+
+#include "device_common.cuh"
+
+namespace sphnj {
+
+__device__ __forceinline__ float2 add2(float2 a, float2 b) { return make_float2(a.x + b.x, a.y + b.y); }
+
+// Frame arithmetic of the mixed form is written with round-to-nearest
+// intrinsics: a frame shift k * width is loop-invariant in the neighbour
+// loops, and left to the compiler it may be hoisted (two roundings) in one
+// instantiation of a kernel and contracted into an FMA with the offset (one
+// rounding) in another - the one-scene and batched launches would then
+// differ in the last bit.
+__device__ __forceinline__ float2 add2_rn(float2 a, float2 b) {
+    return make_float2(__fadd_rn(a.x, b.x), __fadd_rn(a.y, b.y));
+}
+__device__ __forceinline__ float2 cells_to_len(const sphnj_params &p, int kx, int ky) {
+    return make_float2(__fmul_rn((float)kx, p.interval[0]), __fmul_rn((float)ky, p.interval[1]));
+}
+
+// Home cell minus frame cell, in cells (mixed form; ignored by the plain form).
+struct Frame {
+    int dx, dy;
+};
+
+struct FormPlain {
+    static constexpr bool kMixed = false;
+    // frame shift of neighbour slot n (0..8) of the home cell
+    __device__ static __forceinline__ float2 shift(const sphnj_params &, Frame, int) { return make_float2(0.f, 0.f); }
+    __device__ static __forceinline__ float2 f_home(const sphnj_params &, const DevState &d, Frame, int i) {
+        return d.f_pos[i];
+    }
+    __device__ static __forceinline__ float2 f_nbr(const DevState &d, int j, float2) { return __ldg(&d.f_pos[j]); }
+    __device__ static __forceinline__ float2 s_home(const sphnj_params &, const DevState &d, Frame, int i) {
+        return to_f2(d.s_pos[i]);
+    }
+    __device__ static __forceinline__ float2 s_nbr(const DevState &d, int j, float2) { return to_f2(d.s_pos[j]); }
+    __device__ static __forceinline__ float2 s_vel(const DevState &d, int j) { return to_f2(d.s_vel[j]); }
+    __device__ static __forceinline__ float2 v_home(const sphnj_params &, const DevState &d, Frame, int i) {
+        return d.v_pos[i];
+    }
+    __device__ static __forceinline__ float2 v_nbr(const DevState &d, int j, float2) { return __ldg(&d.v_pos[j]); }
+};
+
+struct FormMixed {
+    static constexpr bool kMixed = true;
+    __device__ static __forceinline__ float2 shift(const sphnj_params &p, Frame f, int n) {
+        return cells_to_len(p, f.dx + n / 3 - 1, f.dy + n % 3 - 1);
+    }
+    __device__ static __forceinline__ float2 corner(const sphnj_params &p, Frame f) {
+        return cells_to_len(p, f.dx, f.dy);
+    }
+    __device__ static __forceinline__ float2 f_home(const sphnj_params &p, const DevState &d, Frame f, int i) {
+        return add2_rn(d.f_off[i], corner(p, f));
+    }
+    __device__ static __forceinline__ float2 f_nbr(const DevState &d, int j, float2 sh) {
+        return add2_rn(__ldg(&d.f_off[j]), sh);
+    }
+    __device__ static __forceinline__ float2 s_home(const sphnj_params &p, const DevState &d, Frame f, int i) {
+        return add2_rn(d.s_off[i], corner(p, f));
+    }
+    __device__ static __forceinline__ float2 s_nbr(const DevState &d, int j, float2 sh) {
+        return add2_rn(__ldg(&d.s_off[j]), sh);
+    }
+    __device__ static __forceinline__ float2 s_vel(const DevState &d, int j) { return __ldg(&d.s_v[j]); }
+    __device__ static __forceinline__ float2 v_home(const sphnj_params &p, const DevState &d, Frame f, int i) {
+        return add2_rn(d.v_off[i], corner(p, f));
+    }
+    __device__ static __forceinline__ float2 v_nbr(const DevState &d, int j, float2 sh) {
+        return add2_rn(__ldg(&d.v_off[j]), sh);
+    }
+};
+
+// Current position of a solid particle relative to the corner of cell c:
+// its reference offset plus displacement, shifted by (reference cell - c).
+// Binning and every solid sub-step write it, so the neighbour loops of the
+// rest of the step see the solid where it is now.
+__device__ __forceinline__ float2 solid_offset(const sphnj_params &p, int2 rc, float2 roff, float2 u, int c) {
+    const int ny = p.cell_number[1];
+    const int cx = c / ny, cy = c - cx * ny;
+    return add2_rn(add2_rn(roff, u), cells_to_len(p, rc.x - cx, rc.y - cy));
+}
+
+// Kahan-compensated accumulation x += y with compensation c (Kahan 1965,
+// "Further remarks on reducing truncation errors"): c carries the low-order
+// part lost by the last addition.
+__device__ __forceinline__ void kahan_add(float &x, float &c, float y) {
+    const float yc = __fsub_rn(y, c);
+    const float t = __fadd_rn(x, yc);
+    c = __fsub_rn(__fsub_rn(t, x), yc);
+    x = t;
+}
+__device__ __forceinline__ void kahan_add2(float2 &x, float2 &c, float2 y) {
+    kahan_add(x.x, c.x, y.x);
+    kahan_add(x.y, c.y, y.y);
+}
+
+}  // namespace sphnj

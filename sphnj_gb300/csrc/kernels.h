@@ -42,6 +42,7 @@ inline long long site_key(int site, int arg = 0) { return ((long long)site << 32
 struct GroupOne {
     using Dev = One;
     Scene s;
+    int form = SPHNJ_FORM_PLAIN;
     template <class F> bool prepare(long long, F &&blocks_of, unsigned &blocks, Dev &dev) {
         blocks = blocks_of(s);
         dev.s = s;
@@ -54,6 +55,7 @@ struct GroupMany {
     using Dev = Many;
     const Scene *h_scenes = nullptr;  // host copies of the records in d_scenes
     int n = 0;
+    int form = SPHNJ_FORM_PLAIN;      // every scene of a group has the same form
     const Scene *d_scenes = nullptr;  // device records of the current parity
     // With `planning` set, prepare() builds the block table of each launch
     // (synchronous allocation and copy) and launches nothing; a launch
@@ -164,6 +166,12 @@ template <class G> int launch_solid_couple(cudaStream_t st, G &g);
 template <class G> int launch_solid_deformation(cudaStream_t st, G &g, int sub);
 template <class G> int launch_solid_force(cudaStream_t st, G &g, int sub);
 template <class G> int launch_solid_update(cudaStream_t st, G &g, int sub);
+
+// mixed form: host layout -> mixed state for the kinds in `kinds` (bit 0
+// fluid, bit 1 solid, bit 2 virtual), and mixed state -> host layout
+// (absolute positions, FP64 solid position / velocity / acceleration)
+void launch_mixed_split(cudaStream_t st, const GroupOne &g, int kinds);
+void launch_mixed_join(cudaStream_t st, const GroupOne &g);
 
 // state conversion helpers (upload / download of 32-bit enums)
 void launch_u8_from_i32(cudaStream_t st, uint8_t *dst, const int32_t *src, int n);

@@ -29,6 +29,7 @@
 //   - every kernel runs over one scene or a batch of scenes (SPHNJ_SCENE):
 //     each scene's scan, sort and rebuild use that scene's own scratch, so
 //     the scenes of a batch share launches but no data.
+#include "forms.cuh"
 #include "kernels.h"
 
 #include <climits>
@@ -46,6 +47,40 @@ __device__ __forceinline__ const CellList &list_of(const Scene &S, int k, int pa
     return k == KF ? S.lf[parity] : k == KS ? S.ls[parity] : S.lv;
 }
 
+// Mixed form: the cell of a position given as offset `off` from the corner of
+// cell (cx, cy), with `off` moved into that cell (off - k w in one rounding).
+// A cell outside the grid is reported as the reference's out-of-bounds read
+// would not be (SPHNJ_ERR_OUT_OF_GRID) and clamped to the grid, the offset
+// kept relative to the clamped cell.
+__device__ __forceinline__ int rebase(const sphnj_params &p, const DevState &d, int kind, int i, int cx, int cy,
+                                      float2 &off) {
+    const int nx = p.cell_number[0], ny = p.cell_number[1];
+    const float wx = p.interval[0], wy = p.interval[1];
+    if (!(off.x >= 0.0f && off.x < wx)) {
+        const float k = fminf(fmaxf(floorf(__fdiv_rn(off.x, wx)), -1.0e6f), 1.0e6f);
+        if (k == k) {
+            off.x = __fmaf_rn(-k, wx, off.x);
+            cx += (int)k;
+        }
+    }
+    if (!(off.y >= 0.0f && off.y < wy)) {
+        const float k = fminf(fmaxf(floorf(__fdiv_rn(off.y, wy)), -1.0e6f), 1.0e6f);
+        if (k == k) {
+            off.y = __fmaf_rn(-k, wy, off.y);
+            cy += (int)k;
+        }
+    }
+    if (cx < 0 || cx >= nx || cy < 0 || cy >= ny) {
+        raise_error(d.err, SPHNJ_ERR_OUT_OF_GRID, kind, i, cx * ny + cy);
+        const int qx = min(max(cx, 0), nx - 1), qy = min(max(cy, 0), ny - 1);
+        off.x = __fmaf_rn((float)(cx - qx), wx, off.x);
+        off.y = __fmaf_rn((float)(cy - qy), wy, off.y);
+        cx = qx;
+        cy = qy;
+    }
+    return cx * ny + cy;
+}
+
 template <class G> __global__ void k_bin(const __grid_constant__ G g, int with_virt) {
     SPHNJ_SCENE(g);
     const int nf = p.fluid_number_total, ns = p.solid_number, nv = with_virt ? p.virt_number : 0;
@@ -57,6 +92,27 @@ template <class G> __global__ void k_bin(const __grid_constant__ G g, int with_v
     }
     if (t < 1 + kMaskShifts) d.disp2_bits[t] = 0u;  // every scene has >= 256 threads
     int kind, i, c;
+    if (d.f_off) {  // mixed form
+        if (t < nf) {
+            i = (int)t;
+            const int c0 = d.f_cell[i];
+            float2 off = d.f_off[i];
+            c = rebase(p, d, 0, i, c0 / p.cell_number[1], c0 % p.cell_number[1], off);
+            if (c != c0) {
+                d.f_off[i] = off;
+                d.f_cell[i] = c;
+            }
+        } else if (t < (long)nf + ns) {
+            i = (int)(t - nf);
+            const int2 rc = d.s_rc[i];
+            const float2 roff = d.s_roff[i], u = d.s_u[i];
+            float2 off = add2_rn(roff, u);
+            c = rebase(p, d, 1, i, rc.x, rc.y, off);
+            d.s_off[i] = solid_offset(p, rc, roff, u, c);
+            d.s_cell[i] = c;
+        }
+        return;  // virtual particles keep the cells and offsets set at upload
+    }
     if (t < nf) {
         kind = 0;
         i = (int)t;
@@ -263,16 +319,23 @@ template <class T> __device__ __forceinline__ T *carve(char *&q, size_t n) {
     return r;
 }
 
+// Mixed form (`mixed`): the position is the cell + offset pair with its
+// compensation, and the velocity compensation travels too.
 struct FluidPayload {
     float2 *pos, *vel;
     float *rho, *p;
     uint8_t *phase, *fbt;
     int *cell;
-    __device__ FluidPayload(char *q, int n) {
+    float2 *off, *offc, *velc;
+    __device__ FluidPayload(char *q, int n, bool mixed) {
         pos = carve<float2>(q, n); vel = carve<float2>(q, n);
         rho = carve<float>(q, n); p = carve<float>(q, n);
         phase = carve<uint8_t>(q, n); fbt = carve<uint8_t>(q, n);
         cell = carve<int>(q, n);
+        off = offc = velc = nullptr;
+        if (mixed) {
+            off = carve<float2>(q, n); offc = carve<float2>(q, n); velc = carve<float2>(q, n);
+        }
     }
 };
 template <class G> __global__ void k_gather_fluid(const __grid_constant__ G g, int parity) {
@@ -280,10 +343,16 @@ template <class G> __global__ void k_gather_fluid(const __grid_constant__ G g, i
     const int n = p.fluid_number_total;
     const int k = blk * blockDim.x + threadIdx.x;
     if (k >= n) return;
-    const FluidPayload o(S.payload, n);
+    const FluidPayload o(S.payload, n, d.f_off != nullptr);
     if (d.f_listed) d.f_listed[k] = *d.stamp;
     const int s = S.sc.sorted[k];
-    o.pos[k] = d.f_pos[s];
+    if (o.off) {
+        o.off[k] = d.f_off[s];
+        o.offc[k] = d.f_offc[s];
+        o.velc[k] = d.f_velc[s];
+    } else {
+        o.pos[k] = d.f_pos[s];
+    }
     o.vel[k] = d.f_vel[s];
     o.rho[k] = d.f_rho[s];
     o.p[k] = d.f_p[s];
@@ -297,8 +366,14 @@ template <class G> __global__ void k_scatter_back_fluid(const __grid_constant__ 
     const int n = p.fluid_number_total;
     const int k = blk * blockDim.x + threadIdx.x;
     if (k >= n) return;
-    const FluidPayload o(S.payload, n);
-    d.f_pos[k] = o.pos[k];
+    const FluidPayload o(S.payload, n, d.f_off != nullptr);
+    if (o.off) {
+        d.f_off[k] = o.off[k];
+        d.f_offc[k] = o.offc[k];
+        d.f_velc[k] = o.velc[k];
+    } else {
+        d.f_pos[k] = o.pos[k];
+    }
     d.f_vel[k] = o.vel[k];
     d.f_rho[k] = o.rho[k];
     d.f_p[k] = o.p[k];
@@ -307,16 +382,28 @@ template <class G> __global__ void k_scatter_back_fluid(const __grid_constant__ 
     d.f_cell[k] = o.cell[k];
 }
 
+// Mixed form (`mixed`): the reference cell + offset, displacement and
+// velocity (with their compensations) replace the FP64 position and velocity.
 struct SolidPayload {
     double2 *ref, *pos, *vel;
     dmat2 *maxstrain;
     uint8_t *mat, *bt;
     int *cell;
-    __device__ SolidPayload(char *q, int n) {
+    int2 *rc;
+    float2 *roff, *u, *uc, *v, *vc, *off;
+    __device__ SolidPayload(char *q, int n, bool mixed) {
         ref = carve<double2>(q, n); pos = carve<double2>(q, n); vel = carve<double2>(q, n);
         maxstrain = carve<dmat2>(q, n);
         mat = carve<uint8_t>(q, n); bt = carve<uint8_t>(q, n);
         cell = carve<int>(q, n);
+        rc = nullptr;
+        roff = u = uc = v = vc = off = nullptr;
+        if (mixed) {
+            rc = carve<int2>(q, n);
+            roff = carve<float2>(q, n); u = carve<float2>(q, n); uc = carve<float2>(q, n);
+            v = carve<float2>(q, n); vc = carve<float2>(q, n);
+            off = carve<float2>(q, n);  // set by this step's binning, before the sort
+        }
     }
 };
 template <class G> __global__ void k_gather_solid(const __grid_constant__ G g, int parity) {
@@ -324,11 +411,21 @@ template <class G> __global__ void k_gather_solid(const __grid_constant__ G g, i
     const int n = p.solid_number;
     const int k = blk * blockDim.x + threadIdx.x;
     if (k >= n) return;
-    const SolidPayload o(S.payload, n);
+    const SolidPayload o(S.payload, n, d.s_rc != nullptr);
     const int s = S.sc.sorted[k];
     o.ref[k] = d.s_ref[s];
-    o.pos[k] = d.s_pos[s];
-    o.vel[k] = d.s_vel[s];
+    if (o.rc) {
+        o.rc[k] = d.s_rc[s];
+        o.roff[k] = d.s_roff[s];
+        o.u[k] = d.s_u[s];
+        o.uc[k] = d.s_uc[s];
+        o.v[k] = d.s_v[s];
+        o.vc[k] = d.s_vc[s];
+        o.off[k] = d.s_off[s];
+    } else {
+        o.pos[k] = d.s_pos[s];
+        o.vel[k] = d.s_vel[s];
+    }
     o.maxstrain[k] = d.s_maxstrain[s];
     o.mat[k] = d.s_mat[s];
     o.bt[k] = d.s_bt[s];
@@ -340,10 +437,20 @@ template <class G> __global__ void k_scatter_back_solid(const __grid_constant__ 
     const int n = p.solid_number;
     const int k = blk * blockDim.x + threadIdx.x;
     if (k >= n) return;
-    const SolidPayload o(S.payload, n);
+    const SolidPayload o(S.payload, n, d.s_rc != nullptr);
     d.s_ref[k] = o.ref[k];
-    d.s_pos[k] = o.pos[k];
-    d.s_vel[k] = o.vel[k];
+    if (o.rc) {
+        d.s_rc[k] = o.rc[k];
+        d.s_roff[k] = o.roff[k];
+        d.s_u[k] = o.u[k];
+        d.s_uc[k] = o.uc[k];
+        d.s_v[k] = o.v[k];
+        d.s_vc[k] = o.vc[k];
+        d.s_off[k] = o.off[k];
+    } else {
+        d.s_pos[k] = o.pos[k];
+        d.s_vel[k] = o.vel[k];
+    }
     d.s_maxstrain[k] = o.maxstrain[k];
     d.s_mat[k] = o.mat[k];
     d.s_bt[k] = o.bt[k];
@@ -354,10 +461,12 @@ struct VirtPayload {
     float2 *pos, *normal;
     uint8_t *bt;
     int *cell;
-    __device__ VirtPayload(char *q, int n) {
+    float2 *off;  // mixed form
+    __device__ VirtPayload(char *q, int n, bool mixed) {
         pos = carve<float2>(q, n); normal = carve<float2>(q, n);
         bt = carve<uint8_t>(q, n);
         cell = carve<int>(q, n);
+        off = mixed ? carve<float2>(q, n) : nullptr;
     }
 };
 template <class G> __global__ void k_gather_virt(const __grid_constant__ G g) {
@@ -365,8 +474,9 @@ template <class G> __global__ void k_gather_virt(const __grid_constant__ G g) {
     const int n = p.virt_number;
     const int k = blk * blockDim.x + threadIdx.x;
     if (k >= n) return;
-    const VirtPayload o(S.payload, n);
+    const VirtPayload o(S.payload, n, d.v_off != nullptr);
     const int s = S.sc.sorted[k];
+    if (o.off) o.off[k] = d.v_off[s];
     o.pos[k] = d.v_pos[s];
     o.normal[k] = d.v_normal[s];
     o.bt[k] = d.v_bt[s];
@@ -378,7 +488,8 @@ template <class G> __global__ void k_scatter_back_virt(const __grid_constant__ G
     const int n = p.virt_number;
     const int k = blk * blockDim.x + threadIdx.x;
     if (k >= n) return;
-    const VirtPayload o(S.payload, n);
+    const VirtPayload o(S.payload, n, d.v_off != nullptr);
+    if (o.off) d.v_off[k] = o.off[k];
     d.v_pos[k] = o.pos[k];
     d.v_normal[k] = o.normal[k];
     d.v_bt[k] = o.bt[k];

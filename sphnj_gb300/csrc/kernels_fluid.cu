@@ -32,6 +32,7 @@
 // that the reference's -use_fast_math build uses for expf and '/'
 // (CMakeLists.txt:16-19); the equation of state keeps powf, whose fast form
 // loses ~1e-4 relative pressure accuracy near the reference density.
+#include "forms.cuh"
 #include "kernels.h"
 
 #include <algorithm>
@@ -63,11 +64,15 @@ __device__ __forceinline__ float by_phase(const float (&a)[2], int ph) { return 
 // key(t): handle of the t-th entry of a fluid range; the other members read
 // that neighbour's fields.  Global: through the CSR index list.  Tile: from
 // the block's shared-memory copy.
-struct SrcGlobal {
+// x(k, sh): position of entry k in the sweep's frame; sh is the frame shift
+// of the neighbour cell the entry was listed in (mixed form).
+template <class F> struct SrcGlobal {
     const DevState *d;
     __device__ __forceinline__ int2 range(int, int2 r) const { return r; }
     __device__ __forceinline__ int key(int t) const { return __ldg(&d->lst_f[t]); }
-    __device__ __forceinline__ float2 x(int k) const { return __ldg(&d->f_pos[k]); }
+    // (the list bodies, which call x(k) without a shift, take their entries
+    // from a tile only; with a global source they return before reading)
+    __device__ __forceinline__ float2 x(int k, float2 sh = float2()) const { return F::f_nbr(*d, k, sh); }
     __device__ __forceinline__ float2 u(int k) const { return __ldg(&d->f_vel[k]); }
     __device__ __forceinline__ float rho(int k) const { return __ldg(&d->f_rho[k]); }
     __device__ __forceinline__ float pr(int k) const { return __ldg(&d->f_p[k]); }
@@ -85,7 +90,7 @@ struct SrcTile {
         return make_int2(off[strip] + r.x - base[strip], r.y);
     }
     __device__ __forceinline__ int key(int t) const { return t; }
-    __device__ __forceinline__ float2 x(int k) const { return pos[k]; }
+    __device__ __forceinline__ float2 x(int k, float2 = float2()) const { return pos[k]; }
     __device__ __forceinline__ float2 u(int k) const { return vel[k]; }
     __device__ __forceinline__ float rho(int k) const { return rp[k].x; }
     __device__ __forceinline__ float pr(int k) const { return rp[k].y; }
@@ -141,10 +146,10 @@ struct PairI {
     float p, rho, cs;
 };
 
-__device__ __forceinline__ PairI load_pair_i(const sphnj_params &p, const DevState &d, int i) {
+__device__ __forceinline__ PairI load_pair_i(const sphnj_params &p, const DevState &d, int i, float2 x) {
     PairI s;
     s.i = i;
-    s.x = d.f_pos[i];
+    s.x = x;
     s.u = d.f_vel[i];
     s.p = d.f_p[i];
     s.rho = d.f_rho[i];
@@ -192,14 +197,15 @@ __device__ __forceinline__ void store_pair(const DevState &d, int i, const FAcc 
     d.f_dudx[i] = a.du_dx;
 }
 
-// findFluidPair for particle i (fluid.cu:193-254)
-template <class Src>
-__device__ __forceinline__ void pair_particle(const sphnj_params &p, const DevState &d, const Src &src, int i) {
+// findFluidPair for particle i (fluid.cu:193-254), in frame fr
+template <class F, class Src>
+__device__ __forceinline__ void pair_particle(const sphnj_params &p, const DevState &d, const Src &src, int i,
+                                              Frame fr) {
     const int nf = p.fluid_number_total;
     const int nx = p.cell_number[0], ny = p.cell_number[1];
     const float R2 = p.impact_distance_square, hinv2 = p.smoothing_length_inverse_square;
     const bool viscid = p.is_fluid_viscid != 0;
-    const PairI si = load_pair_i(p, d, i);
+    const PairI si = load_pair_i(p, d, i, F::f_home(p, d, fr, i));
     const float2 x_i = si.x, u_i = si.u;
     const float p_i = si.p, rho_i = si.rho, cs = si.cs;
     const int ph_i = si.ph;
@@ -209,19 +215,20 @@ __device__ __forceinline__ void pair_particle(const sphnj_params &p, const DevSt
     for (int n = 0; n < 9; ++n) {
         const int m = neighbour_cell(c, n, nx, ny);
         if (m < 0) continue;
+        const float2 sh = F::shift(p, fr, n);
         const int2 rf = src.range(n / 3, __ldg(&d.rng_f[m]));
         for (int t = rf.x; t < rf.x + rf.y; ++t) {
             const int k = src.key(t);
-            const float2 dx = sub2(src.x(k), x_i);
+            const float2 dx = sub2(src.x(k, sh), x_i);
             if (sqn(dx) < R2) fluid_term(p, src, k, si, dx, a);
         }
         const int2 rs = __ldg(&d.rng_s[m]);
         for (int t = rs.x; t < rs.x + rs.y; ++t) {
             const int j = __ldg(&d.lst_s[t]);
-            const float2 dx = sub2(to_f2(d.s_pos[j]), x_i);
+            const float2 dx = sub2(F::s_nbr(d, j, sh), x_i);
             if (!(sqn(dx) < R2)) continue;
             const float kc = gw(p, sqn(dx) * hinv2);
-            const float2 u_j = to_f2(d.s_vel[j]);
+            const float2 u_j = F::s_vel(d, j);
             riemann(u_i, u_j, p_i, __ldg(&d.s_p[j]), rho_i, rho_i, cs, dx, kc, a);
             a.grad.x += dx.x * kc;
             a.grad.y += dx.y * kc;
@@ -230,7 +237,7 @@ __device__ __forceinline__ void pair_particle(const sphnj_params &p, const DevSt
         const int2 rv = __ldg(&d.rng_v[m]);
         for (int t = rv.x; t < rv.x + rv.y; ++t) {
             const int j = __ldg(&d.lst_v[t]);
-            const float2 dx = sub2(__ldg(&d.v_pos[j]), x_i);
+            const float2 dx = sub2(F::v_nbr(d, j, sh), x_i);
             if (!(sqn(dx) < R2)) continue;
             const float kc = gw(p, sqn(dx) * hinv2);
             const float rho_j = by_phase(p.reference_density, __ldg(&d.v_phase[j]));
@@ -251,19 +258,21 @@ __device__ __forceinline__ void pair_particle(const sphnj_params &p, const DevSt
 }
 
 // correctionCalculate for particle i (fluid.cu:316-367)
-template <class Src>
-__device__ __forceinline__ void shift_particle(const sphnj_params &p, const DevState &d, const Src &src, int i) {
+template <class F, class Src>
+__device__ __forceinline__ void shift_particle(const sphnj_params &p, const DevState &d, const Src &src, int i,
+                                               Frame fr) {
     const int nx = p.cell_number[0], ny = p.cell_number[1];
     const float R2 = p.impact_distance_square, hinv2 = p.smoothing_length_inverse_square;
-    const float2 x_i = d.f_pos[i];
+    const float2 x_i = F::f_home(p, d, fr, i);
     const int c = d.f_cell[i];
     float2 g = make_float2(0.f, 0.f);
     for (int n = 0; n < 9; ++n) {
         const int m = neighbour_cell(c, n, nx, ny);
         if (m < 0) continue;
+        const float2 sh = F::shift(p, fr, n);
         const int2 rf = src.range(n / 3, __ldg(&d.rng_f[m]));
         for (int t = rf.x; t < rf.x + rf.y; ++t) {
-            const float2 dx = sub2(src.x(src.key(t)), x_i);
+            const float2 dx = sub2(src.x(src.key(t), sh), x_i);
             if (sqn(dx) < R2) {
                 const float kc = gw(p, sqn(dx) * hinv2);
                 g.x += dx.x * kc;
@@ -272,7 +281,7 @@ __device__ __forceinline__ void shift_particle(const sphnj_params &p, const DevS
         }
         const int2 rs = __ldg(&d.rng_s[m]);
         for (int t = rs.x; t < rs.x + rs.y; ++t) {
-            const float2 dx = sub2(to_f2(d.s_pos[__ldg(&d.lst_s[t])]), x_i);
+            const float2 dx = sub2(F::s_nbr(d, __ldg(&d.lst_s[t]), sh), x_i);
             if (sqn(dx) < R2) {
                 const float kc = gw(p, sqn(dx) * hinv2);
                 g.x += dx.x * kc;
@@ -281,7 +290,7 @@ __device__ __forceinline__ void shift_particle(const sphnj_params &p, const DevS
         }
         const int2 rv = __ldg(&d.rng_v[m]);
         for (int t = rv.x; t < rv.x + rv.y; ++t) {
-            const float2 dx = sub2(__ldg(&d.v_pos[__ldg(&d.lst_v[t])]), x_i);
+            const float2 dx = sub2(F::v_nbr(d, __ldg(&d.lst_v[t]), sh), x_i);
             if (sqn(dx) < R2) {
                 const float kc = gw(p, sqn(dx) * hinv2);
                 g.x += dx.x * kc;
@@ -337,21 +346,19 @@ __device__ __forceinline__ float list_radius2(const sphnj_params &p) {
 
 // Pair pass for particle i at CSR position h; records its neighbour list
 // when `listable` (its tile was staged, so the source is the tile).
-template <class Src>
+template <class F, class Src>
 __device__ __forceinline__ void pair_particle_listed(const sphnj_params &p, const DevState &d, const Src &src, int i,
-                                                     int h, bool listable) {
-    const int nf = p.fluid_number_total;
+                                                     int h, bool listable, Frame fr) {
     bool ok = false;
     Strips S;
     if (listable) S = strips_of(p, d, d.f_cell[i], ok);
     if (!ok) {
         d.f_nbr_cnt[h] = kNbrNone;
-        pair_particle(p, d, src, i);
+        pair_particle<F>(p, d, src, i, fr);
         return;
     }
-    (void)nf;
     const float R2 = p.impact_distance_square, Rs2 = list_radius2(p);
-    const PairI si = load_pair_i(p, d, i);
+    const PairI si = load_pair_i(p, d, i, F::f_home(p, d, fr, i));
     uint4 *row = d.f_nbr + (size_t)h * kNbrChunks;
     // 8-slot FIFO in four registers: each push shifts the 128-bit value down
     // by 16 bits and inserts at the top, so after 8 pushes the first slot is
@@ -375,7 +382,7 @@ __device__ __forceinline__ void pair_particle_listed(const sphnj_params &p, cons
     }
     if (n > kNbrCap) {
         d.f_nbr_cnt[h] = kNbrNone;
-        pair_particle(p, d, src, i);
+        pair_particle<F>(p, d, src, i, fr);
         return;
     }
     if (n & 7) {  // last, partial chunk: move its slots to the low end
@@ -407,16 +414,16 @@ __device__ __forceinline__ void pair_particle_listed(const sphnj_params &p, cons
 
 // Shifting gradient of particle i at CSR position h through its neighbour
 // list when use_list (and it has one).
-template <class Src>
+template <class F, class Src>
 __device__ __forceinline__ void shift_particle_listed(const sphnj_params &p, const DevState &d, const Src &src, int i,
-                                                      int h, bool use_list) {
+                                                      int h, bool use_list, Frame fr) {
     const int n = use_list ? (int)d.f_nbr_cnt[h] : (int)kNbrNone;
     if (n == kNbrNone) {
-        shift_particle(p, d, src, i);
+        shift_particle<F>(p, d, src, i, fr);
         return;
     }
     const float R2 = p.impact_distance_square, hinv2 = p.smoothing_length_inverse_square;
-    const float2 x_i = d.f_pos[i];
+    const float2 x_i = F::f_home(p, d, fr, i);
     const uint4 *row = d.f_nbr + (size_t)h * kNbrChunks;
     float2 g = make_float2(0.f, 0.f);
     for (int c = 0; c < n; c += 8) {
@@ -480,6 +487,7 @@ __device__ __forceinline__ unsigned int disp2(float2 a, float2 b) {
 // has no home particle.
 struct TileGeom {
     int home_b, home_e, total;
+    int col, row0;  // the tile's column and first row (its frame origin in the mixed form)
 };
 
 __device__ __forceinline__ bool tile_setup(const sphnj_params &p, const DevState &d, int blk, int tile_h,
@@ -488,6 +496,8 @@ __device__ __forceinline__ bool tile_setup(const sphnj_params &p, const DevState
     const int tiles_y = (ny + tile_h - 1) / tile_h;
     const int ci = blk / tiles_y, cj0 = (blk - ci * tiles_y) * tile_h;
     const int cj1 = min(cj0 + tile_h, ny);
+    g.col = ci;
+    g.row0 = cj0;
     const int2 h0 = __ldg(&d.rng_f[ci * ny + cj0]), h1 = __ldg(&d.rng_f[ci * ny + cj1 - 1]);
     g.home_b = h0.x;
     g.home_e = h1.x + h1.y;
@@ -518,7 +528,28 @@ __device__ __forceinline__ bool tile_setup(const sphnj_params &p, const DevState
 
 __device__ __forceinline__ int tile_strip(const int *s_off, int k) { return k < s_off[1] ? 0 : (k < s_off[2] ? 1 : 2); }
 
-template <class G>
+// Position of fluid particle j, listed in column strip s of tile g, as the
+// tile stages it: absolute (plain) or relative to the tile's origin cell
+// (mixed).
+template <class F>
+__device__ __forceinline__ float2 tile_pos(const sphnj_params &p, const DevState &d, const TileGeom &g, int s, int j) {
+    if constexpr (F::kMixed) {
+        const int col = g.col + s - 1;
+        const int row = __ldg(&d.f_cell[j]) - col * p.cell_number[1];
+        return add2_rn(__ldg(&d.f_off[j]), cells_to_len(p, s - 1, row - g.row0));
+    } else {
+        return __ldg(&d.f_pos[j]);
+    }
+}
+
+// Frame of home particle i in tile g (mixed form: the tile's origin cell).
+template <class F>
+__device__ __forceinline__ Frame tile_frame(const sphnj_params &p, const DevState &d, const TileGeom &g, int i) {
+    if constexpr (F::kMixed) return Frame{0, d.f_cell[i] - g.col * p.cell_number[1] - g.row0};
+    else return Frame{0, 0};
+}
+
+template <class G, class F>
 __global__ void __launch_bounds__(kTileBlock) k_fluid_pair_tiled(const __grid_constant__ G gs, int tile_h, int cap) {
     SPHNJ_SCENE(gs);
     extern __shared__ __align__(16) unsigned char smem[];
@@ -535,7 +566,7 @@ __global__ void __launch_bounds__(kTileBlock) k_fluid_pair_tiled(const __grid_co
         for (int k = threadIdx.x; k < g.total; k += blockDim.x) {
             const int s = tile_strip(s_off, k);
             const int j = __ldg(&d.lst_f[s_base[s] + k - s_off[s]]);
-            s_pos[k] = __ldg(&d.f_pos[j]);
+            s_pos[k] = tile_pos<F>(p, d, g, s, j);
             s_vel[k] = __ldg(&d.f_vel[j]);
             s_rp[k] = make_float2(__ldg(&d.f_rho[j]), __ldg(&d.f_p[j]));
             s_idx[k] = j;
@@ -545,16 +576,18 @@ __global__ void __launch_bounds__(kTileBlock) k_fluid_pair_tiled(const __grid_co
     __syncthreads();
     if (staged) {
         const SrcTile src{s_pos, s_vel, s_rp, s_fl, s_idx, s_base, s_off};
-        for (int h = g.home_b + threadIdx.x; h < g.home_e; h += blockDim.x)
-            pair_particle_listed(p, d, src, d.lst_f[h], h, true);
+        for (int h = g.home_b + threadIdx.x; h < g.home_e; h += blockDim.x) {
+            const int i = d.lst_f[h];
+            pair_particle_listed<F>(p, d, src, i, h, true, tile_frame<F>(p, d, g, i));
+        }
     } else {
-        const SrcGlobal src{&d};
+        const SrcGlobal<F> src{&d};
         for (int h = g.home_b + threadIdx.x; h < g.home_e; h += blockDim.x)
-            pair_particle_listed(p, d, src, d.lst_f[h], h, false);
+            pair_particle_listed<F>(p, d, src, d.lst_f[h], h, false, Frame{0, 0});
     }
 }
 
-template <class G>
+template <class G, class F>
 __global__ void __launch_bounds__(kTileBlock) k_shift_gradient_tiled(const __grid_constant__ G gs, int tile_h, int cap,
                                                                      int pass) {
     SPHNJ_SCENE(gs);
@@ -567,45 +600,47 @@ __global__ void __launch_bounds__(kTileBlock) k_shift_gradient_tiled(const __gri
     if (staged) {
         for (int k = threadIdx.x; k < g.total; k += blockDim.x) {
             const int s = tile_strip(s_off, k);
-            s_pos[k] = __ldg(&d.f_pos[__ldg(&d.lst_f[s_base[s] + k - s_off[s]])]);
+            s_pos[k] = tile_pos<F>(p, d, g, s, __ldg(&d.lst_f[s_base[s] + k - s_off[s]]));
         }
     }
     __syncthreads();
     const bool use_list = lists_valid(p, d, pass);
     if (staged) {
         const SrcTile src{s_pos, nullptr, nullptr, nullptr, nullptr, s_base, s_off};
-        for (int h = g.home_b + threadIdx.x; h < g.home_e; h += blockDim.x)
-            shift_particle_listed(p, d, src, d.lst_f[h], h, use_list);
+        for (int h = g.home_b + threadIdx.x; h < g.home_e; h += blockDim.x) {
+            const int i = d.lst_f[h];
+            shift_particle_listed<F>(p, d, src, i, h, use_list, tile_frame<F>(p, d, g, i));
+        }
     } else {
         // a tile the pair pass could not stage has no lists either
-        const SrcGlobal src{&d};
+        const SrcGlobal<F> src{&d};
         for (int h = g.home_b + threadIdx.x; h < g.home_e; h += blockDim.x)
-            shift_particle_listed(p, d, src, d.lst_f[h], h, false);
+            shift_particle_listed<F>(p, d, src, d.lst_f[h], h, false, Frame{0, 0});
     }
 }
 
 // Per-particle forms: every particle (listed == null), or only the particles
 // that are in no cell list.
-template <class G>
+template <class G, class F>
 __global__ void __launch_bounds__(kPairBlock) k_fluid_pair_each(const __grid_constant__ G g, int only_unlisted) {
     SPHNJ_SCENE(g);
     const int nf = p.fluid_number_total;
     if (only_unlisted && *d.f_listed_total == nf) return;
     const int stamp = *d.stamp;
-    const SrcGlobal src{&d};
+    const SrcGlobal<F> src{&d};
     for (int i = blk * blockDim.x + threadIdx.x; i < nf; i += nblk * blockDim.x)
-        if (!only_unlisted || d.f_listed[i] != stamp) pair_particle(p, d, src, i);
+        if (!only_unlisted || d.f_listed[i] != stamp) pair_particle<F>(p, d, src, i, Frame{0, 0});
 }
 
-template <class G>
+template <class G, class F>
 __global__ void __launch_bounds__(kPairBlock) k_shift_gradient_each(const __grid_constant__ G g, int only_unlisted) {
     SPHNJ_SCENE(g);
     const int nf = p.fluid_number_total;
     if (only_unlisted && *d.f_listed_total == nf) return;
     const int stamp = *d.stamp;
-    const SrcGlobal src{&d};
+    const SrcGlobal<F> src{&d};
     for (int i = blk * blockDim.x + threadIdx.x; i < nf; i += nblk * blockDim.x)
-        if (!only_unlisted || d.f_listed[i] != stamp) shift_particle(p, d, src, i);
+        if (!only_unlisted || d.f_listed[i] != stamp) shift_particle<F>(p, d, src, i, Frame{0, 0});
 }
 
 // densityToPressure, fluid.cu:15-23
@@ -615,31 +650,57 @@ __device__ __forceinline__ float density_to_pressure(const sphnj_params &p, floa
     return fmaxf(pr, p.min_pressure);
 }
 
-template <class G> __global__ void __launch_bounds__(kBlock) k_fluid_update(const __grid_constant__ G g) {
+// Lower-left corner of cell c, relative to the domain box: the box bounds in
+// the frame of cell c (mixed form), for the position clamp.
+__device__ __forceinline__ float4 box_in_cell(const sphnj_params &p, int c) {
+    const int ny = p.cell_number[1];
+    const int cx = c / ny, cy = c - cx * ny;
+    const float ox = __fmaf_rn((float)cx, p.interval[0], p.cell_xmin[0]);
+    const float oy = __fmaf_rn((float)cy, p.interval[1], p.cell_xmin[1]);
+    return make_float4(p.domain_xmin[0] - ox, p.domain_xmin[1] - oy, p.domain_xmax[0] - ox, p.domain_xmax[1] - oy);
+}
+
+// fluidUpdate (fluid.cu:256-287).  Mixed form: the position offset and the
+// velocity are integrated with Kahan compensation.
+template <class G, class F> __global__ void __launch_bounds__(kBlock) k_fluid_update(const __grid_constant__ G g) {
     SPHNJ_SCENE(g);
     const int i = blk * blockDim.x + threadIdx.x;
     unsigned int sp2 = 0u, moved2 = 0u;
     if (i < p.fluid_number_total) {
         const int ph = d.f_phase[i];
         const float dt = p.dt;
-        float2 x = d.f_pos[i], v = d.f_vel[i], a = d.f_dudt[i];
+        float2 x = F::kMixed ? d.f_off[i] : d.f_pos[i], v = d.f_vel[i], a = d.f_dudt[i];
         const float2 x0 = x;
         if (p.transient_type == SPHNJ_STEADY) {
             a.x += -0.1f * v.x;
             a.y += -0.1f * v.y;
             d.f_dudt[i] = a;
         }
-        x.x += v.x * dt;
-        x.y += v.y * dt;
-        v.x += (a.x + p.gravity[0]) * dt;
-        v.y += (a.y + p.gravity[1]) * dt;
+        if constexpr (F::kMixed) {
+            float2 xc = d.f_offc[i], vc = d.f_velc[i];
+            kahan_add2(x, xc, make_float2(v.x * dt, v.y * dt));
+            kahan_add2(v, vc, make_float2((a.x + p.gravity[0]) * dt, (a.y + p.gravity[1]) * dt));
+            const float4 box = box_in_cell(p, d.f_cell[i]);
+            if (x.x < box.x || x.x > box.z) xc.x = 0.0f;
+            if (x.y < box.y || x.y > box.w) xc.y = 0.0f;
+            x.x = fminf(fmaxf(x.x, box.x), box.z);
+            x.y = fminf(fmaxf(x.y, box.y), box.w);
+            d.f_off[i] = x;
+            d.f_offc[i] = xc;
+            d.f_velc[i] = vc;
+        } else {
+            x.x += v.x * dt;
+            x.y += v.y * dt;
+            v.x += (a.x + p.gravity[0]) * dt;
+            v.y += (a.y + p.gravity[1]) * dt;
+            x.x = fminf(fmaxf(x.x, p.domain_xmin[0]), p.domain_xmax[0]);
+            x.y = fminf(fmaxf(x.y, p.domain_xmin[1]), p.domain_xmax[1]);
+            d.f_pos[i] = x;
+        }
         float rho = d.f_rho[i] + d.f_drho[i] * dt;
         rho = fmaxf(rho, by_phase(p.min_density, ph));
         d.f_rho[i] = rho;
         d.f_p[i] = density_to_pressure(p, rho, ph);
-        x.x = fminf(fmaxf(x.x, p.domain_xmin[0]), p.domain_xmax[0]);
-        x.y = fminf(fmaxf(x.y, p.domain_xmin[1]), p.domain_xmax[1]);
-        d.f_pos[i] = x;
         d.f_vel[i] = v;
         float s2 = __fadd_rn(__fmul_rn(v.x, v.x), __fmul_rn(v.y, v.y));
         if (s2 == s2) sp2 = __float_as_uint(s2);  // NaN never wins, as on the host
@@ -661,6 +722,7 @@ __device__ __forceinline__ float2 project(float2 g, float2 disp) {
 
 // shiftDisplacementCalculate + correctionUpdate for particle i; returns the
 // squared displacement (float bits)
+template <class F>
 __device__ __forceinline__ unsigned int shift_update_particle(const sphnj_params &p, const DevState &d, int i) {
     // getMaxSpeed's clamp, fluid.cu:438-439
     const float vmax = __fsqrt_rn(__uint_as_float(*d.max_speed2_bits));
@@ -693,24 +755,37 @@ __device__ __forceinline__ unsigned int shift_update_particle(const sphnj_params
     }
     d.f_fbt[i] = bt;
     const float2 sh = make_float2(max_speed * dd.x, max_speed * dd.y);
-    const float2 x0 = d.f_pos[i];
-    float2 x = x0;
-    x.x += sh.x;
-    x.y += sh.y;
-    d.f_pos[i] = x;
     const float4 m = d.f_dudx[i];
-    float2 v = d.f_vel[i];
-    v.x += m.x * sh.x + m.z * sh.y;
-    v.y += m.y * sh.x + m.w * sh.y;
-    d.f_vel[i] = v;
-    return disp2(x0, x);
+    if constexpr (F::kMixed) {
+        float2 x = d.f_off[i], xc = d.f_offc[i], v = d.f_vel[i], vc = d.f_velc[i];
+        const float2 x0 = x;
+        kahan_add2(x, xc, sh);
+        kahan_add2(v, vc, make_float2(m.x * sh.x + m.z * sh.y, m.y * sh.x + m.w * sh.y));
+        d.f_off[i] = x;
+        d.f_offc[i] = xc;
+        d.f_vel[i] = v;
+        d.f_velc[i] = vc;
+        return disp2(x0, x);
+    } else {
+        const float2 x0 = d.f_pos[i];
+        float2 x = x0;
+        x.x += sh.x;
+        x.y += sh.y;
+        d.f_pos[i] = x;
+        float2 v = d.f_vel[i];
+        v.x += m.x * sh.x + m.z * sh.y;
+        v.y += m.y * sh.x + m.w * sh.y;
+        d.f_vel[i] = v;
+        return disp2(x0, x);
+    }
 }
 
-template <class G> __global__ void __launch_bounds__(kBlock) k_shift_update(const __grid_constant__ G g, int pass) {
+template <class G, class F>
+__global__ void __launch_bounds__(kBlock) k_shift_update(const __grid_constant__ G g, int pass) {
     SPHNJ_SCENE(g);
     const int i = blk * blockDim.x + threadIdx.x;
     unsigned int moved2 = 0u;
-    if (i < p.fluid_number_total) moved2 = shift_update_particle(p, d, i);
+    if (i < p.fluid_number_total) moved2 = shift_update_particle<F>(p, d, i);
     if (pass < kMaskShifts) block_max_to<kBlock>(moved2, &d.disp2_bits[1 + pass]);
 }
 
@@ -725,64 +800,84 @@ constexpr size_t kPairSmemPerEntry = 3 * sizeof(float2) + sizeof(int) + 1;
 cudaError_t configure_sweeps(const TileConfig &tc) {
     const size_t smem = tile_cap(tc.tile_h) * kPairSmemPerEntry;  // above 48 KB needs an opt-in
     if (smem <= 48 * 1024) return cudaSuccess;
-    cudaError_t e = cudaFuncSetAttribute(k_fluid_pair_tiled<One>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-    if (e == cudaSuccess)
-        e = cudaFuncSetAttribute(k_fluid_pair_tiled<Many>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    const int a = cudaFuncAttributeMaxDynamicSharedMemorySize;
+    cudaError_t e = cudaFuncSetAttribute(k_fluid_pair_tiled<One, FormPlain>, (cudaFuncAttribute)a, (int)smem);
+    if (e == cudaSuccess) e = cudaFuncSetAttribute(k_fluid_pair_tiled<Many, FormPlain>, (cudaFuncAttribute)a, (int)smem);
+    if (e == cudaSuccess) e = cudaFuncSetAttribute(k_fluid_pair_tiled<One, FormMixed>, (cudaFuncAttribute)a, (int)smem);
+    if (e == cudaSuccess) e = cudaFuncSetAttribute(k_fluid_pair_tiled<Many, FormMixed>, (cudaFuncAttribute)a, (int)smem);
     return e;
 }
 
 // Per-particle fallback grid of one scene: grid-stride, at most 2 blocks per SM.
 inline unsigned fallback_blocks(int n) { return n > 0 ? (unsigned)std::min<long>(kFallbackBlocks, grid_for(n, kPairBlock)) : 0u; }
 
-template <class G> int launch_fluid_pair(cudaStream_t st, G &g, const TileConfig &tc) {
+namespace {
+
+template <class F, class G> int fluid_pair(cudaStream_t st, G &g, const TileConfig &tc) {
     using D = typename G::Dev;
     if (!tc.tiled)
         return launch(
             g, site_key(SITE_PAIR_EACH), [](const Scene &s) { return grid_for(s.p.fluid_number_total, kPairBlock); },
-            k_fluid_pair_each<D>, kPairBlock, 0, st, 0);
+            k_fluid_pair_each<D, F>, kPairBlock, 0, st, 0);
     const int cap = tile_cap(tc.tile_h);
     const size_t smem = cap * kPairSmemPerEntry;
     int n = launch(
         g, site_key(SITE_PAIR_TILED, tc.tile_h),
         [&](const Scene &s) { return s.p.fluid_number_total > 0 ? tile_blocks(s.p, tc.tile_h) : 0u; },
-        k_fluid_pair_tiled<D>, kTileBlock, smem, st, tc.tile_h, cap);
+        k_fluid_pair_tiled<D, F>, kTileBlock, smem, st, tc.tile_h, cap);
     n += launch(
         g, site_key(SITE_PAIR_FALLBACK), [](const Scene &s) { return fallback_blocks(s.p.fluid_number_total); },
-        k_fluid_pair_each<D>, kPairBlock, 0, st, 1);
+        k_fluid_pair_each<D, F>, kPairBlock, 0, st, 1);
     return n;
 }
 
-template <class G> int launch_fluid_update(cudaStream_t st, G &g) {
+template <class F, class G> int fluid_update(cudaStream_t st, G &g) {
     return launch(
         g, site_key(SITE_FLUID_UPDATE), [](const Scene &s) { return grid_for(s.p.fluid_number_total, kBlock); },
-        k_fluid_update<typename G::Dev>, kBlock, 0, st);
+        k_fluid_update<typename G::Dev, F>, kBlock, 0, st);
 }
 
-template <class G> int launch_shift_gradient(cudaStream_t st, G &g, const TileConfig &tc, int pass) {
+template <class F, class G> int shift_gradient(cudaStream_t st, G &g, const TileConfig &tc, int pass) {
     using D = typename G::Dev;
     auto active = [pass](const Scene &s) { return s.p.fluid_number_total > 0 && pass < s.p.shift_per_step; };
     if (!tc.tiled)
         return launch(
             g, site_key(SITE_SHIFT_EACH, pass),
             [&](const Scene &s) { return active(s) ? grid_for(s.p.fluid_number_total, kPairBlock) : 0u; },
-            k_shift_gradient_each<D>, kPairBlock, 0, st, 0);
+            k_shift_gradient_each<D, F>, kPairBlock, 0, st, 0);
     const int cap = tile_cap(tc.tile_h);
     int n = launch(
         g, site_key(SITE_SHIFT_TILED, (tc.tile_h << 8) | pass),
-        [&](const Scene &s) { return active(s) ? tile_blocks(s.p, tc.tile_h) : 0u; }, k_shift_gradient_tiled<D>,
+        [&](const Scene &s) { return active(s) ? tile_blocks(s.p, tc.tile_h) : 0u; }, k_shift_gradient_tiled<D, F>,
         kTileBlock, cap * sizeof(float2), st, tc.tile_h, cap, pass);
     n += launch(
         g, site_key(SITE_SHIFT_FALLBACK, pass),
         [&](const Scene &s) { return active(s) ? fallback_blocks(s.p.fluid_number_total) : 0u; },
-        k_shift_gradient_each<D>, kPairBlock, 0, st, 1);
+        k_shift_gradient_each<D, F>, kPairBlock, 0, st, 1);
     return n;
 }
 
-template <class G> int launch_shift_update(cudaStream_t st, G &g, int pass) {
+template <class F, class G> int shift_update(cudaStream_t st, G &g, int pass) {
     return launch(
         g, site_key(SITE_SHIFT_UPDATE, pass),
         [pass](const Scene &s) { return pass < s.p.shift_per_step ? grid_for(s.p.fluid_number_total, kBlock) : 0u; },
-        k_shift_update<typename G::Dev>, kBlock, 0, st, pass);
+        k_shift_update<typename G::Dev, F>, kBlock, 0, st, pass);
+}
+
+}  // namespace
+
+template <class G> int launch_fluid_pair(cudaStream_t st, G &g, const TileConfig &tc) {
+    return g.form == SPHNJ_FORM_MIXED ? fluid_pair<FormMixed>(st, g, tc) : fluid_pair<FormPlain>(st, g, tc);
+}
+template <class G> int launch_fluid_update(cudaStream_t st, G &g) {
+    return g.form == SPHNJ_FORM_MIXED ? fluid_update<FormMixed>(st, g) : fluid_update<FormPlain>(st, g);
+}
+template <class G> int launch_shift_gradient(cudaStream_t st, G &g, const TileConfig &tc, int pass) {
+    return g.form == SPHNJ_FORM_MIXED ? shift_gradient<FormMixed>(st, g, tc, pass)
+                                      : shift_gradient<FormPlain>(st, g, tc, pass);
+}
+template <class G> int launch_shift_update(cudaStream_t st, G &g, int pass) {
+    return g.form == SPHNJ_FORM_MIXED ? shift_update<FormMixed>(st, g, pass) : shift_update<FormPlain>(st, g, pass);
 }
 
 SPHNJ_INSTANTIATE_GROUPS(launch_fluid_pair, const TileConfig &);

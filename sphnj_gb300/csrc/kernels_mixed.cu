@@ -1,0 +1,130 @@
+// Conversions between the host layout (absolute positions, the plain form's
+// arrays) and the mixed-precision form's state, for upload and download.
+//
+//   split  absolute position x  ->  cell (floor((x - cell_min) / width), in
+//          FP64) + FP32 offset from that cell's corner (x - corner in FP64,
+//          rounded once); solid displacement u = x - X and velocity rounded
+//          to FP32 with the rounding error kept as the Kahan compensation
+//          (value = main part - compensation).
+//   join   the inverse, in FP64: x = corner + offset - compensation.
+#include "forms.cuh"
+#include "kernels.h"
+
+namespace sphnj {
+
+namespace {
+
+constexpr int kBlock = 256;
+
+struct Grid2 {
+    double x0, y0, wx, wy;
+    int nx, ny;
+};
+__device__ __forceinline__ Grid2 grid_of(const sphnj_params &p) {
+    return {(double)p.cell_xmin[0], (double)p.cell_xmin[1], (double)p.interval[0], (double)p.interval[1],
+            p.cell_number[0], p.cell_number[1]};
+}
+
+// Cell (x, y) holding absolute position (x, y) and the FP32 offset from its
+// corner; positions outside the grid are reported and clamped into it.
+__device__ __forceinline__ int2 split_pos(const Grid2 &g, double x, double y, float2 &off, DevErr *err, int kind,
+                                          int i) {
+    double fx = floor((x - g.x0) / g.wx), fy = floor((y - g.y0) / g.wy);
+    if (!(fx >= 0.0 && fx < g.nx && fy >= 0.0 && fy < g.ny)) {
+        raise_error(err, SPHNJ_ERR_OUT_OF_GRID, kind, i, -1);
+        fx = fx == fx ? fmin(fmax(fx, 0.0), (double)(g.nx - 1)) : 0.0;
+        fy = fy == fy ? fmin(fmax(fy, 0.0), (double)(g.ny - 1)) : 0.0;
+    }
+    off = make_float2((float)(x - (g.x0 + fx * g.wx)), (float)(y - (g.y0 + fy * g.wy)));
+    return make_int2((int)fx, (int)fy);
+}
+
+__device__ __forceinline__ float2 round_f2(double2 v, float2 &comp) {
+    const float2 r = make_float2((float)v.x, (float)v.y);
+    comp = make_float2((float)((double)r.x - v.x), (float)((double)r.y - v.y));
+    return r;
+}
+
+// kinds: bit 0 fluid, bit 1 solid, bit 2 virtual
+__global__ void k_split(const __grid_constant__ One g, int kinds) {
+    const Scene &S = g.s;
+    const sphnj_params &p = S.p;
+    const DevState &d = S.d;
+    const Grid2 gr = grid_of(p);
+    const int nf = p.fluid_number_total, ns = p.solid_number, nv = p.virt_number;
+    const long t = (long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (t < nf) {
+        if (!(kinds & 1)) return;
+        const int i = (int)t;
+        const float2 x = d.f_pos[i];
+        float2 off;
+        const int2 c = split_pos(gr, x.x, x.y, off, d.err, 0, i);
+        d.f_cell[i] = c.x * gr.ny + c.y;
+        d.f_off[i] = off;
+        d.f_offc[i] = make_float2(0.f, 0.f);
+        d.f_velc[i] = make_float2(0.f, 0.f);
+    } else if (t < (long)nf + ns) {
+        if (!(kinds & 2)) return;
+        const int i = (int)(t - nf);
+        const double2 X = d.s_ref[i], x = d.s_pos[i];
+        float2 roff;
+        const int2 rc = split_pos(gr, X.x, X.y, roff, d.err, 1, i);
+        d.s_rc[i] = rc;
+        d.s_roff[i] = roff;
+        float2 comp;
+        d.s_u[i] = round_f2(make_double2(x.x - X.x, x.y - X.y), comp);
+        d.s_uc[i] = comp;
+        d.s_v[i] = round_f2(d.s_vel[i], comp);
+        d.s_vc[i] = comp;
+        const double2 a = d.s_dudt[i];
+        d.s_acc[i] = make_float2((float)a.x, (float)a.y);
+    } else if (t < (long)nf + ns + nv) {
+        if (!(kinds & 4)) return;
+        const int i = (int)(t - nf - ns);
+        const float2 x = d.v_pos[i];
+        float2 off;
+        const int2 c = split_pos(gr, x.x, x.y, off, d.err, 2, i);
+        d.v_cell[i] = c.x * gr.ny + c.y;
+        d.v_off[i] = off;
+    }
+}
+
+__global__ void k_join(const __grid_constant__ One g) {
+    const Scene &S = g.s;
+    const sphnj_params &p = S.p;
+    const DevState &d = S.d;
+    const Grid2 gr = grid_of(p);
+    const int nf = p.fluid_number_total, ns = p.solid_number;
+    const long t = (long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (t < nf) {
+        const int i = (int)t;
+        const int c = d.f_cell[i];
+        const int cx = c / gr.ny, cy = c - cx * gr.ny;
+        const float2 off = d.f_off[i], oc = d.f_offc[i];
+        d.f_pos[i] = make_float2((float)(gr.x0 + cx * gr.wx + ((double)off.x - (double)oc.x)),
+                                 (float)(gr.y0 + cy * gr.wy + ((double)off.y - (double)oc.y)));
+    } else if (t < (long)nf + ns) {
+        const int i = (int)(t - nf);
+        const double2 X = d.s_ref[i];
+        const float2 u = d.s_u[i], uc = d.s_uc[i], v = d.s_v[i], vc = d.s_vc[i], a = d.s_acc[i];
+        d.s_pos[i] = make_double2(X.x + ((double)u.x - (double)uc.x), X.y + ((double)u.y - (double)uc.y));
+        d.s_vel[i] = make_double2((double)v.x - (double)vc.x, (double)v.y - (double)vc.y);
+        d.s_dudt[i] = make_double2((double)a.x, (double)a.y);
+    }
+}
+
+}  // namespace
+
+void launch_mixed_split(cudaStream_t st, const GroupOne &g, int kinds) {
+    const sphnj_params &p = g.s.p;
+    const long n = (long)p.fluid_number_total + p.solid_number + p.virt_number;
+    if (n > 0) k_split<<<grid_for(n, kBlock), kBlock, 0, st>>>(One{g.s}, kinds);
+}
+
+void launch_mixed_join(cudaStream_t st, const GroupOne &g) {
+    const sphnj_params &p = g.s.p;
+    const long n = (long)p.fluid_number_total + p.solid_number;
+    if (n > 0) k_join<<<grid_for(n, kBlock), kBlock, 0, st>>>(One{g.s});
+}
+
+}  // namespace sphnj

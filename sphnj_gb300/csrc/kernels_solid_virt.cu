@@ -11,6 +11,7 @@
 //                      with the SVK / auxetic-plastic stress (solid.cu:80-167)
 //   k_solid_force      solidForceCalculate (solid.cu:211-353)
 //   k_solid_update     solidUpdate (solid.cu:446-471)
+#include "forms.cuh"
 #include "kernels.h"
 
 namespace sphnj {
@@ -54,14 +55,15 @@ template <class G> __global__ void __launch_bounds__(256) k_virt_normal(const __
     if (i < nv) d.v_normal[i] = sqrtf(sqn(nrm)) < EPS_FOR_SUM ? make_float2(0.f, 0.f) : normalized(nrm);
 }
 
-template <class G> __global__ void __launch_bounds__(kBlock) k_virt_data(const __grid_constant__ G g) {
+template <class G, class F> __global__ void __launch_bounds__(kBlock) k_virt_data(const __grid_constant__ G g) {
     SPHNJ_SCENE(g);
     const int i = blk * blockDim.x + threadIdx.x;
     if (i >= p.virt_number) return;
     const int nx = p.cell_number[0], ny = p.cell_number[1];
     const float R2 = p.impact_distance_square, hinv2 = p.smoothing_length_inverse_square;
     const float gx = p.gravity[0], gy = p.gravity[1];
-    const float2 x_i = d.v_pos[i];
+    const Frame fr{0, 0};
+    const float2 x_i = F::v_home(p, d, fr, i);
     float2 vel = make_float2(0.f, 0.f);
     float pr = 0.f, sum = 0.f, nearest = LARGE_FLOAT;
     int phase = d.v_phase[i];
@@ -69,10 +71,11 @@ template <class G> __global__ void __launch_bounds__(kBlock) k_virt_data(const _
     for (int n = 0; n < 9; ++n) {
         const int m = neighbour_cell(c, n, nx, ny);
         if (m < 0) continue;
+        const float2 sh = F::shift(p, fr, n);
         const int2 rf = __ldg(&d.rng_f[m]);
         for (int t = rf.x; t < rf.x + rf.y; ++t) {
             const int j = __ldg(&d.lst_f[t]);
-            const float2 dx = sub2(__ldg(&d.f_pos[j]), x_i);
+            const float2 dx = sub2(F::f_nbr(d, j, sh), x_i);
             const float d2 = sqn(dx);
             if (!(d2 < R2)) continue;
             const float kc = sw(p, d2 * hinv2);
@@ -113,23 +116,25 @@ template <class G> __global__ void __launch_bounds__(kBlock) k_virt_data(const _
                  powf(pv * by_phase(p.coefficient_p2rho, phase) + 1.0f, by_phase(p.gamma_inv, phase));
 }
 
-template <class G> __global__ void __launch_bounds__(kBlock) k_solid_couple(const __grid_constant__ G g) {
+template <class G, class F> __global__ void __launch_bounds__(kBlock) k_solid_couple(const __grid_constant__ G g) {
     SPHNJ_SCENE(g);
     const int i = blk * blockDim.x + threadIdx.x;
     if (i >= p.solid_number) return;
     const int nx = p.cell_number[0], ny = p.cell_number[1];
     const float R2 = p.impact_distance_square, hinv2 = p.smoothing_length_inverse_square;
-    const float2 x_i = to_f2(d.s_pos[i]);
+    const Frame fr{0, 0};
+    const float2 x_i = F::s_home(p, d, fr, i);
     float2 nrm = make_float2(0.f, 0.f);
     float pr = 0.f, sum = 0.f;
     const int c = d.s_cell[i];
     for (int n = 0; n < 9; ++n) {
         const int m = neighbour_cell(c, n, nx, ny);
         if (m < 0) continue;
+        const float2 sh = F::shift(p, fr, n);
         const int2 rf = __ldg(&d.rng_f[m]);
         for (int t = rf.x; t < rf.x + rf.y; ++t) {
             const int j = __ldg(&d.lst_f[t]);
-            const float2 dx = sub2(__ldg(&d.f_pos[j]), x_i);
+            const float2 dx = sub2(F::f_nbr(d, j, sh), x_i);
             if (!(sqn(dx) < R2)) continue;
             const float kc = sw(p, sqn(dx) * hinv2);
             sum += kc;
@@ -138,7 +143,7 @@ template <class G> __global__ void __launch_bounds__(kBlock) k_solid_couple(cons
         const int2 rs = __ldg(&d.rng_s[m]);
         for (int t = rs.x; t < rs.x + rs.y; ++t) {
             const int j = __ldg(&d.lst_s[t]);
-            const float2 dx = sub2(to_f2(d.s_pos[j]), x_i);
+            const float2 dx = sub2(F::s_nbr(d, j, sh), x_i);
             if (!(sqn(dx) < R2)) continue;
             const float kc = gw(p, sqn(dx) * hinv2);
             nrm.x -= dx.x * kc;
@@ -169,8 +174,8 @@ __device__ dmat2 green(const dmat2 &F) {
     return {0.5 * (ftf.m00 - 1.0), 0.5 * (ftf.m10 - 0.0), 0.5 * (ftf.m01 - 0.0), 0.5 * (ftf.m11 - 1.0)};
 }
 
-__device__ dmat2 auxetic_stress(const sphnj_params &p, const dmat2 &F, dmat2 &max_strain) {
-    const dmat2 g = green(F);
+// g: the Green strain of F
+__device__ dmat2 auxetic_stress(const sphnj_params &p, const dmat2 &F, const dmat2 &g, dmat2 &max_strain) {
     const double mid = 0.5 * (g.m00 + g.m11);
     const double df = g.m00 - g.m11;
     const double rad = sqrt(0.25 * (df * df) + g.m01 * g.m10);
@@ -187,9 +192,8 @@ __device__ dmat2 auxetic_stress(const sphnj_params &p, const dmat2 &F, dmat2 &ma
     return dmul(dmul(dmul(F, rot), ps), rinv);
 }
 
-__device__ dmat2 linear_stress(const sphnj_params &p, const dmat2 &F) {
+__device__ dmat2 linear_stress(const sphnj_params &p, const dmat2 &F, const dmat2 &g) {
     const double lambda = p.lambda, nu = p.nu;
-    const dmat2 g = green(F);
     const double a = 2.0 * nu, b = lambda * (g.m00 + g.m11);
     const dmat2 S = {a * g.m00 + b * 1.0, a * g.m10 + b * 0.0, a * g.m01 + b * 0.0, a * g.m11 + b * 1.0};
     return dmul(F, S);
@@ -240,10 +244,10 @@ template <class G> __global__ void __launch_bounds__(kBlock) k_solid_deform(cons
     const int mat = d.s_mat[i];
     dmat2 P = {0, 0, 0, 0};
     if (mat == SPHNJ_AUXETIC) {
-        P = auxetic_stress(p, F, ms);
+        P = auxetic_stress(p, F, green(F), ms);
         d.s_maxstrain[i] = ms;
     } else if (mat == SPHNJ_LINEAR_ELASTIC) {
-        P = linear_stress(p, F);
+        P = linear_stress(p, F, green(F));
     }
     d.s_P[i] = P;
     d.s_L[i] = L;
@@ -348,7 +352,182 @@ template <class G> __global__ void __launch_bounds__(256) k_solid_update(const _
     d.s_vel[i] = v;
 }
 
+// ---- mixed form -------------------------------------------------------------
+// Reference separation X_j - X_i from reference cells + FP32 offsets.
+__device__ __forceinline__ float2 ref_delta(const sphnj_params &p, int2 rc_i, float2 ro_i, int2 rc_j, float2 ro_j) {
+    return make_float2(__fmaf_rn((float)(rc_j.x - rc_i.x), p.interval[0], ro_j.x - ro_i.x),
+                       __fmaf_rn((float)(rc_j.y - rc_i.y), p.interval[1], ro_j.y - ro_i.y));
+}
+
+__device__ __forceinline__ float4 to_f4(const dmat2 &a) {
+    return make_float4((float)a.m00, (float)a.m10, (float)a.m01, (float)a.m11);
+}
+
+// solidDeformationCalculate (solid.cu:169-209) in displacement form.  The
+// pair loop sums in FP32, over the same neighbours as the plain form
+// (current-position stencil, reference-distance filter),
+//   H~ = sum (u_j - u_i) (x) dX W'   and   M = sum dX (x) dX W';
+// then in FP64: L = M^-1, H = H~ L, F = I + H (the plain form's F~ L, since
+// F~ = M + H~), the Green strain E = (H + H^T + H^T H) / 2 without the
+// cancellation of F^T F - I, and the PK1 stress.  P L and F L are stored in
+// FP32 for the force loop.
+template <class G> __global__ void __launch_bounds__(kBlock) k_solid_deform_mixed(const __grid_constant__ G g) {
+    SPHNJ_SCENE(g);
+    const int i = blk * blockDim.x + threadIdx.x;
+    if (i >= p.solid_number) return;
+    const int nx = p.cell_number[0], ny = p.cell_number[1];
+    const float R2 = p.impact_distance_square, hinv2 = p.smoothing_length_inverse_square;
+    const int2 rc_i = d.s_rc[i];
+    const float2 ro_i = d.s_roff[i], u_i = d.s_u[i];
+    float h00 = 0.f, h10 = 0.f, h01 = 0.f, h11 = 0.f, m00 = 0.f, m10 = 0.f, m01 = 0.f, m11 = 0.f;
+    const int c = d.s_cell[i];
+    for (int n = 0; n < 9; ++n) {
+        const int m = neighbour_cell(c, n, nx, ny);
+        if (m < 0) continue;
+        const int2 rs = __ldg(&d.rng_s[m]);
+        for (int t = rs.x; t < rs.x + rs.y; ++t) {
+            const int j = __ldg(&d.lst_s[t]);
+            const float2 dX = ref_delta(p, rc_i, ro_i, __ldg(&d.s_rc[j]), __ldg(&d.s_roff[j]));
+            const float q = sqn(dX);
+            if (!(q < R2)) continue;
+            const float kc = gw(p, q * hinv2);
+            const float2 du = sub2(__ldg(&d.s_u[j]), u_i);
+            const float ax = dX.x * kc, ay = dX.y * kc;
+            h00 += du.x * ax;
+            h10 += du.y * ax;
+            h01 += du.x * ay;
+            h11 += du.y * ay;
+            m00 += dX.x * ax;
+            m10 += dX.y * ax;
+            m01 += dX.x * ay;
+            m11 += dX.y * ay;
+        }
+    }
+    const dmat2 M = {m00, m10, m01, m11};
+    const dmat2 L = ddet(M) != 0.0 ? dinv(M) : dmat2{1.0, 0.0, 0.0, 1.0};
+    const dmat2 H = dmul(dmat2{h00, h10, h01, h11}, L);
+    const dmat2 F = {1.0 + H.m00, H.m10, H.m01, 1.0 + H.m11};
+    const dmat2 HtH = dmul(dtrans(H), H);
+    const dmat2 E = {0.5 * (2.0 * H.m00 + HtH.m00), 0.5 * (H.m10 + H.m01 + HtH.m10),
+                     0.5 * (H.m01 + H.m10 + HtH.m01), 0.5 * (2.0 * H.m11 + HtH.m11)};
+    dmat2 ms = d.s_maxstrain[i];
+    const int mat = d.s_mat[i];
+    dmat2 P = {0, 0, 0, 0};
+    if (mat == SPHNJ_AUXETIC) {
+        P = auxetic_stress(p, F, E, ms);
+        d.s_maxstrain[i] = ms;
+    } else if (mat == SPHNJ_LINEAR_ELASTIC) {
+        P = linear_stress(p, F, E);
+    }
+    d.s_F[i] = F;
+    d.s_P[i] = P;
+    d.s_L[i] = L;
+    d.s_PL[i] = to_f4(dmul(P, L));
+    d.s_FL[i] = to_f4(dmul(F, L));
+}
+
+// solidForceCalculate (solid.cu:211-353), FP32: the stress divergence from
+// the stored P L, the artificial viscosity with dx = dX + du, and the fluid
+// coupling in the solid particle's cell frame.
+template <class G> __global__ void __launch_bounds__(kBlock) k_solid_force_mixed(const __grid_constant__ G g) {
+    SPHNJ_SCENE(g);
+    const int i = blk * blockDim.x + threadIdx.x;
+    if (i >= p.solid_number) return;
+    using F = FormMixed;
+    const int nx = p.cell_number[0], ny = p.cell_number[1];
+    const float R2 = p.impact_distance_square, hinv2 = p.smoothing_length_inverse_square;
+    const float alpha = p.artificial_viscosity[0], beta = p.artificial_viscosity[1];
+    const float eps = 0.01f * p.smoothing_length_square;
+    const float cs_s = p.solid_sound_speed, hs = p.smoothing_length;
+    const Frame fr{0, 0};
+    const float2 x_i = F::s_home(p, d, fr, i);
+    const float2 v_i = d.s_v[i], u_i = d.s_u[i], ro_i = d.s_roff[i];
+    const int2 rc_i = d.s_rc[i];
+    const float rho_ref = d.s_mat[i] == SPHNJ_AUXETIC ? p.auxetic_density : p.solid_reference_density;
+    const float rinv = 1.0f / rho_ref;
+    const float4 PL_i = d.s_PL[i], FL_i = d.s_FL[i];
+    const float p_i = d.s_p[i];
+    float2 couple = make_float2(0.f, 0.f), acc = make_float2(0.f, 0.f);
+    const int c = d.s_cell[i];
+    for (int n = 0; n < 9; ++n) {
+        const int m = neighbour_cell(c, n, nx, ny);
+        if (m < 0) continue;
+        const float2 sh = F::shift(p, fr, n);
+        const int2 rf = __ldg(&d.rng_f[m]);
+        for (int t = rf.x; t < rf.x + rf.y; ++t) {  // solidFluidCouple, solid.cu:211-255
+            const int j = __ldg(&d.lst_f[t]);
+            const float2 dx = sub2(F::f_nbr(d, j, sh), x_i);
+            if (!(sqn(dx) < R2)) continue;
+            const float kc = gw(p, sqn(dx) * hinv2);
+            const float p_j = __ldg(&d.f_p[j]);
+            const float cs = by_phase(p.sound_speed, __ldg(&d.f_phase[j]));
+            const float rho_j = __ldg(&d.f_rho[j]), rho_f = rho_j;
+            const float2 u_j = __ldg(&d.f_vel[j]);
+            float ps = fdiv(rho_f * p_j + rho_j * p_i, rho_f + rho_j);
+            float2 nn = sqn(dx) > 0.f ? make_float2(fdiv(dx.x, sqrtf(sqn(dx))), fdiv(dx.y, sqrtf(sqn(dx)))) : dx;
+            const float du = dot2(sub2(v_i, u_j), nn);
+            if (du >= 0.0f) ps += fdiv(rho_f * rho_j * du, rho_f + rho_j) * fminf(3.0f * du, cs);
+            const float am = fdiv(-2.0f * ps, rho_ref);
+            couple.x += am * dx.x * kc;
+            couple.y += am * dx.y * kc;
+        }
+        const int2 rs = __ldg(&d.rng_s[m]);
+        for (int t = rs.x; t < rs.x + rs.y; ++t) {  // solidSolidForce, solid.cu:257-305
+            const int j = __ldg(&d.lst_s[t]);
+            const float2 dX = ref_delta(p, rc_i, ro_i, __ldg(&d.s_rc[j]), __ldg(&d.s_roff[j]));
+            const float q = sqn(dX);
+            if (!(q < R2)) continue;
+            const float kc = gw(p, q * hinv2);
+            const float4 PL_j = __ldg(&d.s_PL[j]);
+            const float4 M = make_float4(PL_j.x + PL_i.x, PL_j.y + PL_i.y, PL_j.z + PL_i.z, PL_j.w + PL_i.w);
+            const float kr = kc * rinv;
+            acc.x += sum2(M.x, dX.x, M.z, dX.y) * kr;
+            acc.y += sum2(M.y, dX.x, M.w, dX.y) * kr;
+            const float2 dx = add2(dX, sub2(__ldg(&d.s_u[j]), u_i));
+            const float2 dv = sub2(__ldg(&d.s_v[j]), v_i);
+            const float nuv = hs * dot2(dv, dx) / (sqn(dx) + eps);
+            const float visc = sum2(alpha * nuv, cs_s, -beta * nuv, nuv) * kc;
+            acc.x += sum2(FL_i.x, dX.x, FL_i.z, dX.y) * visc;
+            acc.y += sum2(FL_i.y, dX.x, FL_i.w, dX.y) * visc;
+        }
+    }
+    d.s_couple[i] = couple;
+    d.s_acc[i] = add2(acc, couple);
+}
+
+// solidUpdate (solid.cu:446-471): displacement and velocity integrated with
+// Kahan compensation over the sub-step dt / k.
+template <class G> __global__ void __launch_bounds__(256) k_solid_update_mixed(const __grid_constant__ G g) {
+    SPHNJ_SCENE(g);
+    const int i = blk * blockDim.x + threadIdx.x;
+    if (i >= p.solid_number) return;
+    const float dt = p.dt / (float)p.solid_sub_step;
+    const int bt = d.s_bt[i];
+    float2 u = d.s_u[i], uc = d.s_uc[i], v = d.s_v[i], vc = d.s_vc[i];
+    if (bt == SPHNJ_FIXED) {
+        v = make_float2((float)p.fixed_speed[0], (float)p.fixed_speed[1]);
+        vc = make_float2(0.f, 0.f);
+        kahan_add2(u, uc, make_float2(v.x * dt, v.y * dt));
+        d.s_acc[i] = make_float2(0.f, 0.f);
+    } else if (bt == SPHNJ_UNCONSTRAINED) {
+        float2 a = d.s_acc[i];
+        if (p.transient_type == SPHNJ_STEADY) {
+            a.x += -0.1f * v.x;
+            a.y += -0.1f * v.y;
+            d.s_acc[i] = a;
+        }
+        kahan_add2(u, uc, make_float2(v.x * dt, v.y * dt));
+        kahan_add2(v, vc, make_float2((a.x + p.gravity[0]) * dt, (a.y + p.gravity[1]) * dt));
+    }
+    d.s_u[i] = u;
+    d.s_uc[i] = uc;
+    d.s_v[i] = v;
+    d.s_vc[i] = vc;
+    d.s_off[i] = solid_offset(p, d.s_rc[i], d.s_roff[i], u, d.s_cell[i]);
+}
+
 }  // namespace
+
 
 template <class G> int launch_virt_normal(cudaStream_t st, G &g) {
     return launch(
@@ -356,34 +535,43 @@ template <class G> int launch_virt_normal(cudaStream_t st, G &g) {
         k_virt_normal<typename G::Dev>, 256, 0, st);
 }
 template <class G> int launch_virt_data(cudaStream_t st, G &g) {
-    return launch(
-        g, site_key(SITE_VIRT_DATA), [](const Scene &s) { return grid_for(s.p.virt_number, kBlock); },
-        k_virt_data<typename G::Dev>, kBlock, 0, st);
+    using D = typename G::Dev;
+    auto blocks = [](const Scene &s) { return grid_for(s.p.virt_number, kBlock); };
+    return g.form == SPHNJ_FORM_MIXED
+               ? launch(g, site_key(SITE_VIRT_DATA), blocks, k_virt_data<D, FormMixed>, kBlock, 0, st)
+               : launch(g, site_key(SITE_VIRT_DATA), blocks, k_virt_data<D, FormPlain>, kBlock, 0, st);
 }
 template <class G> int launch_solid_couple(cudaStream_t st, G &g) {
-    return launch(
-        g, site_key(SITE_COUPLE),
-        [](const Scene &s) { return s.p.fluid_number_total > 0 ? grid_for(s.p.solid_number, kBlock) : 0u; },
-        k_solid_couple<typename G::Dev>, kBlock, 0, st);
+    using D = typename G::Dev;
+    auto blocks = [](const Scene &s) { return s.p.fluid_number_total > 0 ? grid_for(s.p.solid_number, kBlock) : 0u; };
+    return g.form == SPHNJ_FORM_MIXED
+               ? launch(g, site_key(SITE_COUPLE), blocks, k_solid_couple<D, FormMixed>, kBlock, 0, st)
+               : launch(g, site_key(SITE_COUPLE), blocks, k_solid_couple<D, FormPlain>, kBlock, 0, st);
 }
 // scenes with fewer solid sub-steps per fluid step own no block of sub-step `sub`
 inline unsigned solid_blocks(const sphnj_params &p, int sub, int block) {
     return sub < p.solid_sub_step ? grid_for(p.solid_number, block) : 0u;
 }
 template <class G> int launch_solid_deformation(cudaStream_t st, G &g, int sub) {
-    return launch(
-        g, site_key(SITE_SOLID_DEFORM, sub), [sub](const Scene &s) { return solid_blocks(s.p, sub, kBlock); },
-        k_solid_deform<typename G::Dev>, kBlock, 0, st);
+    using D = typename G::Dev;
+    auto blocks = [sub](const Scene &s) { return solid_blocks(s.p, sub, kBlock); };
+    return g.form == SPHNJ_FORM_MIXED
+               ? launch(g, site_key(SITE_SOLID_DEFORM, sub), blocks, k_solid_deform_mixed<D>, kBlock, 0, st)
+               : launch(g, site_key(SITE_SOLID_DEFORM, sub), blocks, k_solid_deform<D>, kBlock, 0, st);
 }
 template <class G> int launch_solid_force(cudaStream_t st, G &g, int sub) {
-    return launch(
-        g, site_key(SITE_SOLID_FORCE, sub), [sub](const Scene &s) { return solid_blocks(s.p, sub, kBlock); },
-        k_solid_force<typename G::Dev>, kBlock, 0, st);
+    using D = typename G::Dev;
+    auto blocks = [sub](const Scene &s) { return solid_blocks(s.p, sub, kBlock); };
+    return g.form == SPHNJ_FORM_MIXED
+               ? launch(g, site_key(SITE_SOLID_FORCE, sub), blocks, k_solid_force_mixed<D>, kBlock, 0, st)
+               : launch(g, site_key(SITE_SOLID_FORCE, sub), blocks, k_solid_force<D>, kBlock, 0, st);
 }
 template <class G> int launch_solid_update(cudaStream_t st, G &g, int sub) {
-    return launch(
-        g, site_key(SITE_SOLID_UPDATE, sub), [sub](const Scene &s) { return solid_blocks(s.p, sub, 256); },
-        k_solid_update<typename G::Dev>, 256, 0, st);
+    using D = typename G::Dev;
+    auto blocks = [sub](const Scene &s) { return solid_blocks(s.p, sub, 256); };
+    return g.form == SPHNJ_FORM_MIXED
+               ? launch(g, site_key(SITE_SOLID_UPDATE, sub), blocks, k_solid_update_mixed<D>, 256, 0, st)
+               : launch(g, site_key(SITE_SOLID_UPDATE, sub), blocks, k_solid_update<D>, 256, 0, st);
 }
 
 SPHNJ_INSTANTIATE_GROUPS(launch_virt_normal);
