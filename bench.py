@@ -46,7 +46,8 @@ def parse():
     ap.add_argument("--dx", type=float, default=0.0017)
     ap.add_argument("--cpu-dx", type=float, default=0.0068,
                     help="dx of the bounded CPU sample (same geometry, 1/16 of the particles)")
-    ap.add_argument("--cpu-steps", type=int, default=3)
+    ap.add_argument("--cpu-steps", type=int, default=150,
+                    help="timed oracle steps of the CPU sample (~10 s on 16 host cores)")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--untiled", action="store_true", help="one thread per particle in the neighbour sweeps")
@@ -181,22 +182,36 @@ def run_sweep(args, stream):
     import sphnj_gb300 as S
     from sphnj_gb300 import abi, cases
 
+    from sphnj_gb300.sharding import balanced_partition
+
+    rank, world, _ = dist_env()
     t0 = time.perf_counter()
     scenes = [cases.sweep_scene(s) for s in range(cases.SWEEP_SCENES)]
-    params = [c.params() for c in scenes]
-    arrays = [c.arrays() for c in scenes]
+    all_params = [c.params() for c in scenes]
+    weights = [p.fluid_number_total + p.solid_number for p in all_params]
+    # one process per GPU: this rank's particle-balanced share of the scenes
+    mine = balanced_partition(weights, world)[rank]
+    params = [all_params[i] for i in mine]
+    arrays = [scenes[i].arrays() for i in mine]
     setup_s = time.perf_counter() - t0
-    units = sum(p.fluid_number_total + p.solid_number for p in params)
+    units = sum(weights)  # all ranks' particles: the whole-job rate
     K = args.sweep_steps
 
     def timed(fn):
+        if world > 1:
+            torch.distributed.barrier()
         torch.cuda.synchronize()
         e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
         e0.record(stream)
         fn()
         e1.record(stream)
         torch.cuda.synchronize()
-        return e0.elapsed_time(e1)
+        ms = e0.elapsed_time(e1)
+        if world > 1:
+            t = torch.tensor([ms], device="cuda")
+            torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+            ms = float(t.item())
+        return ms
 
     def make(form):
         sims = []
@@ -249,7 +264,8 @@ def run_sweep(args, stream):
         "workload": "256 independent scenes (seeds 0..255): 128 water dam breaks of 2k-60k particles "
                     "(H/W in [0.5, 2.5]), 128 cantilever beams of 1k-20k particles (E 0.5-20 MPa, "
                     "nu 0.3-0.45, L 0.1-0.3 m), +-0.01 dx jitter",
-        "scenes": len(params), "particles": units, "steps": K, "warmup": args.warmup,
+        "scenes": len(all_params), "particles": units, "steps": K, "warmup": args.warmup,
+        "sharding": f"{world} rank(s), particle-balanced scene partition, no data-path collective",
         "plain_scene_by_scene": dict(rate(ms_plain), launches_per_step=launches_plain / K),
         **out,
         "setup_s": setup_s,
