@@ -337,6 +337,26 @@ int  sphnj_set_tiling(sphnj_ctx *ctx, int tiled, int tile_h);
  * (sphnj_profile_enable) always launches individually. */
 int  sphnj_set_graphs(sphnj_ctx *ctx, int on);
 
+/* Tiled sweeps: on != 0 (default) stores per-step neighbour lists in the pair
+ * pass for the shifting passes of the same step; 0 walks the 3x3 stencil in
+ * every pass.  Results are identical.  sphnj_get_sweeps reports the current
+ * configuration (any pointer may be NULL). */
+int  sphnj_set_neighbour_lists(sphnj_ctx *ctx, int on);
+int  sphnj_get_sweeps(const sphnj_ctx *ctx, int *tiled, int *tile_h, int *lists);
+
+/* Autotuner of the sweep configuration (no counterpart in the reference,
+ * whose launch shape is fixed at thread_num = 32).  Candidates: one thread
+ * per particle; tiles of 8, 12, 16, 24, 32 cells with stored neighbour lists;
+ * tiles of 8, 16, 32 cells without.  Each runs `steps` steps from a device
+ * copy of the current state (once to capture its graphs, once timed with CUDA
+ * events); the state is put back after each trial, so tuning does not advance
+ * or change the run.  The fastest candidate is installed and reported. */
+typedef struct sphnj_tuning {
+    int32_t tiled, tile_h, lists, candidates;
+    double  ms_per_step;
+} sphnj_tuning;
+int  sphnj_autotune(sphnj_ctx *ctx, int steps, sphnj_tuning *out);
+
 /* ---- measurement (the reference has only a host clock() around its loop,
  * calculation.cu:24-46) -------------------------------------------------- */
 
@@ -413,6 +433,10 @@ int  sphnj_batch_set_stream(sphnj_batch *b, void *cuda_stream);
 /* As sphnj_set_tiling / sphnj_set_graphs, for every scene of the batch. */
 int  sphnj_batch_set_tiling(sphnj_batch *b, int tiled, int tile_h);
 int  sphnj_batch_set_graphs(sphnj_batch *b, int on);
+int  sphnj_batch_set_neighbour_lists(sphnj_batch *b, int on);
+int  sphnj_batch_get_sweeps(const sphnj_batch *b, int *tiled, int *tile_h, int *lists);
+/* As sphnj_autotune, over the whole batch (every scene copied and put back). */
+int  sphnj_batch_autotune(sphnj_batch *b, int steps, sphnj_tuning *out);
 /* Advances every scene n fluid steps (asynchronous, as sphnj_step). */
 int  sphnj_batch_step(sphnj_batch *b, int n);
 /* Waits for the batch's stream; reports the first scene with a device error. */
@@ -421,6 +445,20 @@ int  sphnj_batch_profile_enable(sphnj_batch *b, int on);
 int  sphnj_batch_profile_read(sphnj_batch *b, double *ms, int64_t *calls, int64_t *kernels);
 int  sphnj_batch_stat_launches(const sphnj_batch *b, uint64_t *launches);
 const char *sphnj_batch_last_error(const sphnj_batch *b);
+
+/* ---- checkpoint / restart ---------------------------------------------------
+ * The reference has no checkpoint (it restarts only from its generated .dat
+ * files).  A checkpoint holds the complete device state of a context - every
+ * field, both cell-list buffers, the per-step neighbour lists and counters -
+ * after a versioned header ("SPHNJCK1", form, step state, the parameters).
+ * Loading it into a context created with the same particle counts, cell grid
+ * and form continues the run bit-identically.  The host buffer variant takes
+ * sphnj_checkpoint_size() bytes; the file variants write / read one file. */
+int  sphnj_checkpoint_size(const sphnj_ctx *ctx, uint64_t *bytes);
+int  sphnj_checkpoint_save(sphnj_ctx *ctx, void *buffer, uint64_t bytes);
+int  sphnj_checkpoint_load(sphnj_ctx *ctx, const void *buffer, uint64_t bytes);
+int  sphnj_checkpoint_write(sphnj_ctx *ctx, const char *path);
+int  sphnj_checkpoint_read(sphnj_ctx *ctx, const char *path);
 
 #ifdef __cplusplus
 }

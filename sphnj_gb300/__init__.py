@@ -175,6 +175,21 @@ class Simulation:
     def set_graphs(self, on: bool = True):
         self._check(self._lib.sphnj_set_graphs(self._h, 1 if on else 0), "set_graphs")
 
+    def set_neighbour_lists(self, on: bool = True):
+        self._check(self._lib.sphnj_set_neighbour_lists(self._h, 1 if on else 0), "set_neighbour_lists")
+
+    def sweeps(self) -> dict:
+        t, h, l = C.c_int(), C.c_int(), C.c_int()
+        self._check(self._lib.sphnj_get_sweeps(self._h, C.byref(t), C.byref(h), C.byref(l)), "get_sweeps")
+        return {"tiled": bool(t.value), "tile_h": h.value, "lists": bool(l.value)}
+
+    def autotune(self, steps: int = 5) -> dict:
+        """Times the sweep configurations from the current state (which is put
+        back) and installs the fastest (sphnj_autotune)."""
+        r = abi.Tuning()
+        self._check(self._lib.sphnj_autotune(self._h, int(steps), C.byref(r)), "autotune")
+        return r.as_dict()
+
     def upload_fields(self, mask: int, arrays: dict):
         s = state_struct(arrays)
         self._check(self._lib.sphnj_upload_fields(self._h, int(mask), C.byref(s)), "upload_fields")
@@ -230,6 +245,24 @@ class Simulation:
 
     def set_step(self, step: int):
         self._check(self._lib.sphnj_debug_set_step(self._h, int(step)), "set_step")
+
+    def checkpoint(self) -> np.ndarray:
+        """The complete device state as bytes (sphnj_checkpoint_save)."""
+        n = C.c_uint64()
+        self._check(self._lib.sphnj_checkpoint_size(self._h, C.byref(n)), "checkpoint_size")
+        buf = np.empty(n.value, np.uint8)
+        self._check(self._lib.sphnj_checkpoint_save(self._h, buf.ctypes.data, n.value), "checkpoint_save")
+        return buf
+
+    def restore(self, buf: np.ndarray):
+        buf = np.ascontiguousarray(buf, np.uint8)
+        self._check(self._lib.sphnj_checkpoint_load(self._h, buf.ctypes.data, buf.nbytes), "checkpoint_load")
+
+    def save(self, path):
+        self._check(self._lib.sphnj_checkpoint_write(self._h, str(path).encode()), "checkpoint_write")
+
+    def load(self, path):
+        self._check(self._lib.sphnj_checkpoint_read(self._h, str(path).encode()), "checkpoint_read")
 
     def max_speed(self) -> float:
         v = C.c_float()
@@ -289,6 +322,19 @@ class Batch:
 
     def set_graphs(self, on: bool = True):
         self._check(self._lib.sphnj_batch_set_graphs(self._h, 1 if on else 0), "set_graphs")
+
+    def set_neighbour_lists(self, on: bool = True):
+        self._check(self._lib.sphnj_batch_set_neighbour_lists(self._h, 1 if on else 0), "set_neighbour_lists")
+
+    def sweeps(self) -> dict:
+        t, h, l = C.c_int(), C.c_int(), C.c_int()
+        self._check(self._lib.sphnj_batch_get_sweeps(self._h, C.byref(t), C.byref(h), C.byref(l)), "get_sweeps")
+        return {"tiled": bool(t.value), "tile_h": h.value, "lists": bool(l.value)}
+
+    def autotune(self, steps: int = 5) -> dict:
+        r = abi.Tuning()
+        self._check(self._lib.sphnj_batch_autotune(self._h, int(steps), C.byref(r)), "autotune")
+        return r.as_dict()
 
     def step(self, n: int = 1):
         self._check(self._lib.sphnj_batch_step(self._h, int(n)), "step")

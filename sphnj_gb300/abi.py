@@ -138,6 +138,16 @@ INPUT_FIELDS = {
 }
 
 
+class Tuning(C.Structure):
+    """sphnj_tuning: the sweep configuration the autotuner chose."""
+    _fields_ = [("tiled", C.c_int32), ("tile_h", C.c_int32), ("lists", C.c_int32), ("candidates", C.c_int32),
+                ("ms_per_step", C.c_double)]
+
+    def as_dict(self) -> dict:
+        return {"tiled": bool(self.tiled), "tile_h": self.tile_h, "lists": bool(self.lists),
+                "candidates": self.candidates, "ms_per_step": self.ms_per_step}
+
+
 class HostState(C.Structure):
     _fields_ = [(name, ptr) for name, ptr, _, _, _ in STATE_FIELDS]
 
@@ -220,6 +230,20 @@ def declare(lib: C.CDLL, prefix: str) -> None:
             g(n).restype = C.c_int
         g("batch_last_error").argtypes = [vp]
         g("batch_last_error").restype = C.c_char_p
+        g("checkpoint_size").argtypes = [vp, C.POINTER(C.c_uint64)]
+        g("checkpoint_save").argtypes = [vp, vp, C.c_uint64]
+        g("checkpoint_load").argtypes = [vp, vp, C.c_uint64]
+        g("checkpoint_write").argtypes = [vp, C.c_char_p]
+        g("checkpoint_read").argtypes = [vp, C.c_char_p]
+        for n in ("checkpoint_size", "checkpoint_save", "checkpoint_load", "checkpoint_write", "checkpoint_read"):
+            g(n).restype = C.c_int
+        PIi = C.POINTER(C.c_int)
+        for pre in ("", "batch_"):
+            g(pre + "set_neighbour_lists").argtypes = [vp, C.c_int]
+            g(pre + "get_sweeps").argtypes = [vp, PIi, PIi, PIi]
+            g(pre + "autotune").argtypes = [vp, C.c_int, C.POINTER(Tuning)]
+            for n in ("set_neighbour_lists", "get_sweeps", "autotune"):
+                g(pre + n).restype = C.c_int
     else:
         g("create").argtypes = [C.POINTER(Params), C.c_int, C.c_int, C.POINTER(vp)]
         g("error").argtypes = [vp]

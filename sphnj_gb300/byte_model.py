@@ -56,3 +56,21 @@ def bytes_per_launch(stage: str, nf: int, ns: int, nv: int) -> float:
 
 def bytes_per_step(nf: int, ns: int, nv: int, shifts: int, substeps: int) -> float:
     return float(nf * (153 + 79 * shifts) + nv * 46 + ns * (48 + 440 * substeps))
+
+
+# DRAM traffic (dram__bytes_read.sum + dram__bytes_write.sum) per fluid
+# particle of one launch of the tiled neighbour sweeps, from one ncu capture of
+# the 2,083,750-particle gas-liquid dam break (plain form, tiles of 16 cells,
+# stored neighbour lists); it grows in proportion to the particle count (same
+# tile shape, same list length per particle).  Well above the compulsory bytes
+# above: the pair pass writes the per-step neighbour lists and every shifting
+# pass reads them back.
+MEASURED_TRAFFIC_PER_PARTICLE = {
+    "fluid_pair": 165.6,
+    "shift_gradient": 148.0,
+}
+
+
+def measured_traffic_per_launch(stage: str, nf: int) -> float | None:
+    b = MEASURED_TRAFFIC_PER_PARTICLE.get(stage)
+    return None if b is None else float(b * nf)

@@ -182,6 +182,23 @@ int sphnj_batch_set_tiling(sphnj_batch *b, int tiled, int tile_h) {
     return SPHNJ_OK;
 }
 
+int sphnj_batch_set_neighbour_lists(sphnj_batch *b, int on) {
+    if (!b) return SPHNJ_ERR_ARG;
+    cudaSetDevice(b->device);
+    BCK(cudaStreamSynchronize(b->st));
+    b->tiles.lists = on != 0;
+    drop_graphs(b);
+    return SPHNJ_OK;
+}
+
+int sphnj_batch_get_sweeps(const sphnj_batch *b, int *tiled, int *tile_h, int *lists) {
+    if (!b) return SPHNJ_ERR_ARG;
+    if (tiled) *tiled = b->tiles.tiled ? 1 : 0;
+    if (tile_h) *tile_h = b->tiles.tile_h;
+    if (lists) *lists = b->tiles.lists ? 1 : 0;
+    return SPHNJ_OK;
+}
+
 int sphnj_batch_set_graphs(sphnj_batch *b, int on) {
     if (!b) return SPHNJ_ERR_ARG;
     cudaSetDevice(b->device);
@@ -292,5 +309,37 @@ int sphnj_batch_stat_launches(const sphnj_batch *b, uint64_t *launches) {
 }
 
 const char *sphnj_batch_last_error(const sphnj_batch *b) { return b ? b->msg.c_str() : "null batch"; }
+
+}  // extern "C"
+
+namespace {
+
+int apply_batch(void *o, const TileConfig &t) {
+    sphnj_batch *b = static_cast<sphnj_batch *>(o);
+    int rc = sphnj_batch_set_tiling(b, t.tiled ? 1 : 0, t.tile_h);
+    return rc ? rc : sphnj_batch_set_neighbour_lists(b, t.lists ? 1 : 0);
+}
+int step_batch(void *o, int n) { return sphnj_batch_step(static_cast<sphnj_batch *>(o), n); }
+
+}  // namespace
+
+extern "C" {
+
+int sphnj_batch_autotune(sphnj_batch *b, int steps, sphnj_tuning *out) {
+    if (!b || steps < 1) return SPHNJ_ERR_ARG;
+    cudaSetDevice(b->device);
+    BCK(cudaStreamSynchronize(b->st));
+    TuneResult r{};
+    const int rc = tune_sweeps(b->scenes, b->st, steps, apply_batch, step_batch, b, &r);
+    if (rc) return rc == SPHNJ_ERR_CUDA ? bfail(b, rc, "batch autotune: CUDA error") : rc;
+    if (out) {
+        out->tiled = r.best.tiled ? 1 : 0;
+        out->tile_h = r.best.tile_h;
+        out->lists = r.best.lists ? 1 : 0;
+        out->candidates = r.tried;
+        out->ms_per_step = r.ms_per_step;
+    }
+    return SPHNJ_OK;
+}
 
 }  // extern "C"

@@ -667,6 +667,23 @@ int sphnj_set_tiling(sphnj_ctx *ctx, int tiled, int tile_h) {
     return SPHNJ_OK;
 }
 
+int sphnj_set_neighbour_lists(sphnj_ctx *ctx, int on) {
+    if (!ctx) return SPHNJ_ERR_ARG;
+    cudaSetDevice(ctx->device);
+    CK(cudaStreamSynchronize(ctx->st));
+    ctx->tiles.lists = on != 0;
+    drop_graphs(ctx);  // the pair pass takes the switch as a launch argument
+    return SPHNJ_OK;
+}
+
+int sphnj_get_sweeps(const sphnj_ctx *ctx, int *tiled, int *tile_h, int *lists) {
+    if (!ctx) return SPHNJ_ERR_ARG;
+    if (tiled) *tiled = ctx->tiles.tiled ? 1 : 0;
+    if (tile_h) *tile_h = ctx->tiles.tile_h;
+    if (lists) *lists = ctx->tiles.lists ? 1 : 0;
+    return SPHNJ_OK;
+}
+
 int sphnj_profile_stage_count(void) { return ST_COUNT; }
 const char *sphnj_profile_stage_name(int s) { return s >= 0 && s < ST_COUNT ? kStageNames[s] : ""; }
 

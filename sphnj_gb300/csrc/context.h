@@ -94,4 +94,17 @@ int check_device_error(sphnj_ctx *ctx);
 // The status and message of the device error record last copied to the host.
 int device_error_status(sphnj_ctx *ctx);
 
+// Trial runs of the sweep configurations (autotune.cu): from a device copy
+// of the contexts' complete state, each candidate runs `steps` steps twice
+// (the first captures its graphs), the second timed with CUDA events on `st`;
+// the state is put back after every trial and at the end.  `apply` installs a
+// candidate, `step` advances every context; returns the fastest candidate.
+struct TuneResult {
+    TileConfig best;
+    double ms_per_step;
+    int tried;
+};
+int tune_sweeps(const std::vector<sphnj_ctx *> &ctxs, cudaStream_t st, int steps,
+                int (*apply)(void *, const TileConfig &), int (*step)(void *, int), void *obj, TuneResult *out);
+
 }  // namespace sphnj

@@ -27,6 +27,7 @@ namespace sphnj {
 struct TileConfig {
     bool tiled = true;
     int tile_h = 16;
+    bool lists = true;  // tiled: store per-step neighbour lists (else walk the stencil in every pass)
 };
 
 // Launch sites: a batch keeps one block table per (site, argument).

@@ -550,7 +550,8 @@ __device__ __forceinline__ Frame tile_frame(const sphnj_params &p, const DevStat
 }
 
 template <class G, class F>
-__global__ void __launch_bounds__(kTileBlock) k_fluid_pair_tiled(const __grid_constant__ G gs, int tile_h, int cap) {
+__global__ void __launch_bounds__(kTileBlock) k_fluid_pair_tiled(const __grid_constant__ G gs, int tile_h, int cap,
+                                                                 int use_lists) {
     SPHNJ_SCENE(gs);
     extern __shared__ __align__(16) unsigned char smem[];
     __shared__ int s_base[3], s_off[3];
@@ -578,7 +579,7 @@ __global__ void __launch_bounds__(kTileBlock) k_fluid_pair_tiled(const __grid_co
         const SrcTile src{s_pos, s_vel, s_rp, s_fl, s_idx, s_base, s_off};
         for (int h = g.home_b + threadIdx.x; h < g.home_e; h += blockDim.x) {
             const int i = d.lst_f[h];
-            pair_particle_listed<F>(p, d, src, i, h, true, tile_frame<F>(p, d, g, i));
+            pair_particle_listed<F>(p, d, src, i, h, use_lists != 0, tile_frame<F>(p, d, g, i));
         }
     } else {
         const SrcGlobal<F> src{&d};
@@ -824,7 +825,7 @@ template <class F, class G> int fluid_pair(cudaStream_t st, G &g, const TileConf
     int n = launch(
         g, site_key(SITE_PAIR_TILED, tc.tile_h),
         [&](const Scene &s) { return s.p.fluid_number_total > 0 ? tile_blocks(s.p, tc.tile_h) : 0u; },
-        k_fluid_pair_tiled<D, F>, kTileBlock, smem, st, tc.tile_h, cap);
+        k_fluid_pair_tiled<D, F>, kTileBlock, smem, st, tc.tile_h, cap, tc.lists ? 1 : 0);
     n += launch(
         g, site_key(SITE_PAIR_FALLBACK), [](const Scene &s) { return fallback_blocks(s.p.fluid_number_total); },
         k_fluid_pair_each<D, F>, kPairBlock, 0, st, 1);
