@@ -252,8 +252,9 @@ int sphnj_params_derive(sphnj_params *inout);
 int sphnj_read_particles(const char *data_dir, const sphnj_params *p,
                          sphnj_host_state *out);
 
-/* Byte layout check for foreign bindings: returns sizeof(sphnj_params) or
- * sizeof(sphnj_host_state) for which = 0 / 1, else -1. */
+/* Byte layout check for foreign bindings: returns sizeof(sphnj_params),
+ * sizeof(sphnj_host_state), sizeof(sphnj_diag), sizeof(sphnj_tuning) for
+ * which = 0 / 1 / 2 / 3, else -1. */
 int sphnj_abi_sizeof(int which);
 
 /* ---- simulation context (GPU) --------------------------------------------- */
@@ -356,6 +357,35 @@ typedef struct sphnj_tuning {
     double  ms_per_step;
 } sphnj_tuning;
 int  sphnj_autotune(sphnj_ctx *ctx, int steps, sphnj_tuning *out);
+
+/* ---- global diagnostics, reduced on the device in FP64 --------------------
+ * The quantities of the reference's global outputs (output.cu:283-560),
+ * which it computes on the host from full device->host copies of the state:
+ * here one small device reduction, deterministic (fixed summation order),
+ * no per-particle copy.  d = particle_diameter, dv = d^2, m = rho0[phase] dv. */
+typedef struct sphnj_diag {
+    int32_t step;              /* step counter when computed                  */
+    int32_t n_liquid;          /* liquid particles counted for the front      */
+    double  front;             /* max x over liquid + d/2 (outputEdge, output.cu:339-352); -1e300 without liquid */
+    double  fluid_momentum[2]; /* sum m v                                     */
+    double  fluid_kinetic;     /* sum m |v|^2 / 2                             */
+    double  fluid_mass;        /* sum rho dv                                  */
+    double  tip_disp[2];       /* x - X of the solid particle with the largest reference x
+                                  (ties: closest to the mean reference y)    */
+    double  solid_kinetic;     /* sum rho_s dv |v|^2 / 2 over reference x >= 0 (outputTotalEnergy, output.cu:426-455) */
+    double  solid_strain;      /* sum (lambda/2 tr(E)^2 + mu E:E) dv, E = (F^T F - I)/2 (same)                     */
+    double  total_force[2];    /* sum couple_dudt dv rho_material (outputTotalForce, output.cu:283-305)             */
+    double  von_mises[2];      /* max von Mises stress of F^-1 P over LINEAR_ELASTIC, AUXETIC (output.cu:503-544)  */
+    double  mean_pressure;     /* mean solid pressure (outputMeanPressure, output.cu:546-560)                     */
+} sphnj_diag;
+int  sphnj_diagnostics(sphnj_ctx *ctx, sphnj_diag *out);
+
+/* Point probes (Probe::getData, probe.cu:7-119): Shepard-interpolated fluid
+ * and solid velocity, pressure and density (solid density 0) at n points
+ * xy[2n], written to out[4n] as vx vy p rho; a point with no neighbour gives
+ * 0 0 0 rho0_liquid.  Each neighbour cell's own entries are used (the
+ * reference indexes neighbour cells with the probe cell's counts). */
+int  sphnj_probe(sphnj_ctx *ctx, int n, const float *xy, float *out);
 
 /* ---- measurement (the reference has only a host clock() around its loop,
  * calculation.cu:24-46) -------------------------------------------------- */

@@ -72,7 +72,8 @@ def lib() -> C.CDLL:
         for f in ("sphnj_params_read_ini", "sphnj_params_read_counts", "sphnj_params_derive",
                   "sphnj_read_particles", "sphnj_abi_sizeof"):
             getattr(L, f).restype = C.c_int
-        if L.sphnj_abi_sizeof(0) != C.sizeof(Params) or L.sphnj_abi_sizeof(1) != C.sizeof(abi.HostState):
+        if (L.sphnj_abi_sizeof(0) != C.sizeof(Params) or L.sphnj_abi_sizeof(1) != C.sizeof(abi.HostState)
+                or L.sphnj_abi_sizeof(2) != C.sizeof(abi.Diag) or L.sphnj_abi_sizeof(3) != C.sizeof(abi.Tuning)):
             raise SphnjError(abi.ERR_ARG, "ABI layout mismatch between include/sphnj.h and sphnj_gb300/abi.py")
         _lib = L
     return _lib
@@ -245,6 +246,20 @@ class Simulation:
 
     def set_step(self, step: int):
         self._check(self._lib.sphnj_debug_set_step(self._h, int(step)), "set_step")
+
+    def diagnostics(self) -> dict:
+        """Global diagnostics reduced on the device in FP64 (sphnj_diagnostics)."""
+        out = abi.Diag()
+        self._check(self._lib.sphnj_diagnostics(self._h, C.byref(out)), "diagnostics")
+        return out.as_dict()
+
+    def probe(self, points) -> np.ndarray:
+        """Shepard probes at points (n, 2): rows vx, vy, p, rho (sphnj_probe)."""
+        pts = np.ascontiguousarray(points, np.float32).reshape(-1, 2)
+        out = np.empty((len(pts), 4), np.float32)
+        self._check(self._lib.sphnj_probe(self._h, len(pts), pts.ctypes.data_as(abi.PF), out.ctypes.data_as(abi.PF)),
+                    "probe")
+        return out
 
     def checkpoint(self) -> np.ndarray:
         """The complete device state as bytes (sphnj_checkpoint_save)."""

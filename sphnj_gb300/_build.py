@@ -59,22 +59,44 @@ def _compile(src: Path, verbose: bool) -> Path:
     return obj
 
 
+DRIVER_SRC = PKG / "driver" / "sphnj_run.cpp"
+DRIVER = LIBDIR / "sphnj_run"
+
+
+def _build_driver(verbose: bool) -> Path:
+    """The host driver executable, linked against libsphnj.so (found next to
+    it at run time)."""
+    newest = max(DRIVER_SRC.stat().st_mtime, LIB.stat().st_mtime, (ROOT / "include" / "sphnj.h").stat().st_mtime)
+    if DRIVER.exists() and DRIVER.stat().st_mtime >= newest:
+        return DRIVER
+    cxx = os.environ.get("CXX") or shutil.which("g++") or "g++"
+    cmd = [cxx, "-O2", "-std=c++17", f"-I{ROOT / 'include'}", str(DRIVER_SRC), f"-L{LIBDIR}", "-lsphnj",
+           "-Wl,-rpath,$ORIGIN", "-lpthread", "-o", str(DRIVER)]
+    if verbose:
+        print(" ".join(cmd), flush=True)
+    r = subprocess.run(cmd, capture_output=True, text=True)
+    if r.returncode != 0:
+        raise RuntimeError(f"driver build failed\n{r.stdout}\n{r.stderr}")
+    return DRIVER
+
+
 def build(verbose: bool = False, jobs: int | None = None) -> Path:
-    """Compile and link libsphnj.so; returns its path."""
+    """Compile and link libsphnj.so and the sphnj_run driver; returns the
+    library's path."""
     BUILD.mkdir(exist_ok=True)
     LIBDIR.mkdir(exist_ok=True)
     srcs = _sources()
     with cf.ThreadPoolExecutor(max_workers=jobs or min(8, len(srcs))) as ex:
         objs = list(ex.map(lambda s: _compile(s, verbose), srcs))
-    if LIB.exists() and LIB.stat().st_mtime >= max(o.stat().st_mtime for o in objs):
-        return LIB
-    cmd = [nvcc(), *ARCH, "-shared", "-o", str(LIB), *map(str, objs), "-lcudart_static", "-lrt", "-ldl",
-           "-lpthread"]
-    if verbose:
-        print(" ".join(cmd), flush=True)
-    r = subprocess.run(cmd, capture_output=True, text=True)
-    if r.returncode != 0:
-        raise RuntimeError(f"link failed\n{r.stdout}\n{r.stderr}")
+    if not (LIB.exists() and LIB.stat().st_mtime >= max(o.stat().st_mtime for o in objs)):
+        cmd = [nvcc(), *ARCH, "-shared", "-o", str(LIB), *map(str, objs), "-lcudart_static", "-lrt", "-ldl",
+               "-lpthread"]
+        if verbose:
+            print(" ".join(cmd), flush=True)
+        r = subprocess.run(cmd, capture_output=True, text=True)
+        if r.returncode != 0:
+            raise RuntimeError(f"link failed\n{r.stdout}\n{r.stderr}")
+    _build_driver(verbose)
     return LIB
 
 

@@ -148,6 +148,21 @@ class Tuning(C.Structure):
                 "candidates": self.candidates, "ms_per_step": self.ms_per_step}
 
 
+class Diag(C.Structure):
+    """sphnj_diag: global diagnostics reduced on the device in FP64."""
+    _fields_ = [("step", C.c_int32), ("n_liquid", C.c_int32), ("front", C.c_double),
+                ("fluid_momentum", C.c_double * 2), ("fluid_kinetic", C.c_double), ("fluid_mass", C.c_double),
+                ("tip_disp", C.c_double * 2), ("solid_kinetic", C.c_double), ("solid_strain", C.c_double),
+                ("total_force", C.c_double * 2), ("von_mises", C.c_double * 2), ("mean_pressure", C.c_double)]
+
+    def as_dict(self) -> dict:
+        out = {}
+        for name, _ in self._fields_:
+            v = getattr(self, name)
+            out[name] = list(v) if hasattr(v, "__len__") else v
+        return out
+
+
 class HostState(C.Structure):
     _fields_ = [(name, ptr) for name, ptr, _, _, _ in STATE_FIELDS]
 
@@ -237,6 +252,10 @@ def declare(lib: C.CDLL, prefix: str) -> None:
         g("checkpoint_read").argtypes = [vp, C.c_char_p]
         for n in ("checkpoint_size", "checkpoint_save", "checkpoint_load", "checkpoint_write", "checkpoint_read"):
             g(n).restype = C.c_int
+        g("diagnostics").argtypes = [vp, C.POINTER(Diag)]
+        g("diagnostics").restype = C.c_int
+        g("probe").argtypes = [vp, C.c_int, PF, PF]
+        g("probe").restype = C.c_int
         PIi = C.POINTER(C.c_int)
         for pre in ("", "batch_"):
             g(pre + "set_neighbour_lists").argtypes = [vp, C.c_int]

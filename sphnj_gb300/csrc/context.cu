@@ -206,6 +206,8 @@ size_t layout(sphnj_ctx *ctx, char *base) {
     ctx->payload = a.take<char>(pay);
     d.max_speed2_bits = a.take<unsigned int>(1);
     d.err = a.take<DevErr>(1);
+    ctx->diag_part = a.take<double>((size_t)kDiagBlocks * kDiagSlots);
+    ctx->diag_out = a.take<sphnj_diag>(1);
     return a.off;
 }
 
@@ -358,6 +360,7 @@ void sphnj_destroy(sphnj_ctx *ctx) {
     cudaSetDevice(ctx->device);
     if (ctx->st) cudaStreamSynchronize(ctx->st);
     ctx->prof.release();
+    if (ctx->probe_buf) cudaFree(ctx->probe_buf);
     for (auto &g : ctx->graphs) cudaGraphExecDestroy(g.second.exec);
     if (ctx->arena) cudaFree(ctx->arena);
     if (ctx->h_err) cudaFreeHost(ctx->h_err);
@@ -664,6 +667,41 @@ int sphnj_set_tiling(sphnj_ctx *ctx, int tiled, int tile_h) {
     ctx->tiles.tile_h = tile_h;
     drop_graphs(ctx);
     CK(configure_sweeps(ctx->tiles));
+    return SPHNJ_OK;
+}
+
+int sphnj_diagnostics(sphnj_ctx *ctx, sphnj_diag *out) {
+    if (!ctx || !out) return SPHNJ_ERR_ARG;
+    if (!ctx->uploaded) return fail(ctx, SPHNJ_ERR_ARG, "sphnj_diagnostics before sphnj_upload");
+    cudaSetDevice(ctx->device);
+    launch_diagnostics(ctx->st, GroupOne{scene_of(ctx, ctx->parity), ctx->form}, ctx->diag_part, ctx->step,
+                       ctx->diag_out);
+    CK(cudaGetLastError());
+    CK(cudaMemcpyAsync(out, ctx->diag_out, sizeof(sphnj_diag), cudaMemcpyDeviceToHost, ctx->st));
+    CK(cudaStreamSynchronize(ctx->st));
+    return check_device_error(ctx);
+}
+
+int sphnj_probe(sphnj_ctx *ctx, int n, const float *xy, float *out) {
+    if (!ctx || n < 0 || (n > 0 && (!xy || !out))) return SPHNJ_ERR_ARG;
+    if (!ctx->uploaded) return fail(ctx, SPHNJ_ERR_ARG, "sphnj_probe before sphnj_upload");
+    if (n == 0) return SPHNJ_OK;
+    cudaSetDevice(ctx->device);
+    if (n > ctx->probe_cap) {
+        CK(cudaStreamSynchronize(ctx->st));
+        if (ctx->probe_buf) cudaFree(ctx->probe_buf);
+        ctx->probe_buf = nullptr;
+        ctx->probe_cap = 0;
+        CK(cudaMalloc(&ctx->probe_buf, (size_t)n * (sizeof(float2) + sizeof(float4))));
+        ctx->probe_cap = n;
+    }
+    float4 *d_out = static_cast<float4 *>(ctx->probe_buf);
+    float2 *d_pts = reinterpret_cast<float2 *>(d_out + ctx->probe_cap);
+    CK(cudaMemcpyAsync(d_pts, xy, sizeof(float2) * n, cudaMemcpyHostToDevice, ctx->st));
+    launch_probe(ctx->st, GroupOne{scene_of(ctx, ctx->parity), ctx->form}, n, d_pts, d_out);
+    CK(cudaGetLastError());
+    CK(cudaMemcpyAsync(out, d_out, sizeof(float4) * n, cudaMemcpyDeviceToHost, ctx->st));
+    CK(cudaStreamSynchronize(ctx->st));
     return SPHNJ_OK;
 }
 

@@ -74,6 +74,10 @@ struct sphnj_ctx {
     bool virt_cells_valid = false;  // virtual cell ids computed since the last upload
     bool uploaded = false;
     int *f_listed_total = nullptr;
+    double *diag_part = nullptr;       // device: per-block diagnostic partials
+    sphnj_diag *diag_out = nullptr;    // device: the last diagnostics
+    void *probe_buf = nullptr;         // device: probe points and results (grown on demand)
+    int probe_cap = 0;
     sphnj::TileConfig tiles;
     bool use_graphs = true;  // replay each kind of step as a captured CUDA graph
     std::map<int, sphnj::StepGraph> graphs;

@@ -356,5 +356,7 @@ extern "C" int sphnj_read_particles(const char *data_dir, const sphnj_params *p,
 extern "C" int sphnj_abi_sizeof(int which) {
     if (which == 0) return (int)sizeof(sphnj_params);
     if (which == 1) return (int)sizeof(sphnj_host_state);
+    if (which == 2) return (int)sizeof(sphnj_diag);
+    if (which == 3) return (int)sizeof(sphnj_tuning);
     return -1;
 }

@@ -174,6 +174,14 @@ template <class G> int launch_solid_update(cudaStream_t st, G &g, int sub);
 void launch_mixed_split(cudaStream_t st, const GroupOne &g, int kinds);
 void launch_mixed_join(cudaStream_t st, const GroupOne &g);
 
+// global diagnostics (kernels_diag.cu): kDiagBlocks x kDiagSlots doubles of
+// per-block partials, then the result in *out (device memory)
+constexpr int kDiagBlocks = 304;
+constexpr int kDiagSlots = 16;
+void launch_diagnostics(cudaStream_t st, const GroupOne &g, double *part, int step, sphnj_diag *out);
+// Shepard probes at n points (device arrays): out = {vx, vy, p, rho}
+void launch_probe(cudaStream_t st, const GroupOne &g, int n, const float2 *pts, float4 *out);
+
 // state conversion helpers (upload / download of 32-bit enums)
 void launch_u8_from_i32(cudaStream_t st, uint8_t *dst, const int32_t *src, int n);
 void launch_i32_from_u8(cudaStream_t st, int32_t *dst, const uint8_t *src, int n);
