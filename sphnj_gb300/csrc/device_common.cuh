@@ -61,7 +61,8 @@ struct DevState {
     const int *f_listed_total;
     int *stamp;
     // neighbour lists of this step, indexed by the particle's position h in
-    // the fluid CSR list: the tile slots (uint16) of the fluid entries that
+    // the fluid CSR list: the tile slots t (as uint16 byte offsets 8 t into
+    // the tile's staged positions) of the fluid entries that
     // were within the cutoff plus skin when the pair pass ran, in the
     // reference's order, 128 bytes per particle moved in 16-byte chunks of 8
     // slots (row h = f_nbr[h * kNbrChunks .. +kNbrChunks)), and their count

@@ -73,6 +73,7 @@ template <class F> struct SrcGlobal {
     // (the list bodies, which call x(k) without a shift, take their entries
     // from a tile only; with a global source they return before reading)
     __device__ __forceinline__ float2 x(int k, float2 sh = float2()) const { return F::f_nbr(*d, k, sh); }
+    __device__ __forceinline__ float2 x_byte(unsigned off) const { return x((int)(off >> 3)); }
     __device__ __forceinline__ float2 u(int k) const { return __ldg(&d->f_vel[k]); }
     __device__ __forceinline__ float rho(int k) const { return __ldg(&d->f_rho[k]); }
     __device__ __forceinline__ float pr(int k) const { return __ldg(&d->f_p[k]); }
@@ -91,6 +92,10 @@ struct SrcTile {
     }
     __device__ __forceinline__ int key(int t) const { return t; }
     __device__ __forceinline__ float2 x(int k, float2 = float2()) const { return pos[k]; }
+    // position of the entry at byte offset 8 k (a neighbour-list entry)
+    __device__ __forceinline__ float2 x_byte(unsigned off) const {
+        return *reinterpret_cast<const float2 *>(reinterpret_cast<const char *>(pos) + off);
+    }
     __device__ __forceinline__ float2 u(int k) const { return vel[k]; }
     __device__ __forceinline__ float rho(int k) const { return rp[k].x; }
     __device__ __forceinline__ float pr(int k) const { return rp[k].y; }
@@ -374,7 +379,7 @@ __device__ __forceinline__ void pair_particle_listed(const sphnj_params &p, cons
                     b0 = __funnelshift_r(b0, b1, 16);
                     b1 = __funnelshift_r(b1, b2, 16);
                     b2 = __funnelshift_r(b2, b3, 16);
-                    b3 = __funnelshift_r(b3, (unsigned)t, 16);
+                    b3 = __funnelshift_r(b3, (unsigned)t << 3, 16);  // byte offset 8 t (t < 8192)
                     if ((n & 7) == 7) row[n >> 3] = make_uint4(b0, b1, b2, b3);
                 }
                 ++n;
@@ -403,7 +408,7 @@ __device__ __forceinline__ void pair_particle_listed(const sphnj_params &p, cons
 #pragma unroll
         for (int e = 0; e < 8; ++e) {
             if (c + e < n) {
-                const int k = src.key((int)((w[e >> 1] >> (16 * (e & 1))) & 0xFFFFu));
+                const int k = src.key((int)(((w[e >> 1] >> (16 * (e & 1))) & 0xFFFFu) >> 3));
                 const float2 dx = sub2(src.x(k), si.x);
                 if (sqn(dx) < R2) fluid_term(p, src, k, si, dx, a);
             }
@@ -426,16 +431,17 @@ __device__ __forceinline__ void shift_particle_listed(const sphnj_params &p, con
     const float2 x_i = F::f_home(p, d, fr, i);
     const uint4 *row = d.f_nbr + (size_t)h * kNbrChunks;
     float2 g = make_float2(0.f, 0.f);
-    for (int c = 0; c < n; c += 8) {
-        const uint4 v = __ldg(&row[c >> 3]);
+    // entries e < m of one chunk, in order (m = 8 for the full chunks, which
+    // need no per-entry count test)
+    auto chunk = [&](uint4 v, int m) {
         const unsigned w[4] = {v.x, v.y, v.z, v.w};
         float2 x_j[8];
 #pragma unroll
         for (int e = 0; e < 8; ++e)  // all eight loads in flight first
-            x_j[e] = src.x(src.key((int)((w[e >> 1] >> (16 * (e & 1))) & 0xFFFFu)));
+            x_j[e] = src.x_byte((w[e >> 1] >> (16 * (e & 1))) & 0xFFFFu);
 #pragma unroll
         for (int e = 0; e < 8; ++e) {
-            if (c + e < n) {
+            if (e < m) {
                 const float2 dx = sub2(x_j[e], x_i);
                 if (sqn(dx) < R2) {
                     const float kc = gw(p, sqn(dx) * hinv2);
@@ -444,7 +450,10 @@ __device__ __forceinline__ void shift_particle_listed(const sphnj_params &p, con
                 }
             }
         }
-    }
+    };
+    const int full = n >> 3;
+    for (int c = 0; c < full; ++c) chunk(__ldg(&row[c]), 8);
+    if (n & 7) chunk(__ldg(&row[full]), n & 7);
     d.f_grad[i] = g;
 }
 
@@ -550,7 +559,8 @@ __device__ __forceinline__ Frame tile_frame(const sphnj_params &p, const DevStat
 }
 
 template <class G, class F>
-__global__ void __launch_bounds__(kTileBlock) k_fluid_pair_tiled(const __grid_constant__ G gs, int tile_h, int cap,
+// 5 blocks per SM: 48 registers, no spills (unbounded it takes 64 and 4 blocks)
+__global__ void __launch_bounds__(kTileBlock, 5) k_fluid_pair_tiled(const __grid_constant__ G gs, int tile_h, int cap,
                                                                  int use_lists) {
     SPHNJ_SCENE(gs);
     extern __shared__ __align__(16) unsigned char smem[];
@@ -589,7 +599,9 @@ __global__ void __launch_bounds__(kTileBlock) k_fluid_pair_tiled(const __grid_co
 }
 
 template <class G, class F>
-__global__ void __launch_bounds__(kTileBlock) k_shift_gradient_tiled(const __grid_constant__ G gs, int tile_h, int cap,
+// 8 blocks per SM (32 registers, a 28-byte spill): full occupancy measured
+// 4% faster than 40 registers at 6 blocks
+__global__ void __launch_bounds__(kTileBlock, 8) k_shift_gradient_tiled(const __grid_constant__ G gs, int tile_h, int cap,
                                                                      int pass) {
     SPHNJ_SCENE(gs);
     extern __shared__ __align__(16) unsigned char smem[];
