@@ -32,6 +32,27 @@ __device__ __forceinline__ float2 cells_to_len(const sphnj_params &p, int kx, in
     return make_float2(__fmul_rn((float)kx, p.interval[0]), __fmul_rn((float)ky, p.interval[1]));
 }
 
+// 2^x by the SFU (PTX ex2.approx.ftz.f32, relative error ~2^-22)
+__device__ __forceinline__ float ex2_approx(float x) {
+    float y;
+    asm("ex2.approx.ftz.f32 %0, %1;" : "=f"(y) : "f"(x));
+    return y;
+}
+
+// Gaussian kernel-gradient factor W'(r) = exp(-r^2 / h^2) Kd C32 (fluid.cu:44-46)
+// from r^2, as each form evaluates it: the plain form keeps the reference's
+// expression and rounding (exp of -q^2, then times Kd, then times C32); the
+// mixed form folds the constants, 2^(r^2 a) b with a = -log2(e) / h^2 and
+// b = Kd C32 (both loop-invariant), one multiply, one SFU op, one multiply.
+__device__ __forceinline__ float gw_plain(const sphnj_params &p, float r2) {
+    return __expf(-(r2 * p.smoothing_length_inverse_square)) * p.kernel_differential * p.coefficient_3d_to_2d;
+}
+__device__ __forceinline__ float gw_folded(const sphnj_params &p, float r2) {
+    const float a = -1.4426950408889634f * p.smoothing_length_inverse_square;
+    const float b = p.kernel_differential * p.coefficient_3d_to_2d;
+    return ex2_approx(r2 * a) * b;
+}
+
 // Home cell minus frame cell, in cells (mixed form; ignored by the plain form).
 struct Frame {
     int dx, dy;
@@ -39,6 +60,7 @@ struct Frame {
 
 struct FormPlain {
     static constexpr bool kMixed = false;
+    __device__ static __forceinline__ float gw(const sphnj_params &p, float r2) { return gw_plain(p, r2); }
     // frame shift of neighbour slot n (0..8) of the home cell
     __device__ static __forceinline__ float2 shift(const sphnj_params &, Frame, int) { return make_float2(0.f, 0.f); }
     __device__ static __forceinline__ float2 f_home(const sphnj_params &, const DevState &d, Frame, int i) {
@@ -58,6 +80,7 @@ struct FormPlain {
 
 struct FormMixed {
     static constexpr bool kMixed = true;
+    __device__ static __forceinline__ float gw(const sphnj_params &p, float r2) { return gw_folded(p, r2); }
     __device__ static __forceinline__ float2 shift(const sphnj_params &p, Frame f, int n) {
         return cells_to_len(p, f.dx + n / 3 - 1, f.dy + n % 3 - 1);
     }

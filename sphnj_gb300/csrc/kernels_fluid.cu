@@ -47,9 +47,6 @@ constexpr int kBlock = 256;
 constexpr int kFallbackBlocks = 304;  // 2 x 152 SMs, grid-stride
 
 __device__ __forceinline__ float fdiv(float a, float b) { return __fdividef(a, b); }
-__device__ __forceinline__ float gw(const sphnj_params &p, float q2) {
-    return __expf(-q2) * p.kernel_differential * p.coefficient_3d_to_2d;
-}
 __device__ __forceinline__ float2 nrm_fast(float2 a) {
     float z = sqn(a);
     if (z > 0.0f) {
@@ -173,11 +170,11 @@ __device__ __forceinline__ void zero(FAcc &a) {
 }
 
 // fluidFluidCalculate (fluid.cu:25-80) for a neighbour inside the cutoff
-template <class Src>
+template <class F, class Src>
 __device__ __forceinline__ void fluid_term(const sphnj_params &p, const Src &src, int k, const PairI &s, float2 dx,
                                            FAcc &a) {
     const float R2 = p.impact_distance_square;
-    const float kc = gw(p, sqn(dx) * p.smoothing_length_inverse_square);
+    const float kc = F::gw(p, sqn(dx));
     const float2 u_j = src.u(k);
     riemann(s.u, u_j, s.p, src.pr(k), s.rho, src.rho(k), s.cs, dx, kc, a);
     const int ph_j = src.phase(k);
@@ -225,14 +222,14 @@ __device__ __forceinline__ void pair_particle(const sphnj_params &p, const DevSt
         for (int t = rf.x; t < rf.x + rf.y; ++t) {
             const int k = src.key(t);
             const float2 dx = sub2(src.x(k, sh), x_i);
-            if (sqn(dx) < R2) fluid_term(p, src, k, si, dx, a);
+            if (sqn(dx) < R2) fluid_term<F>(p, src, k, si, dx, a);
         }
         const int2 rs = __ldg(&d.rng_s[m]);
         for (int t = rs.x; t < rs.x + rs.y; ++t) {
             const int j = __ldg(&d.lst_s[t]);
             const float2 dx = sub2(F::s_nbr(d, j, sh), x_i);
             if (!(sqn(dx) < R2)) continue;
-            const float kc = gw(p, sqn(dx) * hinv2);
+            const float kc = F::gw(p, sqn(dx));
             const float2 u_j = F::s_vel(d, j);
             riemann(u_i, u_j, p_i, __ldg(&d.s_p[j]), rho_i, rho_i, cs, dx, kc, a);
             a.grad.x += dx.x * kc;
@@ -244,7 +241,7 @@ __device__ __forceinline__ void pair_particle(const sphnj_params &p, const DevSt
             const int j = __ldg(&d.lst_v[t]);
             const float2 dx = sub2(F::v_nbr(d, j, sh), x_i);
             if (!(sqn(dx) < R2)) continue;
-            const float kc = gw(p, sqn(dx) * hinv2);
+            const float kc = F::gw(p, sqn(dx));
             const float rho_j = by_phase(p.reference_density, __ldg(&d.v_phase[j]));
             const float2 u_j = __ldg(&d.v_vel[j]);
             riemann(u_i, u_j, p_i, __ldg(&d.v_p[j]), rho_i, rho_j, cs, dx, kc, a);
@@ -279,7 +276,7 @@ __device__ __forceinline__ void shift_particle(const sphnj_params &p, const DevS
         for (int t = rf.x; t < rf.x + rf.y; ++t) {
             const float2 dx = sub2(src.x(src.key(t), sh), x_i);
             if (sqn(dx) < R2) {
-                const float kc = gw(p, sqn(dx) * hinv2);
+                const float kc = F::gw(p, sqn(dx));
                 g.x += dx.x * kc;
                 g.y += dx.y * kc;
             }
@@ -288,7 +285,7 @@ __device__ __forceinline__ void shift_particle(const sphnj_params &p, const DevS
         for (int t = rs.x; t < rs.x + rs.y; ++t) {
             const float2 dx = sub2(F::s_nbr(d, __ldg(&d.lst_s[t]), sh), x_i);
             if (sqn(dx) < R2) {
-                const float kc = gw(p, sqn(dx) * hinv2);
+                const float kc = F::gw(p, sqn(dx));
                 g.x += dx.x * kc;
                 g.y += dx.y * kc;
             }
@@ -297,7 +294,7 @@ __device__ __forceinline__ void shift_particle(const sphnj_params &p, const DevS
         for (int t = rv.x; t < rv.x + rv.y; ++t) {
             const float2 dx = sub2(F::v_nbr(d, __ldg(&d.lst_v[t]), sh), x_i);
             if (sqn(dx) < R2) {
-                const float kc = gw(p, sqn(dx) * hinv2);
+                const float kc = F::gw(p, sqn(dx));
                 g.x += dx.x * kc;
                 g.y += dx.y * kc;
             }
@@ -410,7 +407,7 @@ __device__ __forceinline__ void pair_particle_listed(const sphnj_params &p, cons
             if (c + e < n) {
                 const int k = src.key((int)(((w[e >> 1] >> (16 * (e & 1))) & 0xFFFFu) >> 3));
                 const float2 dx = sub2(src.x(k), si.x);
-                if (sqn(dx) < R2) fluid_term(p, src, k, si, dx, a);
+                if (sqn(dx) < R2) fluid_term<F>(p, src, k, si, dx, a);
             }
         }
     }
@@ -444,7 +441,7 @@ __device__ __forceinline__ void shift_particle_listed(const sphnj_params &p, con
             if (e < m) {
                 const float2 dx = sub2(x_j[e], x_i);
                 if (sqn(dx) < R2) {
-                    const float kc = gw(p, sqn(dx) * hinv2);
+                    const float kc = F::gw(p, sqn(dx));
                     g.x += dx.x * kc;
                     g.y += dx.y * kc;
                 }
