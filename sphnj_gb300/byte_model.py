@@ -48,10 +48,27 @@ STAGE_KIND = {
 }
 
 
-def bytes_per_launch(stage: str, nf: int, ns: int, nv: int) -> float:
+# The mixed-precision form's own field sizes, for the passes that differ
+# (the rest are as above):
+#   bin             20   read cell 4 + offset 8, write cell 4 + offset 8 when a particle
+#                        changes cell (counted always: 12 + 8)
+#   fluid_pair      71   the pair pass's 67 + the cell id of each staged neighbour 4
+#   fluid_update    89   57 + offset and velocity compensations read and written 32
+#   shift_gradient  20   read offset 8 + cell 4 (staging), write gradient 8
+#   shift_update    95   63 + the two compensations read and written 32
+#   solid passes         FP32 state: deformation 8 + 8 + 8 + 8 read (reference cell, offset,
+#                        displacement of i; neighbours counted once) + writes F, P, L 96 and
+#                        P L, F L 32 = 160; force 8 + 8 + 8 + 16 + 16 + 4 + 1 read, 16 write = 77;
+#                        update 8 + 8 + 8 + 8 + 8 + 1 + 8 read (+ reference cell / offset 16 for the
+#                        current offset), 8 x 5 write = 105
+PER_PARTICLE_MIXED = dict(PER_PARTICLE, bin=20, fluid_pair=71, fluid_update=89, shift_gradient=20,
+                          shift_update=95, solid_deformation=160, solid_force=77, solid_update=105)
+
+
+def bytes_per_launch(stage: str, nf: int, ns: int, nv: int, mixed: bool = False) -> float:
     kind = STAGE_KIND.get(stage, "none")
     n = {"all": nf + ns + nv, "fluid": nf, "solid": ns, "virt": nv, "none": 0}[kind]
-    return float(PER_PARTICLE.get(stage, 0) * n)
+    return float((PER_PARTICLE_MIXED if mixed else PER_PARTICLE).get(stage, 0) * n)
 
 
 def bytes_per_step(nf: int, ns: int, nv: int, shifts: int, substeps: int) -> float:
@@ -69,8 +86,13 @@ MEASURED_TRAFFIC_PER_PARTICLE = {
     "fluid_pair": 165.6,
     "shift_gradient": 148.0,
 }
+# the same capture of the mixed form
+MEASURED_TRAFFIC_PER_PARTICLE_MIXED = {
+    "fluid_pair": 165.8,
+    "shift_gradient": 151.9,
+}
 
 
-def measured_traffic_per_launch(stage: str, nf: int) -> float | None:
-    b = MEASURED_TRAFFIC_PER_PARTICLE.get(stage)
+def measured_traffic_per_launch(stage: str, nf: int, mixed: bool = False) -> float | None:
+    b = (MEASURED_TRAFFIC_PER_PARTICLE_MIXED if mixed else MEASURED_TRAFFIC_PER_PARTICLE).get(stage)
     return None if b is None else float(b * nf)
