@@ -204,6 +204,8 @@ size_t layout(sphnj_ctx *ctx, char *base) {
     const size_t pf = mixed ? 54 : 30, ps = mixed ? 142 : 86, pv = mixed ? 29 : 21;
     size_t pay = std::max((size_t)nf * pf, std::max((size_t)ns * ps, (size_t)nv * pv)) + 16 * 256;
     ctx->payload = a.take<char>(pay);
+    d.tile_list = a.take<int>(C);  // at most one tile per cell (tile height >= 1)
+    d.tile_count = a.take<int>(1);
     d.max_speed2_bits = a.take<unsigned int>(1);
     d.err = a.take<DevErr>(1);
     ctx->diag_part = a.take<double>((size_t)kDiagBlocks * kDiagSlots);

@@ -36,7 +36,7 @@ enum Site : int {
     SITE_REBUILD_CELLS, SITE_REBUILD_TILES, SITE_REBUILD_ONE, SITE_CAPACITY, SITE_COUPLE, SITE_VIRT_NORMAL,
     SITE_VIRT_DATA, SITE_PAIR_TILED, SITE_PAIR_EACH, SITE_PAIR_FALLBACK, SITE_FLUID_UPDATE, SITE_SOLID_DEFORM,
     SITE_SOLID_FORCE, SITE_SOLID_UPDATE, SITE_SHIFT_TILED, SITE_SHIFT_EACH, SITE_SHIFT_FALLBACK,
-    SITE_SHIFT_UPDATE
+    SITE_SHIFT_UPDATE, SITE_TILE_COMPACT, SITE_TILE_SUMS, SITE_TILE_SCATTER
 };
 inline long long site_key(int site, int arg = 0) { return ((long long)site << 32) | (unsigned)arg; }
 
@@ -131,6 +131,20 @@ __host__ __device__ inline int count_of(const sphnj_params &p, Kind k) {
     return k == KF ? p.fluid_number_total : k == KS ? p.solid_number : p.virt_number;
 }
 
+// Tiles of the neighbour sweeps of one scene (column segments of tile_h cells).
+__host__ __device__ inline int sweep_tiles(const sphnj_params &p, int tile_h) {
+    return p.cell_number[0] * ((p.cell_number[1] + tile_h - 1) / tile_h);
+}
+// A scene whose fluid fills few of its tiles - under 64 particles per tile on
+// average (a dam break before the surge fills a small corner of its tank) -
+// sweeps only the tiles listed active this step; a dense scene swept alone
+// gives every tile a block (an empty one returns at once), which saves the
+// list's dependent loads at the start of every block.  Batched launches sweep
+// every scene through its list.
+__host__ __device__ inline bool sweep_compacted(const sphnj_params &p, int tile_h) {
+    return p.fluid_number_total > 0 && (long)p.fluid_number_total < 64L * sweep_tiles(p, tile_h);
+}
+
 // cells: cell ids of every particle (pair.cu:20-64); also resets the
 // per-step accumulators and advances the list stamp.
 template <class G> int launch_bin(cudaStream_t st, G &g, bool with_virt);
@@ -142,6 +156,11 @@ template <class G> int launch_sort_kind(cudaStream_t st, G &g, Kind k, int parit
 // incremental cell-list rebuild of one kind from list buffer parity ^ 1 into
 // list buffer `parity` (pair.cu:66-181)
 template <class G> int launch_rebuild_kind(cudaStream_t st, G &g, Kind k, int parity);
+
+// this step's active tiles of the tiled sweeps (tile height tile_h) into
+// d.tile_list / d.tile_count, in tile order: for every scene with fluid
+// (all_scenes) or for the scenes that sweep_compacted() selects
+template <class G> int launch_tile_compact(cudaStream_t st, G &g, int tile_h, bool all_scenes);
 
 // per-cell capacity check against the reference's 64 slots
 template <class G> int launch_capacity_check(cudaStream_t st, G &g);

@@ -89,6 +89,7 @@ template <class G> __global__ void k_bin(const __grid_constant__ G g, int with_v
     if (t == 0) {
         *d.max_speed2_bits = 0u;
         *d.stamp += 1;  // this step's stamp (read by kernels launched after this one)
+        *d.tile_count = 0;
     }
     if (t < 1 + kMaskShifts) d.disp2_bits[t] = 0u;  // every scene has >= 256 threads
     int kind, i, c;
@@ -215,14 +216,20 @@ __global__ void __launch_bounds__(kBlock) k_scan_tile(const __grid_constant__ G 
     if (threadIdx.x == 0) sc.sums[blk] = total;
 }
 
-// In-place exclusive scan of the tile sums (<= SCAN_MAX_TILES) by one block;
-// with want_total the grand total goes to the scene's listed-particle count.
-template <class G> __global__ void __launch_bounds__(1024) k_scan_sums(const __grid_constant__ G g, int want_total) {
+// In-place exclusive scan of the tile sums (<= SCAN_MAX_TILES) by one block:
+// of the cell scans (sweep_tile_h == 0: one sum per 1024 cells) or of the
+// sweep-tile compaction (one sum per 1024 sweep tiles of height sweep_tile_h).
+// The grand total goes to the scene's listed-particle count (total_to 1), its
+// active-tile count (2) or nowhere (0).
+template <class G>
+__global__ void __launch_bounds__(1024) k_scan_sums(const __grid_constant__ G g, int total_to, int sweep_tile_h) {
     SPHNJ_SCENE(g);
     __shared__ int ws[33];
-    const int ntiles = (p.cell_number_total + SCAN_TILE - 1) / SCAN_TILE;
+    const int units = sweep_tile_h > 0 ? p.cell_number[0] * ((p.cell_number[1] + sweep_tile_h - 1) / sweep_tile_h)
+                                       : p.cell_number_total;
+    const int ntiles = (units + SCAN_TILE - 1) / SCAN_TILE;
     int *sums = S.sc.sums;
-    int *total = want_total ? S.f_listed_total : nullptr;
+    int *total = total_to == 1 ? S.f_listed_total : total_to == 2 ? d.tile_count : nullptr;
     const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
     int v[4], tsum = 0;
 #pragma unroll
@@ -261,6 +268,47 @@ template <class G> __global__ void __launch_bounds__(1024) k_scan_sums(const __g
 
 __device__ __forceinline__ int cell_start(const int *local, const int *sums, int c) {
     return local[c] + sums[c / SCAN_TILE];
+}
+
+// ---- active sweep tiles ------------------------------------------------------
+// Tile t of the neighbour sweeps (column segments of tile_h cells) holds fluid
+// this step.  The active tiles are listed in tile order - an order-preserving
+// compaction (flag scan per 1024 tiles, scan of the tile sums, scatter) - so
+// that blocks sweeping consecutive list entries share staged strips in L2.
+__device__ __forceinline__ bool tile_active(const sphnj_params &p, const DevState &d, int t, int tile_h) {
+    const int ny = p.cell_number[1], tiles_y = (ny + tile_h - 1) / tile_h;
+    const int ci = t / tiles_y, cj0 = (t - ci * tiles_y) * tile_h, cj1 = min(cj0 + tile_h, ny);
+    const int2 h0 = __ldg(&d.rng_f[ci * ny + cj0]), h1 = __ldg(&d.rng_f[ci * ny + cj1 - 1]);
+    return h1.x + h1.y > h0.x;
+}
+
+template <class G> __global__ void __launch_bounds__(kBlock) k_tile_flag_scan(const __grid_constant__ G g, int tile_h) {
+    SPHNJ_SCENE(g);
+    const int nt = sweep_tiles(p, tile_h);
+    const ListScratch &sc = S.sc;
+    const int t0 = blk * SCAN_TILE + threadIdx.x * 4;
+    int v[4], tsum = 0;
+#pragma unroll
+    for (int q = 0; q < 4; ++q) {
+        const int t = t0 + q;
+        v[q] = t < nt && tile_active(p, d, t, tile_h) ? 1 : 0;
+        tsum += v[q];
+    }
+    int total;
+    int ex = block_excl_scan(tsum, &total);
+#pragma unroll
+    for (int q = 0; q < 4; ++q) {
+        if (t0 + q < nt) sc.local[t0 + q] = ex;
+        ex += v[q];
+    }
+    if (threadIdx.x == 0) sc.sums[blk] = total;
+}
+
+template <class G> __global__ void k_tile_scatter(const __grid_constant__ G g, int tile_h) {
+    SPHNJ_SCENE(g);
+    const int t = blk * blockDim.x + threadIdx.x;
+    if (t < sweep_tiles(p, tile_h) && tile_active(p, d, t, tile_h))
+        d.tile_list[cell_start(S.sc.local, S.sc.sums, t)] = t;
 }
 
 // ---- sort ------------------------------------------------------------------
@@ -603,7 +651,7 @@ template <class G> int launch_sort_kind(cudaStream_t st, G &g, Kind k, int parit
     n += launch(g, site_key(SITE_SORT_CLEAR, ki), cells, k_sort_clear<D>, kBlock, 0, st);
     n += launch(g, site_key(SITE_SORT_N, ki), parts, k_hist<D>, kBlock, 0, st, ki);
     n += launch(g, site_key(SITE_SORT_TILES, ki), tiles, k_scan_tile<D, false>, kBlock, 0, st, ki, parity);
-    n += launch(g, site_key(SITE_SORT_ONE, ki), one, k_scan_sums<D>, 1024, 0, st, k == KF ? 1 : 0);
+    n += launch(g, site_key(SITE_SORT_ONE, ki), one, k_scan_sums<D>, 1024, 0, st, k == KF ? 1 : 0, 0);
     n += launch(g, site_key(SITE_SORT_N, ki), parts, k_bucket<D>, kBlock, 0, st, ki);
     n += launch(g, site_key(SITE_SORT_CELLS32, ki), warps, k_cellsort<D>, kBlock, 0, st, ki, parity);
     if (k == KF) {
@@ -629,8 +677,27 @@ template <class G> int launch_rebuild_kind(cudaStream_t st, G &g, Kind k, int pa
     int n = 0;
     n += launch(g, site_key(SITE_REBUILD_CELLS, ki), cells, k_rebuild_count<D>, kBlock, 0, st, ki, parity);
     n += launch(g, site_key(SITE_REBUILD_TILES, ki), tiles, k_scan_tile<D, true>, kBlock, 0, st, ki, parity);
-    n += launch(g, site_key(SITE_REBUILD_ONE, ki), one, k_scan_sums<D>, 1024, 0, st, k == KF ? 1 : 0);
+    n += launch(g, site_key(SITE_REBUILD_ONE, ki), one, k_scan_sums<D>, 1024, 0, st, k == KF ? 1 : 0, 0);
     n += launch(g, site_key(SITE_REBUILD_CELLS, ki), cells, k_rebuild_write<D>, kBlock, 0, st, ki, parity);
+    return n;
+}
+
+template <class G> int launch_tile_compact(cudaStream_t st, G &g, int tile_h, bool all_scenes) {
+    using D = typename G::Dev;
+    auto has = [tile_h, all_scenes](const Scene &s) {
+        return all_scenes ? s.p.fluid_number_total > 0 : sweep_compacted(s.p, tile_h);
+    };
+    int n = launch(
+        g, site_key(SITE_TILE_COMPACT, tile_h),
+        [&](const Scene &s) { return has(s) ? grid_for(sweep_tiles(s.p, tile_h), SCAN_TILE) : 0u; },
+        k_tile_flag_scan<D>, kBlock, 0, st, tile_h);
+    n += launch(
+        g, site_key(SITE_TILE_SUMS, tile_h), [&](const Scene &s) { return has(s) ? 1u : 0u; }, k_scan_sums<D>, 1024, 0,
+        st, 2, tile_h);
+    n += launch(
+        g, site_key(SITE_TILE_SCATTER, tile_h),
+        [&](const Scene &s) { return has(s) ? grid_for(sweep_tiles(s.p, tile_h), kBlock) : 0u; }, k_tile_scatter<D>,
+        kBlock, 0, st, tile_h);
     return n;
 }
 
@@ -644,5 +711,6 @@ SPHNJ_INSTANTIATE_GROUPS(launch_bin, bool);
 SPHNJ_INSTANTIATE_GROUPS(launch_sort_kind, Kind, int);
 SPHNJ_INSTANTIATE_GROUPS(launch_rebuild_kind, Kind, int);
 SPHNJ_INSTANTIATE_GROUPS(launch_capacity_check);
+SPHNJ_INSTANTIATE_GROUPS(launch_tile_compact, int, bool);
 
 }  // namespace sphnj

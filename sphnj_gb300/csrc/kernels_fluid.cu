@@ -36,6 +36,7 @@
 #include "kernels.h"
 
 #include <algorithm>
+#include <type_traits>
 
 namespace sphnj {
 
@@ -555,47 +556,61 @@ __device__ __forceinline__ Frame tile_frame(const sphnj_params &p, const DevStat
     else return Frame{0, 0};
 }
 
-template <class G, class F>
+// kList: the blocks loop over the scene's listed active tiles (batched
+// launches, and scenes that sweep_compacted() selects); otherwise block b
+// sweeps tile b, returning at once if it is empty.
+template <class G, class F, bool kList>
 // 5 blocks per SM: 48 registers, no spills (unbounded it takes 64 and 4 blocks)
 __global__ void __launch_bounds__(kTileBlock, 5) k_fluid_pair_tiled(const __grid_constant__ G gs, int tile_h, int cap,
                                                                  int use_lists) {
     SPHNJ_SCENE(gs);
     extern __shared__ __align__(16) unsigned char smem[];
     __shared__ int s_base[3], s_off[3];
-    TileGeom g;
-    if (!tile_setup(p, d, blk, tile_h, s_base, s_off, g)) return;
     float2 *s_pos = reinterpret_cast<float2 *>(smem);
     float2 *s_vel = s_pos + cap;
     float2 *s_rp = s_vel + cap;
     int *s_idx = reinterpret_cast<int *>(s_rp + cap);
     uint8_t *s_fl = reinterpret_cast<uint8_t *>(s_idx + cap);
-    const bool staged = g.total <= cap;
-    if (staged) {
-        for (int k = threadIdx.x; k < g.total; k += blockDim.x) {
-            const int s = tile_strip(s_off, k);
-            const int j = __ldg(&d.lst_f[s_base[s] + k - s_off[s]]);
-            s_pos[k] = tile_pos<F>(p, d, g, s, j);
-            s_vel[k] = __ldg(&d.f_vel[j]);
-            s_rp[k] = make_float2(__ldg(&d.f_rho[j]), __ldg(&d.f_p[j]));
-            s_idx[k] = j;
-            s_fl[k] = (uint8_t)(__ldg(&d.f_phase[j]) | (__ldg(&d.f_fbt[j]) << 1));
+    auto sweep = [&](int tile) {
+        TileGeom g;
+        if (!tile_setup(p, d, tile, tile_h, s_base, s_off, g)) return;
+        const bool staged = g.total <= cap;
+        if (staged) {
+            for (int k = threadIdx.x; k < g.total; k += blockDim.x) {
+                const int s = tile_strip(s_off, k);
+                const int j = __ldg(&d.lst_f[s_base[s] + k - s_off[s]]);
+                s_pos[k] = tile_pos<F>(p, d, g, s, j);
+                s_vel[k] = __ldg(&d.f_vel[j]);
+                s_rp[k] = make_float2(__ldg(&d.f_rho[j]), __ldg(&d.f_p[j]));
+                s_idx[k] = j;
+                s_fl[k] = (uint8_t)(__ldg(&d.f_phase[j]) | (__ldg(&d.f_fbt[j]) << 1));
+            }
         }
-    }
-    __syncthreads();
-    if (staged) {
-        const SrcTile src{s_pos, s_vel, s_rp, s_fl, s_idx, s_base, s_off};
-        for (int h = g.home_b + threadIdx.x; h < g.home_e; h += blockDim.x) {
-            const int i = d.lst_f[h];
-            pair_particle_listed<F>(p, d, src, i, h, use_lists != 0, tile_frame<F>(p, d, g, i));
+        __syncthreads();
+        if (staged) {
+            const SrcTile src{s_pos, s_vel, s_rp, s_fl, s_idx, s_base, s_off};
+            for (int h = g.home_b + threadIdx.x; h < g.home_e; h += blockDim.x) {
+                const int i = d.lst_f[h];
+                pair_particle_listed<F>(p, d, src, i, h, use_lists != 0, tile_frame<F>(p, d, g, i));
+            }
+        } else {
+            const SrcGlobal<F> src{&d};
+            for (int h = g.home_b + threadIdx.x; h < g.home_e; h += blockDim.x)
+                pair_particle_listed<F>(p, d, src, d.lst_f[h], h, false, Frame{0, 0});
+        }
+    };
+    if constexpr (kList) {
+        const int n_active = *d.tile_count;
+        for (int a = blk; a < n_active; a += nblk) {
+            sweep(__ldg(&d.tile_list[a]));
+            __syncthreads();  // the next tile overwrites the staged entries
         }
     } else {
-        const SrcGlobal<F> src{&d};
-        for (int h = g.home_b + threadIdx.x; h < g.home_e; h += blockDim.x)
-            pair_particle_listed<F>(p, d, src, d.lst_f[h], h, false, Frame{0, 0});
+        sweep(blk);
     }
 }
 
-template <class G, class F>
+template <class G, class F, bool kList>
 // 8 blocks per SM (32 registers, a 28-byte spill): full occupancy measured
 // 4% faster than 40 registers at 6 blocks
 __global__ void __launch_bounds__(kTileBlock, 8) k_shift_gradient_tiled(const __grid_constant__ G gs, int tile_h, int cap,
@@ -603,29 +618,40 @@ __global__ void __launch_bounds__(kTileBlock, 8) k_shift_gradient_tiled(const __
     SPHNJ_SCENE(gs);
     extern __shared__ __align__(16) unsigned char smem[];
     __shared__ int s_base[3], s_off[3];
-    TileGeom g;
-    if (!tile_setup(p, d, blk, tile_h, s_base, s_off, g)) return;
     float2 *s_pos = reinterpret_cast<float2 *>(smem);
-    const bool staged = g.total <= cap;
-    if (staged) {
-        for (int k = threadIdx.x; k < g.total; k += blockDim.x) {
-            const int s = tile_strip(s_off, k);
-            s_pos[k] = tile_pos<F>(p, d, g, s, __ldg(&d.lst_f[s_base[s] + k - s_off[s]]));
-        }
-    }
-    __syncthreads();
     const bool use_list = lists_valid(p, d, pass);
-    if (staged) {
-        const SrcTile src{s_pos, nullptr, nullptr, nullptr, nullptr, s_base, s_off};
-        for (int h = g.home_b + threadIdx.x; h < g.home_e; h += blockDim.x) {
-            const int i = d.lst_f[h];
-            shift_particle_listed<F>(p, d, src, i, h, use_list, tile_frame<F>(p, d, g, i));
+    auto sweep = [&](int tile) {
+        TileGeom g;
+        if (!tile_setup(p, d, tile, tile_h, s_base, s_off, g)) return;
+        const bool staged = g.total <= cap;
+        if (staged) {
+            for (int k = threadIdx.x; k < g.total; k += blockDim.x) {
+                const int s = tile_strip(s_off, k);
+                s_pos[k] = tile_pos<F>(p, d, g, s, __ldg(&d.lst_f[s_base[s] + k - s_off[s]]));
+            }
+        }
+        __syncthreads();
+        if (staged) {
+            const SrcTile src{s_pos, nullptr, nullptr, nullptr, nullptr, s_base, s_off};
+            for (int h = g.home_b + threadIdx.x; h < g.home_e; h += blockDim.x) {
+                const int i = d.lst_f[h];
+                shift_particle_listed<F>(p, d, src, i, h, use_list, tile_frame<F>(p, d, g, i));
+            }
+        } else {
+            // a tile the pair pass could not stage has no lists either
+            const SrcGlobal<F> src{&d};
+            for (int h = g.home_b + threadIdx.x; h < g.home_e; h += blockDim.x)
+                shift_particle_listed<F>(p, d, src, d.lst_f[h], h, false, Frame{0, 0});
+        }
+    };
+    if constexpr (kList) {
+        const int n_active = *d.tile_count;
+        for (int a = blk; a < n_active; a += nblk) {
+            sweep(__ldg(&d.tile_list[a]));
+            __syncthreads();  // the next tile overwrites the staged entries
         }
     } else {
-        // a tile the pair pass could not stage has no lists either
-        const SrcGlobal<F> src{&d};
-        for (int h = g.home_b + threadIdx.x; h < g.home_e; h += blockDim.x)
-            shift_particle_listed<F>(p, d, src, d.lst_f[h], h, false, Frame{0, 0});
+        sweep(blk);
     }
 }
 
@@ -803,6 +829,17 @@ inline int tile_cap(int tile_h) { return 3 * (tile_h + 2) * 24; }
 inline unsigned tile_blocks(const sphnj_params &p, int tile_h) {
     return (unsigned)p.cell_number[0] * (unsigned)((p.cell_number[1] + tile_h - 1) / tile_h);
 }
+// Blocks of the tiled sweeps of one scene: about one per tile that the
+// scene's fluid can fill at ~8 particles per cell, at most one per tile;
+// blocks loop over the active tiles, so a scene whose fluid spreads over more
+// tiles than this is still swept in full.
+inline unsigned sweep_blocks(const sphnj_params &p, int tile_h) {
+    const int nf = p.fluid_number_total;
+    if (nf <= 0) return 0u;
+    if (!sweep_compacted(p, tile_h)) return tile_blocks(p, tile_h);  // one block per tile
+    const long want = std::max<long>(1, ((long)nf + 8L * tile_h - 1) / (8L * tile_h));
+    return (unsigned)std::min<long>(tile_blocks(p, tile_h), want);
+}
 constexpr size_t kPairSmemPerEntry = 3 * sizeof(float2) + sizeof(int) + 1;
 
 }  // namespace
@@ -811,15 +848,33 @@ cudaError_t configure_sweeps(const TileConfig &tc) {
     const size_t smem = tile_cap(tc.tile_h) * kPairSmemPerEntry;  // above 48 KB needs an opt-in
     if (smem <= 48 * 1024) return cudaSuccess;
     const int a = cudaFuncAttributeMaxDynamicSharedMemorySize;
-    cudaError_t e = cudaFuncSetAttribute(k_fluid_pair_tiled<One, FormPlain>, (cudaFuncAttribute)a, (int)smem);
-    if (e == cudaSuccess) e = cudaFuncSetAttribute(k_fluid_pair_tiled<Many, FormPlain>, (cudaFuncAttribute)a, (int)smem);
-    if (e == cudaSuccess) e = cudaFuncSetAttribute(k_fluid_pair_tiled<One, FormMixed>, (cudaFuncAttribute)a, (int)smem);
-    if (e == cudaSuccess) e = cudaFuncSetAttribute(k_fluid_pair_tiled<Many, FormMixed>, (cudaFuncAttribute)a, (int)smem);
-    return e;
+    const void *kernels[] = {
+        (const void *)k_fluid_pair_tiled<One, FormPlain, false>, (const void *)k_fluid_pair_tiled<One, FormPlain, true>,
+        (const void *)k_fluid_pair_tiled<Many, FormPlain, false>, (const void *)k_fluid_pair_tiled<Many, FormPlain, true>,
+        (const void *)k_fluid_pair_tiled<One, FormMixed, false>, (const void *)k_fluid_pair_tiled<One, FormMixed, true>,
+        (const void *)k_fluid_pair_tiled<Many, FormMixed, false>, (const void *)k_fluid_pair_tiled<Many, FormMixed, true>};
+    for (const void *k : kernels) {
+        const cudaError_t e = cudaFuncSetAttribute(k, (cudaFuncAttribute)a, (int)smem);
+        if (e != cudaSuccess) return e;
+    }
+    return cudaSuccess;
 }
 
-// Per-particle fallback grid of one scene: grid-stride, at most 2 blocks per SM.
-inline unsigned fallback_blocks(int n) { return n > 0 ? (unsigned)std::min<long>(kFallbackBlocks, grid_for(n, kPairBlock)) : 0u; }
+// Single scenes use the active-tile list when sweep_compacted() selects it;
+// batches always do (their scenes share one kernel).
+template <class G> bool use_tile_list(const G &g, int tile_h) {
+    if constexpr (std::is_same<G, GroupMany>::value) return true;
+    else return sweep_compacted(g.s.p, tile_h);
+}
+
+// Per-particle fallback grid of one scene (grid-stride; it returns at once
+// when every particle is listed, as it is on nearly every step): one block per
+// 16k particles, at least 16 and at most 2 per SM.
+inline unsigned fallback_blocks(int n) {
+    if (n <= 0) return 0u;
+    const long b = std::min<long>(kFallbackBlocks, std::max<long>(16, (n + 16383) / 16384));
+    return (unsigned)std::min<long>(b, grid_for(n, kPairBlock));
+}
 
 namespace {
 
@@ -831,10 +886,17 @@ template <class F, class G> int fluid_pair(cudaStream_t st, G &g, const TileConf
             k_fluid_pair_each<D, F>, kPairBlock, 0, st, 0);
     const int cap = tile_cap(tc.tile_h);
     const size_t smem = cap * kPairSmemPerEntry;
-    int n = launch(
-        g, site_key(SITE_PAIR_TILED, tc.tile_h),
-        [&](const Scene &s) { return s.p.fluid_number_total > 0 ? tile_blocks(s.p, tc.tile_h) : 0u; },
-        k_fluid_pair_tiled<D, F>, kTileBlock, smem, st, tc.tile_h, cap, tc.lists ? 1 : 0);
+    // this step's active tiles (the cell lists are final), used by the pair
+    // pass and every shifting pass of the step
+    int n = launch_tile_compact(st, g, tc.tile_h, std::is_same<G, GroupMany>::value);
+    auto blocks = [&](const Scene &s) { return sweep_blocks(s.p, tc.tile_h); };
+    const int lists = tc.lists ? 1 : 0;
+    if (use_tile_list(g, tc.tile_h))
+        n += launch(g, site_key(SITE_PAIR_TILED, tc.tile_h), blocks, k_fluid_pair_tiled<D, F, true>, kTileBlock, smem,
+                    st, tc.tile_h, cap, lists);
+    else
+        n += launch(g, site_key(SITE_PAIR_TILED, tc.tile_h), blocks, k_fluid_pair_tiled<D, F, false>, kTileBlock, smem,
+                    st, tc.tile_h, cap, lists);
     n += launch(
         g, site_key(SITE_PAIR_FALLBACK), [](const Scene &s) { return fallback_blocks(s.p.fluid_number_total); },
         k_fluid_pair_each<D, F>, kPairBlock, 0, st, 1);
@@ -856,10 +918,12 @@ template <class F, class G> int shift_gradient(cudaStream_t st, G &g, const Tile
             [&](const Scene &s) { return active(s) ? grid_for(s.p.fluid_number_total, kPairBlock) : 0u; },
             k_shift_gradient_each<D, F>, kPairBlock, 0, st, 0);
     const int cap = tile_cap(tc.tile_h);
-    int n = launch(
-        g, site_key(SITE_SHIFT_TILED, (tc.tile_h << 8) | pass),
-        [&](const Scene &s) { return active(s) ? tile_blocks(s.p, tc.tile_h) : 0u; }, k_shift_gradient_tiled<D, F>,
-        kTileBlock, cap * sizeof(float2), st, tc.tile_h, cap, pass);
+    auto blocks = [&](const Scene &s) { return active(s) ? sweep_blocks(s.p, tc.tile_h) : 0u; };
+    const long long key = site_key(SITE_SHIFT_TILED, (tc.tile_h << 8) | pass);
+    const size_t smem = cap * sizeof(float2);
+    int n = use_tile_list(g, tc.tile_h)
+                ? launch(g, key, blocks, k_shift_gradient_tiled<D, F, true>, kTileBlock, smem, st, tc.tile_h, cap, pass)
+                : launch(g, key, blocks, k_shift_gradient_tiled<D, F, false>, kTileBlock, smem, st, tc.tile_h, cap, pass);
     n += launch(
         g, site_key(SITE_SHIFT_FALLBACK, pass),
         [&](const Scene &s) { return active(s) ? fallback_blocks(s.p.fluid_number_total) : 0u; },
