@@ -64,8 +64,9 @@ struct DevState {
     // the fluid CSR list: the tile slots t (as uint16 byte offsets 8 t into
     // the tile's staged positions) of the fluid entries that
     // were within the cutoff plus skin when the pair pass ran, in the
-    // reference's order, 128 bytes per particle moved in 16-byte chunks of 8
-    // slots (row h = f_nbr[h * kNbrChunks .. +kNbrChunks)), and their count
+    // reference's order, up to 128 bytes per particle moved in 16-byte chunks
+    // of 8 slots, chunk c of particle h at f_nbr[c nf + h] (a warp's
+    // consecutive particles read one contiguous run per chunk), and their count
     // (kNbrNone: no list - the stencil holds solid or virtual entries, the
     // tile was not staged, or the list would exceed kNbrCap)
     uint4 *f_nbr;

@@ -362,7 +362,8 @@ __device__ __forceinline__ void pair_particle_listed(const sphnj_params &p, cons
     }
     const float R2 = p.impact_distance_square, Rs2 = list_radius2(p);
     const PairI si = load_pair_i(p, d, i, F::f_home(p, d, fr, i));
-    uint4 *row = d.f_nbr + (size_t)h * kNbrChunks;
+    const size_t nf = (size_t)p.fluid_number_total;
+    uint4 *col = d.f_nbr + h;  // chunk c at col[c nf]
     // 8-slot FIFO in four registers: each push shifts the 128-bit value down
     // by 16 bits and inserts at the top, so after 8 pushes the first slot is
     // in the low half of b0; full chunks go out as one 16-byte store.
@@ -378,7 +379,7 @@ __device__ __forceinline__ void pair_particle_listed(const sphnj_params &p, cons
                     b1 = __funnelshift_r(b1, b2, 16);
                     b2 = __funnelshift_r(b2, b3, 16);
                     b3 = __funnelshift_r(b3, (unsigned)t << 3, 16);  // byte offset 8 t (t < 8192)
-                    if ((n & 7) == 7) row[n >> 3] = make_uint4(b0, b1, b2, b3);
+                    if ((n & 7) == 7) col[(n >> 3) * nf] = make_uint4(b0, b1, b2, b3);
                 }
                 ++n;
             }
@@ -395,13 +396,13 @@ __device__ __forceinline__ void pair_particle_listed(const sphnj_params &p, cons
             b2 = __funnelshift_r(b2, b3, 16);
             b3 = b3 >> 16;
         }
-        row[n >> 3] = make_uint4(b0, b1, b2, b3);
+        col[(n >> 3) * nf] = make_uint4(b0, b1, b2, b3);
     }
     d.f_nbr_cnt[h] = (uint8_t)n;
     FAcc a;
     zero(a);
     for (int c = 0; c < n; c += 8) {
-        const uint4 v = row[c >> 3];
+        const uint4 v = col[(c >> 3) * nf];
         const unsigned w[4] = {v.x, v.y, v.z, v.w};
 #pragma unroll
         for (int e = 0; e < 8; ++e) {
@@ -425,9 +426,10 @@ __device__ __forceinline__ void shift_particle_listed(const sphnj_params &p, con
         shift_particle<F>(p, d, src, i, fr);
         return;
     }
-    const float R2 = p.impact_distance_square, hinv2 = p.smoothing_length_inverse_square;
+    const float R2 = p.impact_distance_square;
     const float2 x_i = F::f_home(p, d, fr, i);
-    const uint4 *row = d.f_nbr + (size_t)h * kNbrChunks;
+    const size_t nf = (size_t)p.fluid_number_total;
+    const uint4 *col = d.f_nbr + h;  // chunk c at col[c nf]
     float2 g = make_float2(0.f, 0.f);
     // entries e < m of one chunk, in order (m = 8 for the full chunks, which
     // need no per-entry count test)
@@ -449,9 +451,15 @@ __device__ __forceinline__ void shift_particle_listed(const sphnj_params &p, con
             }
         }
     };
+    // each chunk's load is issued one chunk ahead of its use
     const int full = n >> 3;
-    for (int c = 0; c < full; ++c) chunk(__ldg(&row[c]), 8);
-    if (n & 7) chunk(__ldg(&row[full]), n & 7);
+    uint4 next = n > 0 ? __ldg(col) : make_uint4(0u, 0u, 0u, 0u);
+    for (int c = 0; c < full; ++c) {
+        const uint4 v = next;
+        if (8 * (c + 1) < n) next = __ldg(col + (c + 1) * nf);
+        chunk(v, 8);
+    }
+    if (n & 7) chunk(next, n & 7);
     d.f_grad[i] = g;
 }
 
