@@ -391,7 +391,7 @@ int  sphnj_probe(sphnj_ctx *ctx, int n, const float *xy, float *out);
  * calculation.cu:24-46) -------------------------------------------------- */
 
 /* Number of stages reported by sphnj_profile_read, and the name of each
- * (e.g. "fluid_pair", "shift_gradient"). */
+ * (e.g. "fluid_pair", "shift_pass"). */
 int  sphnj_profile_stage_count(void);
 const char *sphnj_profile_stage_name(int stage);
 

@@ -13,15 +13,16 @@ neighbour re-reads are not counted.  Sizes are those of the plain form
                                     gradient 8, du_dx 16 = 41
   fluid_update              57      read pos 8, vel 8, du_dt 8, rho 4, drho 4, phase 1 = 33;
                                     write pos 8, vel 8, rho 4, p 4 = 24
-  shift_gradient            16      read pos 8 (+ cell id), write gradient 8
-  shift_update              63      read gradient 8, color 4, near 1, phase 1, du_dx 16,
-                                    pos 8, vel 8 = 46; write pos 8, vel 8, boundary 1 = 17
+  shift_pass                63      gradient and update in one sweep: read pos 8, color 4,
+                                    near 1, phase 1, du_dx 16, vel 8 = 38; write gradient 8,
+                                    pos 8 (the other buffer), vel 8, boundary 1 = 25
+  shift_copy_back           16      read pos 8, write pos 8 (odd S only)
   virt_data (per virtual)   34      read pos 8, normal 8, phase 1, boundary 1, cell 4;
                                     write vel 8, p 4, rho 4, phase 1 (~34 with the cell id)
   solid per fluid step      48      bin 20 + coupling 28
   solid per sub-step        440     deformation ~178 + force ~181 + update ~81
 
-B_step = N_f (153 + 79 S) + N_v 46 + N_s (48 + 440 k)   (S shifts, k sub-steps)
+B_step = N_f (153 + 63 S + 16 (S odd)) + N_v 46 + N_s (48 + 440 k)   (S shifts, k sub-steps)
 """
 from __future__ import annotations
 
@@ -31,8 +32,8 @@ PER_PARTICLE = {
     "sort": 2 * 50,  # per sort call (the amortised 2 B/step of the model, over 50 steps)
     "fluid_pair": 67,
     "fluid_update": 57,
-    "shift_gradient": 16,
-    "shift_update": 63,
+    "shift_pass": 63,
+    "shift_copy_back": 16,
     "virt_data": 34,
     "solid_couple": 28,
     "solid_deformation": 178,
@@ -43,7 +44,7 @@ PER_PARTICLE = {
 # which particle count a stage's bytes scale with
 STAGE_KIND = {
     "bin": "all", "rebuild": "fluid", "sort": "fluid", "fluid_pair": "fluid", "fluid_update": "fluid",
-    "shift_gradient": "fluid", "shift_update": "fluid", "virt_data": "virt", "solid_couple": "solid",
+    "shift_pass": "fluid", "shift_copy_back": "fluid", "virt_data": "virt", "solid_couple": "solid",
     "solid_deformation": "solid", "solid_force": "solid", "solid_update": "solid", "capacity": "none",
 }
 
@@ -54,15 +55,15 @@ STAGE_KIND = {
 #                        changes cell (counted always: 12 + 8)
 #   fluid_pair      71   the pair pass's 67 + the cell id of each staged neighbour 4
 #   fluid_update    89   57 + offset and velocity compensations read and written 32
-#   shift_gradient  20   read offset 8 + cell 4 (staging), write gradient 8
-#   shift_update    95   63 + the two compensations read and written 32
+#   shift_pass      99   63 + the cell id of each staged neighbour 4 + the two
+#                        compensations read and written 32
 #   solid passes         FP32 state: deformation 8 + 8 + 8 + 8 read (reference cell, offset,
 #                        displacement of i; neighbours counted once) + writes F, P, L 96 and
 #                        P L, F L 32 = 160; force 8 + 8 + 8 + 16 + 16 + 4 + 1 read, 16 write = 77;
 #                        update 8 + 8 + 8 + 8 + 8 + 1 + 8 read (+ reference cell / offset 16 for the
 #                        current offset), 8 x 5 write = 105
-PER_PARTICLE_MIXED = dict(PER_PARTICLE, bin=20, fluid_pair=71, fluid_update=89, shift_gradient=20,
-                          shift_update=95, solid_deformation=160, solid_force=77, solid_update=105)
+PER_PARTICLE_MIXED = dict(PER_PARTICLE, bin=20, fluid_pair=71, fluid_update=89, shift_pass=99,
+                          solid_deformation=160, solid_force=77, solid_update=105)
 
 
 def bytes_per_launch(stage: str, nf: int, ns: int, nv: int, mixed: bool = False) -> float:
@@ -72,7 +73,7 @@ def bytes_per_launch(stage: str, nf: int, ns: int, nv: int, mixed: bool = False)
 
 
 def bytes_per_step(nf: int, ns: int, nv: int, shifts: int, substeps: int) -> float:
-    return float(nf * (153 + 79 * shifts) + nv * 46 + ns * (48 + 440 * substeps))
+    return float(nf * (153 + 63 * shifts + 16 * (shifts & 1)) + nv * 46 + ns * (48 + 440 * substeps))
 
 
 # DRAM traffic (dram__bytes_read.sum + dram__bytes_write.sum) per fluid
@@ -84,12 +85,12 @@ def bytes_per_step(nf: int, ns: int, nv: int, shifts: int, substeps: int) -> flo
 # pass reads them back.
 MEASURED_TRAFFIC_PER_PARTICLE = {
     "fluid_pair": 165.6,
-    "shift_gradient": 148.0,
+    "shift_pass": 148.0,
 }
 # the same capture of the mixed form
 MEASURED_TRAFFIC_PER_PARTICLE_MIXED = {
     "fluid_pair": 165.8,
-    "shift_gradient": 151.9,
+    "shift_pass": 151.9,
 }
 
 

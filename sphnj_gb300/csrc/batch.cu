@@ -28,7 +28,9 @@ struct sphnj_batch {
     int device = 0;
     cudaStream_t own = nullptr, st = nullptr;
     GroupMany g;
-    std::vector<Scene> recs[2];        // host records, list buffer 0 / 1 bound
+    // host records, list buffer 0 / 1 bound: the n scenes, then the same with
+    // their position buffers exchanged (GroupMany::d_scenes)
+    std::vector<Scene> recs[2];
     Scene *d_recs[2] = {nullptr, nullptr};
     TileConfig tiles;
     bool use_graphs = true;
@@ -115,11 +117,16 @@ int sphnj_batch_create(sphnj_ctx *const *scenes, int n, sphnj_batch **out) {
     }
     b->st = b->own;
     for (int par = 0; par < 2; ++par) {
-        b->recs[par].reserve(n);
+        b->recs[par].reserve(2 * (size_t)n);
         for (sphnj_ctx *c : b->scenes) b->recs[par].push_back(scene_of(c, par));
-        cudaError_t e = cudaMalloc(&b->d_recs[par], sizeof(Scene) * n);
+        for (int k = 0; k < n; ++k) {
+            Scene s = b->recs[par][k];
+            exchange_positions(s, c0->form);
+            b->recs[par].push_back(s);
+        }
+        cudaError_t e = cudaMalloc(&b->d_recs[par], sizeof(Scene) * 2 * n);
         if (e == cudaSuccess)
-            e = cudaMemcpy(b->d_recs[par], b->recs[par].data(), sizeof(Scene) * n, cudaMemcpyHostToDevice);
+            e = cudaMemcpy(b->d_recs[par], b->recs[par].data(), sizeof(Scene) * 2 * n, cudaMemcpyHostToDevice);
         if (e != cudaSuccess) {
             cudaGetLastError();
             for (Scene *r : b->d_recs)

@@ -82,7 +82,7 @@ namespace sphnj {
 
 const char *const kStageNames[ST_COUNT] = {"bin", "sort", "rebuild", "capacity", "solid_couple", "virt_data",
                                            "fluid_pair", "fluid_update", "solid_deformation", "solid_force",
-                                           "solid_update", "shift_gradient", "shift_update"};
+                                           "solid_update", "shift_pass", "shift_copy_back"};
 
 cudaEvent_t Profiler::take() {
     if (!pool.empty()) {
@@ -162,6 +162,7 @@ size_t layout(sphnj_ctx *ctx, char *base) {
     d.f_dudx = a.take<float4>(nf);
     d.f_phase = a.take<uint8_t>(nf); d.f_fbt = a.take<uint8_t>(nf); d.f_near = a.take<uint8_t>(nf);
     d.f_cell = a.take<int>(nf);
+    d.f_x_alt = a.take<float2>(nf);
     d.f_listed = a.take<int>(nf);
     ctx->f_listed_total = a.take<int>(1);
     d.f_listed_total = ctx->f_listed_total;
@@ -504,10 +505,8 @@ template <class G> int issue_step(G &g, const StepKind &k, cudaStream_t st, cons
         stage(ST_SOLID_FORCE, [&] { return launch_solid_force(st, g, s); });
         stage(ST_SOLID_UPDATE, [&] { return launch_solid_update(st, g, s); });
     }
-    for (int s = 0; s < shifts; ++s) {
-        stage(ST_SHIFT_GRADIENT, [&] { return launch_shift_gradient(st, g, tc, s); });
-        stage(ST_SHIFT_UPDATE, [&] { return launch_shift_update(st, g, s); });
-    }
+    for (int s = 0; s < shifts; ++s) stage(ST_SHIFT_PASS, [&] { return launch_shift_pass(st, g, tc, s); });
+    if (shifts) stage(ST_SHIFT_COPY_BACK, [&] { return launch_shift_copy_back(st, g); });
     return launched;
 }
 

@@ -13,7 +13,7 @@ namespace sphnj {
 
 enum Stage {
     ST_BIN, ST_SORT, ST_REBUILD, ST_CAPACITY, ST_SOLID_COUPLE, ST_VIRT_DATA, ST_FLUID_PAIR, ST_FLUID_UPDATE,
-    ST_SOLID_DEFORM, ST_SOLID_FORCE, ST_SOLID_UPDATE, ST_SHIFT_GRADIENT, ST_SHIFT_UPDATE, ST_COUNT
+    ST_SOLID_DEFORM, ST_SOLID_FORCE, ST_SOLID_UPDATE, ST_SHIFT_PASS, ST_SHIFT_COPY_BACK, ST_COUNT
 };
 extern const char *const kStageNames[ST_COUNT];
 

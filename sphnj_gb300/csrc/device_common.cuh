@@ -39,6 +39,10 @@ struct DevState {
     float4 *f_dudx;
     uint8_t *f_phase, *f_fbt, *f_near;
     int *f_cell;
+    // second fluid position buffer of the shifting passes: a pass reads the
+    // positions (f_pos, or f_off in the mixed form) and writes the shifted
+    // ones here; the launches of odd passes exchange the two pointers
+    float2 *f_x_alt;
     // solid
     double2 *s_pos, *s_ref, *s_vel, *s_dudt;
     dmat2 *s_F, *s_P, *s_L, *s_maxstrain;

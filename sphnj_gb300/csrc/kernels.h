@@ -36,10 +36,21 @@ enum Site : int {
     SITE_REBUILD_CELLS, SITE_REBUILD_TILES, SITE_REBUILD_ONE, SITE_CAPACITY, SITE_COUPLE, SITE_VIRT_NORMAL,
     SITE_VIRT_DATA, SITE_PAIR_TILED, SITE_PAIR_EACH, SITE_PAIR_FALLBACK, SITE_FLUID_UPDATE, SITE_SOLID_DEFORM,
     SITE_SOLID_FORCE, SITE_SOLID_UPDATE, SITE_SHIFT_TILED, SITE_SHIFT_EACH, SITE_SHIFT_FALLBACK,
-    SITE_SHIFT_UPDATE, SITE_TILE_COMPACT, SITE_TILE_SUMS, SITE_TILE_SCATTER
+    SITE_SHIFT_COPY_BACK, SITE_TILE_COMPACT, SITE_TILE_SUMS, SITE_TILE_SCATTER
 };
 inline long long site_key(int site, int arg = 0) { return ((long long)site << 32) | (unsigned)arg; }
 
+// The record with its fluid position buffer (f_pos, or f_off in the mixed
+// form) and the shifting passes' second buffer f_x_alt exchanged.
+inline void exchange_positions(Scene &s, int form) {
+    float2 *&x = form == SPHNJ_FORM_MIXED ? s.d.f_off : s.d.f_pos;
+    float2 *t = x;
+    x = s.d.f_x_alt;
+    s.d.f_x_alt = t;
+}
+
+// exchange_positions() switches the group's records between the two buffer
+// assignments (called in pairs around the launches of an odd shifting pass).
 struct GroupOne {
     using Dev = One;
     Scene s;
@@ -50,14 +61,19 @@ struct GroupOne {
         return blocks > 0;
     }
     template <class Pred> bool any(Pred &&pr) const { return pr(s.p); }
+    void exchange_positions() { sphnj::exchange_positions(s, form); }
 };
 
 struct GroupMany {
     using Dev = Many;
-    const Scene *h_scenes = nullptr;  // host copies of the records in d_scenes
+    const Scene *h_scenes = nullptr;  // host copies of the first n records of d_scenes
     int n = 0;
     int form = SPHNJ_FORM_PLAIN;      // every scene of a group has the same form
-    const Scene *d_scenes = nullptr;  // device records of the current parity
+    // device records of the current list parity: n records, then the same n
+    // with their position buffers exchanged
+    const Scene *d_scenes = nullptr;
+    bool exchanged = false;
+    void exchange_positions() { exchanged = !exchanged; }
     // With `planning` set, prepare() builds the block table of each launch
     // (synchronous allocation and copy) and launches nothing; a launch
     // sequence is planned once before it is captured into a graph.
@@ -99,7 +115,7 @@ struct GroupMany {
         }
         if (planning) return false;
         blocks = it->second.total;
-        dev.scenes = d_scenes;
+        dev.scenes = d_scenes + (exchanged ? n : 0);
         dev.first = it->second.first;
         dev.n = n;
         return blocks > 0;
@@ -172,10 +188,12 @@ cudaError_t configure_sweeps(const TileConfig &tc);
 // fluid passes (fluid.cu)
 template <class G> int launch_fluid_pair(cudaStream_t st, G &g, const TileConfig &tc);
 template <class G> int launch_fluid_update(cudaStream_t st, G &g);
-// pass = index of the shifting pass within the step; scenes with fewer
-// shifting passes per step own no block of it
-template <class G> int launch_shift_gradient(cudaStream_t st, G &g, const TileConfig &tc, int pass);
-template <class G> int launch_shift_update(cudaStream_t st, G &g, int pass);
+// Shifting pass `pass` of the step (gradient and position update in one
+// sweep; scenes with fewer shifting passes per step own no block of it), and,
+// after the last pass, the copy of the positions back to f_pos / f_off in the
+// scenes whose number of passes is odd.
+template <class G> int launch_shift_pass(cudaStream_t st, G &g, const TileConfig &tc, int pass);
+template <class G> int launch_shift_copy_back(cudaStream_t st, G &g);
 
 // virtual particles (virt.cu)
 template <class G> int launch_virt_normal(cudaStream_t st, G &g);

@@ -13,9 +13,11 @@
 //                    multiplies and adds and compared as float bits, which
 //                    equals the reference's host loop over |v| (sqrt is
 //                    monotone), so max_speed is bit-identical.
-//   shift gradient   correctionCalculate (fluid.cu:304-367)
-//   k_shift_update   shiftDisplacementCalculate + correctionUpdate
-//                    (fluid.cu:369-427)
+//   shifting pass    correctionCalculate (fluid.cu:304-367) fused with
+//                    shiftDisplacementCalculate + correctionUpdate
+//                    (fluid.cu:369-427): the thread that sums a particle's
+//                    shifting gradient also moves it, into a second position
+//                    buffer (the passes alternate between the two)
 //
 // The two neighbour sweeps are tiled: a block owns a column segment of
 // `tile_h` cells and stages the fluid neighbours of that segment - three
@@ -260,10 +262,10 @@ __device__ __forceinline__ void pair_particle(const sphnj_params &p, const DevSt
     store_pair(d, i, a);
 }
 
-// correctionCalculate for particle i (fluid.cu:316-367)
+// correctionCalculate for particle i (fluid.cu:316-367): its shifting gradient
 template <class F, class Src>
-__device__ __forceinline__ void shift_particle(const sphnj_params &p, const DevState &d, const Src &src, int i,
-                                               Frame fr) {
+__device__ __forceinline__ float2 shift_particle(const sphnj_params &p, const DevState &d, const Src &src, int i,
+                                                 Frame fr) {
     const int nx = p.cell_number[0], ny = p.cell_number[1];
     const float R2 = p.impact_distance_square, hinv2 = p.smoothing_length_inverse_square;
     const float2 x_i = F::f_home(p, d, fr, i);
@@ -301,7 +303,7 @@ __device__ __forceinline__ void shift_particle(const sphnj_params &p, const DevS
             }
         }
     }
-    d.f_grad[i] = g;
+    return g;
 }
 
 // ---- neighbour lists ----------------------------------------------------------
@@ -416,16 +418,13 @@ __device__ __forceinline__ void pair_particle_listed(const sphnj_params &p, cons
     store_pair(d, i, a);
 }
 
-// Shifting gradient of particle i at CSR position h through its neighbour
+// Shifting gradient of particle i at CSR position h, through its neighbour
 // list when use_list (and it has one).
 template <class F, class Src>
-__device__ __forceinline__ void shift_particle_listed(const sphnj_params &p, const DevState &d, const Src &src, int i,
-                                                      int h, bool use_list, Frame fr) {
+__device__ __forceinline__ float2 shift_particle_listed(const sphnj_params &p, const DevState &d, const Src &src,
+                                                        int i, int h, bool use_list, Frame fr) {
     const int n = use_list ? (int)d.f_nbr_cnt[h] : (int)kNbrNone;
-    if (n == kNbrNone) {
-        shift_particle<F>(p, d, src, i, fr);
-        return;
-    }
+    if (n == kNbrNone) return shift_particle<F>(p, d, src, i, fr);
     const float R2 = p.impact_distance_square;
     const float2 x_i = F::f_home(p, d, fr, i);
     const size_t nf = (size_t)p.fluid_number_total;
@@ -460,7 +459,7 @@ __device__ __forceinline__ void shift_particle_listed(const sphnj_params &p, con
         chunk(v, 8);
     }
     if (n & 7) chunk(next, n & 7);
-    d.f_grad[i] = g;
+    return g;
 }
 
 // The lists of this step still hold every pair within the cutoff when twice
@@ -493,6 +492,82 @@ __device__ __forceinline__ unsigned int disp2(float2 a, float2 b) {
     const float dx = b.x - a.x, dy = b.y - a.y;
     const float v = dx * dx + dy * dy;
     return v == v ? __float_as_uint(v) : 0x7f800000u;  // NaN: treat as unbounded
+}
+
+// (I - n n^T) d with n = normalize(g), zeroed below EPS_FOR_SUM
+// (fluid.cu:394-397)
+__device__ __forceinline__ float2 project(float2 g, float2 disp) {
+    float2 n = normalized(g);
+    if (sqrtf(sqn(n)) < EPS_FOR_SUM) n = make_float2(0.f, 0.f);
+    float m00 = 1.0f - n.x * n.x, m10 = 0.0f - n.y * n.x, m01 = 0.0f - n.x * n.y, m11 = 1.0f - n.y * n.y;
+    return make_float2(m00 * disp.x + m01 * disp.y, m10 * disp.x + m11 * disp.y);
+}
+
+// shiftDisplacementCalculate + correctionUpdate (fluid.cu:369-427) for
+// particle i with shifting gradient g, done by the thread that computed g.
+// The pass reads the positions from f_pos (f_off in the mixed form) and
+// writes the shifted one to f_x_alt, so that every other particle's gradient
+// in this pass still sees the positions before the update; the velocity,
+// boundary type, compensations and the gradient itself are only ever read
+// by particle i's own thread during the shifting passes and are updated in
+// place.  Returns the squared displacement (float bits).
+template <class F>
+__device__ __forceinline__ unsigned int shift_update_particle(const sphnj_params &p, const DevState &d, int i,
+                                                              float2 g) {
+    d.f_grad[i] = g;
+    // getMaxSpeed's clamp, fluid.cu:438-439
+    const float vmax = __fsqrt_rn(__uint_as_float(*d.max_speed2_bits));
+    const float max_speed = fminf(vmax, __fmul_rn(0.1f, fminf(p.sound_speed[0], p.sound_speed[1])));
+    const float s = -p.particle_shift_coef * p.smoothing_length * p.dt;
+    const float2 disp = make_float2(s * g.x, s * g.y);
+    const int ph = d.f_phase[i];
+    const float color = d.f_color[i];
+    const int near = d.f_near[i];
+    float2 dd;
+    uint8_t bt;
+    if (ph == SPHNJ_GAS) {
+        bt = SPHNJ_INNER;
+        dd = disp;
+    } else if (color < 1.5f) {
+        if (near == SPHNJ_NO_PARTICLE) {
+            bt = SPHNJ_SPLASH;
+            dd = make_float2(0.f, 0.f);
+        } else {
+            bt = SPHNJ_FREE_SURFACE;
+            dd = project(g, disp);
+        }
+    } else if (color < 2.0f && near == SPHNJ_HAS_NEAR_PARTICLE) {
+        bt = SPHNJ_VICINITY;
+        dd = project(g, disp);
+    } else {
+        bt = SPHNJ_INNER;
+        dd = disp;
+    }
+    d.f_fbt[i] = bt;
+    const float2 sh = make_float2(max_speed * dd.x, max_speed * dd.y);
+    const float4 m = d.f_dudx[i];
+    if constexpr (F::kMixed) {
+        float2 x = d.f_off[i], xc = d.f_offc[i], v = d.f_vel[i], vc = d.f_velc[i];
+        const float2 x0 = x;
+        kahan_add2(x, xc, sh);
+        kahan_add2(v, vc, make_float2(m.x * sh.x + m.z * sh.y, m.y * sh.x + m.w * sh.y));
+        d.f_x_alt[i] = x;
+        d.f_offc[i] = xc;
+        d.f_vel[i] = v;
+        d.f_velc[i] = vc;
+        return disp2(x0, x);
+    } else {
+        const float2 x0 = d.f_pos[i];
+        float2 x = x0;
+        x.x += sh.x;
+        x.y += sh.y;
+        d.f_x_alt[i] = x;
+        float2 v = d.f_vel[i];
+        v.x += m.x * sh.x + m.z * sh.y;
+        v.y += m.y * sh.x + m.w * sh.y;
+        d.f_vel[i] = v;
+        return disp2(x0, x);
+    }
 }
 
 // ---- tiles ---------------------------------------------------------------
@@ -618,6 +693,8 @@ __global__ void __launch_bounds__(kTileBlock, 5) k_fluid_pair_tiled(const __grid
     }
 }
 
+// One shifting pass over the listed particles: each home particle's gradient,
+// then its position update (shift_update_particle) by the same thread.
 template <class G, class F, bool kList>
 // 8 blocks per SM (32 registers, a 28-byte spill): full occupancy measured
 // 4% faster than 40 registers at 6 blocks
@@ -628,6 +705,7 @@ __global__ void __launch_bounds__(kTileBlock, 8) k_shift_gradient_tiled(const __
     __shared__ int s_base[3], s_off[3];
     float2 *s_pos = reinterpret_cast<float2 *>(smem);
     const bool use_list = lists_valid(p, d, pass);
+    unsigned int moved2 = 0u;
     auto sweep = [&](int tile) {
         TileGeom g;
         if (!tile_setup(p, d, tile, tile_h, s_base, s_off, g)) return;
@@ -643,13 +721,17 @@ __global__ void __launch_bounds__(kTileBlock, 8) k_shift_gradient_tiled(const __
             const SrcTile src{s_pos, nullptr, nullptr, nullptr, nullptr, s_base, s_off};
             for (int h = g.home_b + threadIdx.x; h < g.home_e; h += blockDim.x) {
                 const int i = d.lst_f[h];
-                shift_particle_listed<F>(p, d, src, i, h, use_list, tile_frame<F>(p, d, g, i));
+                const float2 gr = shift_particle_listed<F>(p, d, src, i, h, use_list, tile_frame<F>(p, d, g, i));
+                moved2 = max(moved2, shift_update_particle<F>(p, d, i, gr));
             }
         } else {
             // a tile the pair pass could not stage has no lists either
             const SrcGlobal<F> src{&d};
-            for (int h = g.home_b + threadIdx.x; h < g.home_e; h += blockDim.x)
-                shift_particle_listed<F>(p, d, src, d.lst_f[h], h, false, Frame{0, 0});
+            for (int h = g.home_b + threadIdx.x; h < g.home_e; h += blockDim.x) {
+                const int i = d.lst_f[h];
+                const float2 gr = shift_particle_listed<F>(p, d, src, i, h, false, Frame{0, 0});
+                moved2 = max(moved2, shift_update_particle<F>(p, d, i, gr));
+            }
         }
     };
     if constexpr (kList) {
@@ -661,6 +743,7 @@ __global__ void __launch_bounds__(kTileBlock, 8) k_shift_gradient_tiled(const __
     } else {
         sweep(blk);
     }
+    if (pass < kMaskShifts) block_max_to<kTileBlock>(moved2, &d.disp2_bits[1 + pass]);
 }
 
 // Per-particle forms: every particle (listed == null), or only the particles
@@ -677,14 +760,18 @@ __global__ void __launch_bounds__(kPairBlock) k_fluid_pair_each(const __grid_con
 }
 
 template <class G, class F>
-__global__ void __launch_bounds__(kPairBlock) k_shift_gradient_each(const __grid_constant__ G g, int only_unlisted) {
+__global__ void __launch_bounds__(kPairBlock) k_shift_gradient_each(const __grid_constant__ G g, int only_unlisted,
+                                                                   int pass) {
     SPHNJ_SCENE(g);
     const int nf = p.fluid_number_total;
     if (only_unlisted && *d.f_listed_total == nf) return;
     const int stamp = *d.stamp;
     const SrcGlobal<F> src{&d};
+    unsigned int moved2 = 0u;
     for (int i = blk * blockDim.x + threadIdx.x; i < nf; i += nblk * blockDim.x)
-        if (!only_unlisted || d.f_listed[i] != stamp) shift_particle<F>(p, d, src, i, Frame{0, 0});
+        if (!only_unlisted || d.f_listed[i] != stamp)
+            moved2 = max(moved2, shift_update_particle<F>(p, d, i, shift_particle<F>(p, d, src, i, Frame{0, 0})));
+    if (pass < kMaskShifts) block_max_to<kPairBlock>(moved2, &d.disp2_bits[1 + pass]);
 }
 
 // densityToPressure, fluid.cu:15-23
@@ -755,82 +842,12 @@ template <class G, class F> __global__ void __launch_bounds__(kBlock) k_fluid_up
     block_max_to<kBlock>(moved2, &d.disp2_bits[0]);
 }
 
-// (I - n n^T) d with n = normalize(g), zeroed below EPS_FOR_SUM
-// (fluid.cu:394-397)
-__device__ __forceinline__ float2 project(float2 g, float2 disp) {
-    float2 n = normalized(g);
-    if (sqrtf(sqn(n)) < EPS_FOR_SUM) n = make_float2(0.f, 0.f);
-    float m00 = 1.0f - n.x * n.x, m10 = 0.0f - n.y * n.x, m01 = 0.0f - n.x * n.y, m11 = 1.0f - n.y * n.y;
-    return make_float2(m00 * disp.x + m01 * disp.y, m10 * disp.x + m11 * disp.y);
-}
-
-// shiftDisplacementCalculate + correctionUpdate for particle i; returns the
-// squared displacement (float bits)
-template <class F>
-__device__ __forceinline__ unsigned int shift_update_particle(const sphnj_params &p, const DevState &d, int i) {
-    // getMaxSpeed's clamp, fluid.cu:438-439
-    const float vmax = __fsqrt_rn(__uint_as_float(*d.max_speed2_bits));
-    const float max_speed = fminf(vmax, __fmul_rn(0.1f, fminf(p.sound_speed[0], p.sound_speed[1])));
-    const float s = -p.particle_shift_coef * p.smoothing_length * p.dt;
-    const float2 g = d.f_grad[i];
-    const float2 disp = make_float2(s * g.x, s * g.y);
-    const int ph = d.f_phase[i];
-    const float color = d.f_color[i];
-    const int near = d.f_near[i];
-    float2 dd;
-    uint8_t bt;
-    if (ph == SPHNJ_GAS) {
-        bt = SPHNJ_INNER;
-        dd = disp;
-    } else if (color < 1.5f) {
-        if (near == SPHNJ_NO_PARTICLE) {
-            bt = SPHNJ_SPLASH;
-            dd = make_float2(0.f, 0.f);
-        } else {
-            bt = SPHNJ_FREE_SURFACE;
-            dd = project(g, disp);
-        }
-    } else if (color < 2.0f && near == SPHNJ_HAS_NEAR_PARTICLE) {
-        bt = SPHNJ_VICINITY;
-        dd = project(g, disp);
-    } else {
-        bt = SPHNJ_INNER;
-        dd = disp;
-    }
-    d.f_fbt[i] = bt;
-    const float2 sh = make_float2(max_speed * dd.x, max_speed * dd.y);
-    const float4 m = d.f_dudx[i];
-    if constexpr (F::kMixed) {
-        float2 x = d.f_off[i], xc = d.f_offc[i], v = d.f_vel[i], vc = d.f_velc[i];
-        const float2 x0 = x;
-        kahan_add2(x, xc, sh);
-        kahan_add2(v, vc, make_float2(m.x * sh.x + m.z * sh.y, m.y * sh.x + m.w * sh.y));
-        d.f_off[i] = x;
-        d.f_offc[i] = xc;
-        d.f_vel[i] = v;
-        d.f_velc[i] = vc;
-        return disp2(x0, x);
-    } else {
-        const float2 x0 = d.f_pos[i];
-        float2 x = x0;
-        x.x += sh.x;
-        x.y += sh.y;
-        d.f_pos[i] = x;
-        float2 v = d.f_vel[i];
-        v.x += m.x * sh.x + m.z * sh.y;
-        v.y += m.y * sh.x + m.w * sh.y;
-        d.f_vel[i] = v;
-        return disp2(x0, x);
-    }
-}
-
-template <class G, class F>
-__global__ void __launch_bounds__(kBlock) k_shift_update(const __grid_constant__ G g, int pass) {
+// Positions back from the second buffer after an odd number of shifting
+// passes (the record's f_x_alt holds them; f_pos / f_off is their home).
+template <class G, class F> __global__ void __launch_bounds__(kBlock) k_shift_copy_back(const __grid_constant__ G g) {
     SPHNJ_SCENE(g);
     const int i = blk * blockDim.x + threadIdx.x;
-    unsigned int moved2 = 0u;
-    if (i < p.fluid_number_total) moved2 = shift_update_particle<F>(p, d, i);
-    if (pass < kMaskShifts) block_max_to<kBlock>(moved2, &d.disp2_bits[1 + pass]);
+    if (i < p.fluid_number_total) (F::kMixed ? d.f_off : d.f_pos)[i] = d.f_x_alt[i];
 }
 
 inline int tile_cap(int tile_h) { return 3 * (tile_h + 2) * 24; }
@@ -917,14 +934,29 @@ template <class F, class G> int fluid_update(cudaStream_t st, G &g) {
         k_fluid_update<typename G::Dev, F>, kBlock, 0, st);
 }
 
-template <class F, class G> int shift_gradient(cudaStream_t st, G &g, const TileConfig &tc, int pass) {
+// Pass k reads the positions from f_pos / f_off and writes them to f_x_alt;
+// odd passes run with the two exchanged, so pass k + 1 reads what pass k
+// wrote and the positions are home again after every even pass.
+template <class G> struct PositionsExchanged {
+    G &g;
+    bool on;
+    PositionsExchanged(G &g_, bool on_) : g(g_), on(on_) {
+        if (on) g.exchange_positions();
+    }
+    ~PositionsExchanged() {
+        if (on) g.exchange_positions();
+    }
+};
+
+template <class F, class G> int shift_pass(cudaStream_t st, G &g, const TileConfig &tc, int pass) {
     using D = typename G::Dev;
+    const PositionsExchanged<G> buffers(g, (pass & 1) != 0);
     auto active = [pass](const Scene &s) { return s.p.fluid_number_total > 0 && pass < s.p.shift_per_step; };
     if (!tc.tiled)
         return launch(
             g, site_key(SITE_SHIFT_EACH, pass),
             [&](const Scene &s) { return active(s) ? grid_for(s.p.fluid_number_total, kPairBlock) : 0u; },
-            k_shift_gradient_each<D, F>, kPairBlock, 0, st, 0);
+            k_shift_gradient_each<D, F>, kPairBlock, 0, st, 0, pass);
     const int cap = tile_cap(tc.tile_h);
     auto blocks = [&](const Scene &s) { return active(s) ? sweep_blocks(s.p, tc.tile_h) : 0u; };
     const long long key = site_key(SITE_SHIFT_TILED, (tc.tile_h << 8) | pass);
@@ -935,15 +967,15 @@ template <class F, class G> int shift_gradient(cudaStream_t st, G &g, const Tile
     n += launch(
         g, site_key(SITE_SHIFT_FALLBACK, pass),
         [&](const Scene &s) { return active(s) ? fallback_blocks(s.p.fluid_number_total) : 0u; },
-        k_shift_gradient_each<D, F>, kPairBlock, 0, st, 1);
+        k_shift_gradient_each<D, F>, kPairBlock, 0, st, 1, pass);
     return n;
 }
 
-template <class F, class G> int shift_update(cudaStream_t st, G &g, int pass) {
+template <class F, class G> int shift_copy_back(cudaStream_t st, G &g) {
     return launch(
-        g, site_key(SITE_SHIFT_UPDATE, pass),
-        [pass](const Scene &s) { return pass < s.p.shift_per_step ? grid_for(s.p.fluid_number_total, kBlock) : 0u; },
-        k_shift_update<typename G::Dev, F>, kBlock, 0, st, pass);
+        g, site_key(SITE_SHIFT_COPY_BACK),
+        [](const Scene &s) { return (s.p.shift_per_step & 1) ? grid_for(s.p.fluid_number_total, kBlock) : 0u; },
+        k_shift_copy_back<typename G::Dev, F>, kBlock, 0, st);
 }
 
 }  // namespace
@@ -954,17 +986,16 @@ template <class G> int launch_fluid_pair(cudaStream_t st, G &g, const TileConfig
 template <class G> int launch_fluid_update(cudaStream_t st, G &g) {
     return g.form == SPHNJ_FORM_MIXED ? fluid_update<FormMixed>(st, g) : fluid_update<FormPlain>(st, g);
 }
-template <class G> int launch_shift_gradient(cudaStream_t st, G &g, const TileConfig &tc, int pass) {
-    return g.form == SPHNJ_FORM_MIXED ? shift_gradient<FormMixed>(st, g, tc, pass)
-                                      : shift_gradient<FormPlain>(st, g, tc, pass);
+template <class G> int launch_shift_pass(cudaStream_t st, G &g, const TileConfig &tc, int pass) {
+    return g.form == SPHNJ_FORM_MIXED ? shift_pass<FormMixed>(st, g, tc, pass) : shift_pass<FormPlain>(st, g, tc, pass);
 }
-template <class G> int launch_shift_update(cudaStream_t st, G &g, int pass) {
-    return g.form == SPHNJ_FORM_MIXED ? shift_update<FormMixed>(st, g, pass) : shift_update<FormPlain>(st, g, pass);
+template <class G> int launch_shift_copy_back(cudaStream_t st, G &g) {
+    return g.form == SPHNJ_FORM_MIXED ? shift_copy_back<FormMixed>(st, g) : shift_copy_back<FormPlain>(st, g);
 }
 
 SPHNJ_INSTANTIATE_GROUPS(launch_fluid_pair, const TileConfig &);
 SPHNJ_INSTANTIATE_GROUPS(launch_fluid_update);
-SPHNJ_INSTANTIATE_GROUPS(launch_shift_gradient, const TileConfig &, int);
-SPHNJ_INSTANTIATE_GROUPS(launch_shift_update, int);
+SPHNJ_INSTANTIATE_GROUPS(launch_shift_pass, const TileConfig &, int);
+SPHNJ_INSTANTIATE_GROUPS(launch_shift_copy_back);
 
 }  // namespace sphnj
