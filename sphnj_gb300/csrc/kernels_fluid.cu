@@ -488,6 +488,17 @@ __device__ __forceinline__ void block_max_to(unsigned int v, unsigned int *dst) 
     }
 }
 
+// Warp-wide max of non-negative float bits with no block barrier (so a warp
+// that finishes its particles early does not wait for the block's slowest):
+// lane 0 issues the atomicMax only when the value already in *dst is smaller.
+// *dst only grows while the max is taken, so a stale read costs at most a
+// redundant atomic.  All 32 lanes of the warp call it.
+__device__ __forceinline__ void warp_max_to(unsigned int v, unsigned int *dst) {
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v = max(v, __shfl_xor_sync(0xffffffffu, v, o));
+    if ((threadIdx.x & 31) == 0 && v > __ldcg(dst)) atomicMax(dst, v);
+}
+
 __device__ __forceinline__ unsigned int disp2(float2 a, float2 b) {
     const float dx = b.x - a.x, dy = b.y - a.y;
     const float v = dx * dx + dy * dy;
@@ -743,7 +754,7 @@ __global__ void __launch_bounds__(kTileBlock, 8) k_shift_gradient_tiled(const __
     } else {
         sweep(blk);
     }
-    if (pass < kMaskShifts) block_max_to<kTileBlock>(moved2, &d.disp2_bits[1 + pass]);
+    if (pass < kMaskShifts) warp_max_to(moved2, &d.disp2_bits[1 + pass]);
 }
 
 // Per-particle forms: every particle (listed == null), or only the particles
@@ -771,7 +782,7 @@ __global__ void __launch_bounds__(kPairBlock) k_shift_gradient_each(const __grid
     for (int i = blk * blockDim.x + threadIdx.x; i < nf; i += nblk * blockDim.x)
         if (!only_unlisted || d.f_listed[i] != stamp)
             moved2 = max(moved2, shift_update_particle<F>(p, d, i, shift_particle<F>(p, d, src, i, Frame{0, 0})));
-    if (pass < kMaskShifts) block_max_to<kPairBlock>(moved2, &d.disp2_bits[1 + pass]);
+    if (pass < kMaskShifts) warp_max_to(moved2, &d.disp2_bits[1 + pass]);
 }
 
 // densityToPressure, fluid.cu:15-23
