@@ -356,7 +356,7 @@ def run_ours(args):
                 "traffic": byte_model.measured_traffic_per_launch(dom, nf, mixed) if args.tile_h == 16 and not args.untiled
                 else None,
                 "traffic_source": "ncu dram bytes of one launch at 2.08M particles, scaled by particle count "
-                                  "(profiles/k_fluid_pair_k_shift_gradient_2M_plain.md)",
+                                  "(profiles/k_fluid_pair_tiled_k_shift_gradient_tiled_dam_break_gas_2M.md)",
                 "peak_source": "MEASURED_PEAKS.json hbm_gbs (measured)" if peaks else "fallback 6.8 TB/s",
                 "bytes_per_launch": bpl, "avg_launch_ms": avg_ms,
                 "stage_share": {k: round(v[0] / total_ms, 4) for k, v in prof.items() if v[1]}}
