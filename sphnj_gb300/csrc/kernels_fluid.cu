@@ -111,20 +111,54 @@ struct FAcc {
     int near;
 };
 
+// 1 / x and 1 / sqrt(x) by the SFU (PTX rcp.approx.ftz.f32, rsqrt.approx.ftz.f32)
+__device__ __forceinline__ float rcp_approx(float x) {
+    float y;
+    asm("rcp.approx.ftz.f32 %0, %1;" : "=f"(y) : "f"(x));
+    return y;
+}
+__device__ __forceinline__ float rsqrt_approx(float x) {
+    float y;
+    asm("rsqrt.approx.ftz.f32 %0, %1;" : "=f"(y) : "f"(x));
+    return y;
+}
+
 // Riemann pair term shared by fluid, solid and virtual neighbours
-// (fluid.cu:48-58, 115-124, 167-177).
+// (fluid.cu:48-58, 115-124, 167-177).  The plain form divides as the
+// reference's fast-math build does, one approximate division per '/'.  The
+// mixed form takes one SFU reciprocal of rho_i + rho_j for the five divisions
+// by it, reciprocals of rho_i and c_s (loop-invariant), and the direction
+// from an SFU reciprocal square root: the same expressions with fewer
+// roundings' worth of SFU work.
+template <class F>
 __device__ __forceinline__ void riemann(float2 u_i, float2 u_j, float p_i, float p_j, float rho_i, float rho_j,
                                         float cs, float2 dx, float kc, FAcc &a) {
     const float rs = rho_i + rho_j;
-    float ps = fdiv(sum2(rho_i, p_j, rho_j, p_i), rs);
-    float2 n = nrm_fast(dx);
-    float du = dot2(sub2(u_i, u_j), n);
-    if (du >= 0.0f) ps += fdiv(rho_i * rho_j * du, rs) * fminf(3.0f * du, cs);
-    float2 vs = make_float2(fdiv(sum2(rho_i, u_i.x, rho_j, u_j.x), rs), fdiv(sum2(rho_i, u_i.y, rho_j, u_j.y), rs));
-    float t = fdiv(fdiv(p_i - p_j, rs), cs);
-    vs.x += t * n.x;
-    vs.y += t * n.y;
-    float am = fdiv(-2.0f * ps, rho_i);
+    float ps, am, t;
+    float2 n, vs;
+    if constexpr (F::kMixed) {
+        const float irs = rcp_approx(rs);
+        ps = sum2(rho_i, p_j, rho_j, p_i) * irs;
+        const float z = sqn(dx);
+        n = z > 0.0f ? make_float2(dx.x * rsqrt_approx(z), dx.y * rsqrt_approx(z)) : dx;
+        const float du = dot2(sub2(u_i, u_j), n);
+        if (du >= 0.0f) ps += rho_i * rho_j * du * irs * fminf(3.0f * du, cs);
+        vs = make_float2(sum2(rho_i, u_i.x, rho_j, u_j.x) * irs, sum2(rho_i, u_i.y, rho_j, u_j.y) * irs);
+        t = (p_i - p_j) * irs * rcp_approx(cs);
+        vs.x += t * n.x;
+        vs.y += t * n.y;
+        am = -2.0f * ps * rcp_approx(rho_i);
+    } else {
+        ps = fdiv(sum2(rho_i, p_j, rho_j, p_i), rs);
+        n = nrm_fast(dx);
+        const float du = dot2(sub2(u_i, u_j), n);
+        if (du >= 0.0f) ps += fdiv(rho_i * rho_j * du, rs) * fminf(3.0f * du, cs);
+        vs = make_float2(fdiv(sum2(rho_i, u_i.x, rho_j, u_j.x), rs), fdiv(sum2(rho_i, u_i.y, rho_j, u_j.y), rs));
+        t = fdiv(fdiv(p_i - p_j, rs), cs);
+        vs.x += t * n.x;
+        vs.y += t * n.y;
+        am = fdiv(-2.0f * ps, rho_i);
+    }
     a.du_dt.x += am * dx.x * kc;
     a.du_dt.y += am * dx.y * kc;
     a.velo_div += 2.0f * rho_i * dot2(sub2(u_i, vs), dx) * kc;
@@ -135,11 +169,18 @@ __device__ __forceinline__ void riemann(float2 u_i, float2 u_j, float p_i, float
     a.du_dx.w += w.y * dx.y * kc;
 }
 
+template <class F>
 __device__ __forceinline__ void viscous(const sphnj_params &p, float2 u_i, float2 u_j, float rho_i, int ph_i,
                                         float2 dx, float kc, FAcc &a) {
     float vis = dot2(sub2(u_j, u_i), dx);
-    vis = fdiv(vis, sqn(dx) + 0.01f * p.smoothing_length_square);
-    float am = fdiv(8.0f * by_phase(p.viscosity, ph_i) * vis, rho_i);
+    float am;
+    if constexpr (F::kMixed) {
+        vis *= rcp_approx(sqn(dx) + 0.01f * p.smoothing_length_square);
+        am = 8.0f * by_phase(p.viscosity, ph_i) * vis * rcp_approx(rho_i);
+    } else {
+        vis = fdiv(vis, sqn(dx) + 0.01f * p.smoothing_length_square);
+        am = fdiv(8.0f * by_phase(p.viscosity, ph_i) * vis, rho_i);
+    }
     a.du_dt.x += am * dx.x * kc;
     a.du_dt.y += am * dx.y * kc;
 }
@@ -179,7 +220,7 @@ __device__ __forceinline__ void fluid_term(const sphnj_params &p, const Src &src
     const float R2 = p.impact_distance_square;
     const float kc = F::gw(p, sqn(dx));
     const float2 u_j = src.u(k);
-    riemann(s.u, u_j, s.p, src.pr(k), s.rho, src.rho(k), s.cs, dx, kc, a);
+    riemann<F>(s.u, u_j, s.p, src.pr(k), s.rho, src.rho(k), s.cs, dx, kc, a);
     const int ph_j = src.phase(k);
     if (!(s.ph == SPHNJ_LIQUID && ph_j == SPHNJ_GAS)) {
         a.color += dot2(dx, dx) * kc;
@@ -190,7 +231,7 @@ __device__ __forceinline__ void fluid_term(const sphnj_params &p, const Src &src
         if (sqn(dx) < 0.25f * R2) a.near = SPHNJ_HAS_NEAR_PARTICLE;
         else if (a.near == SPHNJ_NO_PARTICLE) a.near = SPHNJ_HAS_PARTICLE;
     }
-    if (p.is_fluid_viscid) viscous(p, s.u, u_j, s.rho, s.ph, dx, kc, a);
+    if (p.is_fluid_viscid) viscous<F>(p, s.u, u_j, s.rho, s.ph, dx, kc, a);
 }
 
 __device__ __forceinline__ void store_pair(const DevState &d, int i, const FAcc &a) {
@@ -234,10 +275,10 @@ __device__ __forceinline__ void pair_particle(const sphnj_params &p, const DevSt
             if (!(sqn(dx) < R2)) continue;
             const float kc = F::gw(p, sqn(dx));
             const float2 u_j = F::s_vel(d, j);
-            riemann(u_i, u_j, p_i, __ldg(&d.s_p[j]), rho_i, rho_i, cs, dx, kc, a);
+            riemann<F>(u_i, u_j, p_i, __ldg(&d.s_p[j]), rho_i, rho_i, cs, dx, kc, a);
             a.grad.x += dx.x * kc;
             a.grad.y += dx.y * kc;
-            if (viscid) viscous(p, u_i, u_j, rho_i, ph_i, dx, kc, a);
+            if (viscid) viscous<F>(p, u_i, u_j, rho_i, ph_i, dx, kc, a);
         }
         const int2 rv = __ldg(&d.rng_v[m]);
         for (int t = rv.x; t < rv.x + rv.y; ++t) {
@@ -247,7 +288,7 @@ __device__ __forceinline__ void pair_particle(const sphnj_params &p, const DevSt
             const float kc = F::gw(p, sqn(dx));
             const float rho_j = by_phase(p.reference_density, __ldg(&d.v_phase[j]));
             const float2 u_j = __ldg(&d.v_vel[j]);
-            riemann(u_i, u_j, p_i, __ldg(&d.v_p[j]), rho_i, rho_j, cs, dx, kc, a);
+            riemann<F>(u_i, u_j, p_i, __ldg(&d.v_p[j]), rho_i, rho_j, cs, dx, kc, a);
             // fluid.cu:179 reads the fluid phase array with the virtual
             // index; past the fluid count it is taken as LIQUID.
             const int ph_j = j < nf ? (int)__ldg(&d.f_phase[j]) : SPHNJ_LIQUID;
@@ -256,7 +297,7 @@ __device__ __forceinline__ void pair_particle(const sphnj_params &p, const DevSt
                 a.grad.x += dx.x * kc;
                 a.grad.y += dx.y * kc;
             }
-            if (viscid) viscous(p, u_i, u_j, rho_i, ph_i, dx, kc, a);
+            if (viscid) viscous<F>(p, u_i, u_j, rho_i, ph_i, dx, kc, a);
         }
     }
     store_pair(d, i, a);
