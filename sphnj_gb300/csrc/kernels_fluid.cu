@@ -50,10 +50,19 @@ constexpr int kBlock = 256;
 constexpr int kFallbackBlocks = 304;  // 2 x 152 SMs, grid-stride
 
 __device__ __forceinline__ float fdiv(float a, float b) { return __fdividef(a, b); }
+// sqrt by the SFU (PTX sqrt.approx.ftz.f32), the square root sqrtf becomes
+// in the reference's -use_fast_math build
+__device__ __forceinline__ float sqrt_approx(float x) {
+    float y;
+    asm("sqrt.approx.ftz.f32 %0, %1;" : "=f"(y) : "f"(x));
+    return y;
+}
+// Eigen's normalized() (x / sqrt(|x|^2), zero vector unchanged) as the
+// reference's fast-math build evaluates it in the pair terms
 __device__ __forceinline__ float2 nrm_fast(float2 a) {
     float z = sqn(a);
     if (z > 0.0f) {
-        float s = sqrtf(z);
+        float s = sqrt_approx(z);
         return make_float2(fdiv(a.x, s), fdiv(a.y, s));
     }
     return a;
