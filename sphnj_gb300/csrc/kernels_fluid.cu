@@ -30,10 +30,11 @@
 // the last sort) are handled by per-particle fallback kernels, which return
 // at once when every particle is listed.
 //
-// Math: the neighbour sweeps use __expf and __fdividef, the approximations
-// that the reference's -use_fast_math build uses for expf and '/'
-// (CMakeLists.txt:16-19); the equation of state keeps powf, whose fast form
-// loses ~1e-4 relative pressure accuracy near the reference density.
+// Math: the neighbour sweeps use __expf, __fdividef and sqrt.approx, the
+// approximations that the reference's -use_fast_math build uses for expf,
+// '/' and sqrtf (CMakeLists.txt:16-19); the equation of state keeps powf,
+// whose fast form loses ~1e-4 relative pressure accuracy near the reference
+// density.  The mixed form's pair term uses SFU reciprocals (riemann).
 #include "forms.cuh"
 #include "kernels.h"
 
@@ -137,8 +138,8 @@ __device__ __forceinline__ float rsqrt_approx(float x) {
 // reference's fast-math build does, one approximate division per '/'.  The
 // mixed form takes one SFU reciprocal of rho_i + rho_j for the five divisions
 // by it, reciprocals of rho_i and c_s (loop-invariant), and the direction
-// from an SFU reciprocal square root: the same expressions with fewer
-// roundings' worth of SFU work.
+// from an SFU reciprocal square root: the same expressions with fewer SFU
+// operations.
 template <class F>
 __device__ __forceinline__ void riemann(float2 u_i, float2 u_j, float p_i, float p_j, float rho_i, float rho_j,
                                         float cs, float2 dx, float kc, FAcc &a) {
