@@ -61,6 +61,10 @@ struct Frame {
 struct FormPlain {
     static constexpr bool kMixed = false;
     __device__ static __forceinline__ float gw(const sphnj_params &p, float r2) { return gw_plain(p, r2); }
+    // shifting gradient: the reference's per-pair weight, no factor after the sum
+    static constexpr bool kShiftScaled = false;
+    __device__ static __forceinline__ float gw_shift(const sphnj_params &p, float r2) { return gw_plain(p, r2); }
+    __device__ static __forceinline__ float shift_scale(const sphnj_params &) { return 1.0f; }
     // frame shift of neighbour slot n (0..8) of the home cell
     __device__ static __forceinline__ float2 shift(const sphnj_params &, Frame, int) { return make_float2(0.f, 0.f); }
     __device__ static __forceinline__ float2 f_home(const sphnj_params &, const DevState &d, Frame, int i) {
@@ -81,6 +85,15 @@ struct FormPlain {
 struct FormMixed {
     static constexpr bool kMixed = true;
     __device__ static __forceinline__ float gw(const sphnj_params &p, float r2) { return gw_folded(p, r2); }
+    // shifting gradient: sum dx 2^(r^2 a) per pair, times b = Kd C32 once
+    // for the finished sum (one multiply per pair fewer)
+    static constexpr bool kShiftScaled = true;
+    __device__ static __forceinline__ float gw_shift(const sphnj_params &p, float r2) {
+        return ex2_approx(r2 * (-1.4426950408889634f * p.smoothing_length_inverse_square));
+    }
+    __device__ static __forceinline__ float shift_scale(const sphnj_params &p) {
+        return p.kernel_differential * p.coefficient_3d_to_2d;
+    }
     __device__ static __forceinline__ float2 shift(const sphnj_params &p, Frame f, int n) {
         return cells_to_len(p, f.dx + n / 3 - 1, f.dy + n % 3 - 1);
     }

@@ -330,7 +330,7 @@ __device__ __forceinline__ float2 shift_particle(const sphnj_params &p, const De
         for (int t = rf.x; t < rf.x + rf.y; ++t) {
             const float2 dx = sub2(src.x(src.key(t), sh), x_i);
             if (sqn(dx) < R2) {
-                const float kc = F::gw(p, sqn(dx));
+                const float kc = F::gw_shift(p, sqn(dx));
                 g.x += dx.x * kc;
                 g.y += dx.y * kc;
             }
@@ -339,7 +339,7 @@ __device__ __forceinline__ float2 shift_particle(const sphnj_params &p, const De
         for (int t = rs.x; t < rs.x + rs.y; ++t) {
             const float2 dx = sub2(F::s_nbr(d, __ldg(&d.lst_s[t]), sh), x_i);
             if (sqn(dx) < R2) {
-                const float kc = F::gw(p, sqn(dx));
+                const float kc = F::gw_shift(p, sqn(dx));
                 g.x += dx.x * kc;
                 g.y += dx.y * kc;
             }
@@ -348,12 +348,13 @@ __device__ __forceinline__ float2 shift_particle(const sphnj_params &p, const De
         for (int t = rv.x; t < rv.x + rv.y; ++t) {
             const float2 dx = sub2(F::v_nbr(d, __ldg(&d.lst_v[t]), sh), x_i);
             if (sqn(dx) < R2) {
-                const float kc = F::gw(p, sqn(dx));
+                const float kc = F::gw_shift(p, sqn(dx));
                 g.x += dx.x * kc;
                 g.y += dx.y * kc;
             }
         }
     }
+    if constexpr (F::kShiftScaled) g = make_float2(g.x * F::shift_scale(p), g.y * F::shift_scale(p));
     return g;
 }
 
@@ -494,7 +495,7 @@ __device__ __forceinline__ float2 shift_particle_listed(const sphnj_params &p, c
             if (e < m) {
                 const float2 dx = sub2(x_j[e], x_i);
                 if (sqn(dx) < R2) {
-                    const float kc = F::gw(p, sqn(dx));
+                    const float kc = F::gw_shift(p, sqn(dx));
                     g.x += dx.x * kc;
                     g.y += dx.y * kc;
                 }
@@ -510,6 +511,7 @@ __device__ __forceinline__ float2 shift_particle_listed(const sphnj_params &p, c
         chunk(v, 8);
     }
     if (n & 7) chunk(next, n & 7);
+    if constexpr (F::kShiftScaled) g = make_float2(g.x * F::shift_scale(p), g.y * F::shift_scale(p));
     return g;
 }
 
