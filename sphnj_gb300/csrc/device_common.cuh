@@ -78,8 +78,8 @@ struct DevState {
     // max |displacement|^2 (float bits) of each position update since the
     // pair pass: [0] fluid update, [1 + k] shifting pass k
     unsigned int *disp2_bits;
-    // tiles of the neighbour sweeps that hold fluid this step (any order) and
-    // their number; reset by binning, filled after the cell lists are built
+    // tiles of the neighbour sweeps that hold fluid this step (in tile order)
+    // and their number; reset by binning, filled after the cell lists are built
     int *tile_list, *tile_count;
     // scalars
     unsigned int *max_speed2_bits;  // max over fluid of |v|^2 (float bits)
