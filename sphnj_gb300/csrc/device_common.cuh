@@ -232,12 +232,17 @@ struct One {
 
 // Many: one launch over many scenes.  Scene k owns the blocks
 // first[k] <= b < first[k + 1]; first[n] is the grid size, and a scene with
-// no work for this launch owns no block.
+// no work for this launch owns no block.  The block copies its scene's record
+// into shared memory, so that the kernel reads its fields with shared loads
+// at fixed addresses (as a one-scene launch reads them from parameter space)
+// rather than holding global addresses in registers.
 struct Many {
     const Scene *scenes;
     const int *first;  // [n + 1]
     int n;
     __device__ __forceinline__ const Scene *locate(int &blk, int &nblk) const {
+        __shared__ __align__(16) Scene s_scene;
+        static_assert(sizeof(Scene) % 16 == 0, "the record is copied in 16-byte words");
         const int b = blockIdx.x;
         int lo = 0, hi = n;  // first[lo] <= b < first[hi]
         while (hi - lo > 1) {
@@ -248,7 +253,11 @@ struct Many {
         const int f0 = __ldg(&first[lo]);
         blk = b - f0;
         nblk = __ldg(&first[lo + 1]) - f0;
-        return scenes + lo;
+        const int4 *src = reinterpret_cast<const int4 *>(scenes + lo);
+        int4 *dst = reinterpret_cast<int4 *>(&s_scene);
+        for (int w = threadIdx.x; w < (int)(sizeof(Scene) / 16); w += blockDim.x) dst[w] = __ldg(&src[w]);
+        __syncthreads();
+        return &s_scene;
     }
 };
 
