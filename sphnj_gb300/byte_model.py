@@ -84,13 +84,13 @@ def bytes_per_step(nf: int, ns: int, nv: int, shifts: int, substeps: int) -> flo
 # the compulsory bytes above: the pair pass writes the per-step neighbour lists
 # and every shifting pass reads them back.
 MEASURED_TRAFFIC_PER_PARTICLE = {
-    "fluid_pair": 146.3,
-    "shift_pass": 157.0,
+    "fluid_pair": 146.6,
+    "shift_pass": 156.4,
 }
 # the same capture of the mixed form
 MEASURED_TRAFFIC_PER_PARTICLE_MIXED = {
-    "fluid_pair": 148.1,
-    "shift_pass": 188.0,
+    "fluid_pair": 148.0,
+    "shift_pass": 186.8,
 }
 
 
