@@ -47,6 +47,7 @@ namespace {
 
 constexpr int kPairBlock = 128;
 constexpr int kTileBlock = 256;  // tiled sweeps: ~208 particles per 16-cell tile
+constexpr int kListBlock = 128;  // shifting passes over an active-tile list
 constexpr int kBlock = 256;
 constexpr int kFallbackBlocks = 304;  // 2 x 152 SMs, grid-stride
 
@@ -759,11 +760,15 @@ __global__ void __launch_bounds__(kTileBlock, 5) k_fluid_pair_tiled(const __grid
 
 // One shifting pass over the listed particles: each home particle's gradient,
 // then its position update (shift_update_particle) by the same thread.
-template <class G, class F, bool kList>
-// 8 blocks per SM (32 registers, a 28-byte spill): full occupancy measured
-// 4% faster than 40 registers at 6 blocks
-__global__ void __launch_bounds__(kTileBlock, 8) k_shift_gradient_tiled(const __grid_constant__ G gs, int tile_h, int cap,
-                                                                     int pass) {
+// kThreads per block at full occupancy, 32 registers (a small spill): 32
+// registers at 8 blocks of 256 measured 4% faster than 40 at 6.  Batched
+// launches over the active-tile lists use blocks of kListBlock threads: their
+// tiles are often partly filled, and a smaller block leaves fewer warps
+// waiting at the tile's barriers while the others work (256-scene mixed
+// sweep: 4.81 -> 4.52 ms/step).
+template <class G, class F, bool kList, int kThreads>
+__global__ void __launch_bounds__(kThreads, 2048 / kThreads)
+    k_shift_gradient_tiled(const __grid_constant__ G gs, int tile_h, int cap, int pass) {
     SPHNJ_SCENE(gs);
     extern __shared__ __align__(16) unsigned char smem[];
     __shared__ int s_base[3], s_off[3];
@@ -1025,9 +1030,19 @@ template <class F, class G> int shift_pass(cudaStream_t st, G &g, const TileConf
     auto blocks = [&](const Scene &s) { return active(s) ? sweep_blocks(s.p, tc.tile_h) : 0u; };
     const long long key = site_key(SITE_SHIFT_TILED, (tc.tile_h << 8) | pass);
     const size_t smem = cap * sizeof(float2);
+    // batched list launches: blocks of kListBlock threads, kTileBlock / kListBlock
+    // times as many (a sparse scene swept alone, one short launch, keeps the
+    // larger blocks: measured 116 against 132 ms/step on the sweep's scenes
+    // stepped one by one)
+    constexpr int kT = std::is_same<G, GroupMany>::value ? kListBlock : kTileBlock;
+    auto list_blocks = [&](const Scene &s) {
+        return active(s) ? std::min<unsigned>(tile_blocks(s.p, tc.tile_h), sweep_blocks(s.p, tc.tile_h) * (kTileBlock / kT))
+                         : 0u;
+    };
     int n = use_tile_list(g, tc.tile_h)
-                ? launch(g, key, blocks, k_shift_gradient_tiled<D, F, true>, kTileBlock, smem, st, tc.tile_h, cap, pass)
-                : launch(g, key, blocks, k_shift_gradient_tiled<D, F, false>, kTileBlock, smem, st, tc.tile_h, cap, pass);
+                ? launch(g, key, list_blocks, k_shift_gradient_tiled<D, F, true, kT>, kT, smem, st, tc.tile_h, cap, pass)
+                : launch(g, key, blocks, k_shift_gradient_tiled<D, F, false, kTileBlock>, kTileBlock, smem, st,
+                         tc.tile_h, cap, pass);
     n += launch(
         g, site_key(SITE_SHIFT_FALLBACK, pass),
         [&](const Scene &s) { return active(s) ? fallback_blocks(s.p.fluid_number_total) : 0u; },
