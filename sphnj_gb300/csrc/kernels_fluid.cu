@@ -134,6 +134,21 @@ __device__ __forceinline__ float rsqrt_approx(float x) {
     return y;
 }
 
+// Products and accumulations of the pair and shifting terms.  The mixed form
+// writes them with round-to-nearest intrinsics - a += x y as one explicit
+// FMA, products rounded one by one - so that every kernel that inlines them
+// (one-scene and batched launches, which have different block shapes and
+// register budgets) rounds them the same way; the plain form leaves
+// contraction to the compiler, as the reference's build does.
+template <class F> __device__ __forceinline__ float mul2(float x, float y) {
+    if constexpr (F::kMixed) return __fmul_rn(x, y);
+    else return x * y;
+}
+template <class F> __device__ __forceinline__ void mad_to(float &a, float x, float y) {
+    if constexpr (F::kMixed) a = __fmaf_rn(x, y, a);
+    else a += x * y;
+}
+
 // Riemann pair term shared by fluid, solid and virtual neighbours
 // (fluid.cu:48-58, 115-124, 167-177).  The plain form divides as the
 // reference's fast-math build does, one approximate division per '/'.  The
@@ -149,16 +164,20 @@ __device__ __forceinline__ void riemann(float2 u_i, float2 u_j, float p_i, float
     float2 n, vs;
     if constexpr (F::kMixed) {
         const float irs = rcp_approx(rs);
-        ps = sum2(rho_i, p_j, rho_j, p_i) * irs;
+        ps = __fmul_rn(sum2(rho_i, p_j, rho_j, p_i), irs);
         const float z = sqn(dx);
-        n = z > 0.0f ? make_float2(dx.x * rsqrt_approx(z), dx.y * rsqrt_approx(z)) : dx;
+        const float iz = rsqrt_approx(z);
+        n = z > 0.0f ? make_float2(__fmul_rn(dx.x, iz), __fmul_rn(dx.y, iz)) : dx;
         const float du = dot2(sub2(u_i, u_j), n);
-        if (du >= 0.0f) ps += rho_i * rho_j * du * irs * fminf(3.0f * du, cs);
-        vs = make_float2(sum2(rho_i, u_i.x, rho_j, u_j.x) * irs, sum2(rho_i, u_i.y, rho_j, u_j.y) * irs);
-        t = (p_i - p_j) * irs * rcp_approx(cs);
-        vs.x += t * n.x;
-        vs.y += t * n.y;
-        am = -2.0f * ps * rcp_approx(rho_i);
+        if (du >= 0.0f)
+            ps = __fadd_rn(ps, __fmul_rn(__fmul_rn(__fmul_rn(__fmul_rn(rho_i, rho_j), du), irs),
+                                         fminf(__fmul_rn(3.0f, du), cs)));
+        vs = make_float2(__fmul_rn(sum2(rho_i, u_i.x, rho_j, u_j.x), irs),
+                         __fmul_rn(sum2(rho_i, u_i.y, rho_j, u_j.y), irs));
+        t = __fmul_rn(__fmul_rn(__fsub_rn(p_i, p_j), irs), rcp_approx(cs));
+        vs.x = __fmaf_rn(t, n.x, vs.x);
+        vs.y = __fmaf_rn(t, n.y, vs.y);
+        am = __fmul_rn(__fmul_rn(-2.0f, ps), rcp_approx(rho_i));
     } else {
         ps = fdiv(sum2(rho_i, p_j, rho_j, p_i), rs);
         n = nrm_fast(dx);
@@ -170,14 +189,14 @@ __device__ __forceinline__ void riemann(float2 u_i, float2 u_j, float p_i, float
         vs.y += t * n.y;
         am = fdiv(-2.0f * ps, rho_i);
     }
-    a.du_dt.x += am * dx.x * kc;
-    a.du_dt.y += am * dx.y * kc;
-    a.velo_div += 2.0f * rho_i * dot2(sub2(u_i, vs), dx) * kc;
+    mad_to<F>(a.du_dt.x, mul2<F>(am, dx.x), kc);
+    mad_to<F>(a.du_dt.y, mul2<F>(am, dx.y), kc);
+    mad_to<F>(a.velo_div, mul2<F>(mul2<F>(2.0f, rho_i), dot2(sub2(u_i, vs), dx)), kc);
     float2 w = sub2(u_j, u_i);
-    a.du_dx.x += w.x * dx.x * kc;
-    a.du_dx.y += w.y * dx.x * kc;
-    a.du_dx.z += w.x * dx.y * kc;
-    a.du_dx.w += w.y * dx.y * kc;
+    mad_to<F>(a.du_dx.x, mul2<F>(w.x, dx.x), kc);
+    mad_to<F>(a.du_dx.y, mul2<F>(w.y, dx.x), kc);
+    mad_to<F>(a.du_dx.z, mul2<F>(w.x, dx.y), kc);
+    mad_to<F>(a.du_dx.w, mul2<F>(w.y, dx.y), kc);
 }
 
 template <class F>
@@ -186,14 +205,14 @@ __device__ __forceinline__ void viscous(const sphnj_params &p, float2 u_i, float
     float vis = dot2(sub2(u_j, u_i), dx);
     float am;
     if constexpr (F::kMixed) {
-        vis *= rcp_approx(sqn(dx) + 0.01f * p.smoothing_length_square);
-        am = 8.0f * by_phase(p.viscosity, ph_i) * vis * rcp_approx(rho_i);
+        vis = __fmul_rn(vis, rcp_approx(__fmaf_rn(0.01f, p.smoothing_length_square, sqn(dx))));
+        am = __fmul_rn(__fmul_rn(__fmul_rn(8.0f, by_phase(p.viscosity, ph_i)), vis), rcp_approx(rho_i));
     } else {
         vis = fdiv(vis, sqn(dx) + 0.01f * p.smoothing_length_square);
         am = fdiv(8.0f * by_phase(p.viscosity, ph_i) * vis, rho_i);
     }
-    a.du_dt.x += am * dx.x * kc;
-    a.du_dt.y += am * dx.y * kc;
+    mad_to<F>(a.du_dt.x, mul2<F>(am, dx.x), kc);
+    mad_to<F>(a.du_dt.y, mul2<F>(am, dx.y), kc);
 }
 
 // State of particle i that every pair term reads.
@@ -234,9 +253,9 @@ __device__ __forceinline__ void fluid_term(const sphnj_params &p, const Src &src
     riemann<F>(s.u, u_j, s.p, src.pr(k), s.rho, src.rho(k), s.cs, dx, kc, a);
     const int ph_j = src.phase(k);
     if (!(s.ph == SPHNJ_LIQUID && ph_j == SPHNJ_GAS)) {
-        a.color += dot2(dx, dx) * kc;
-        a.grad.x += dx.x * kc;
-        a.grad.y += dx.y * kc;
+        mad_to<F>(a.color, dot2(dx, dx), kc);
+        mad_to<F>(a.grad.x, dx.x, kc);
+        mad_to<F>(a.grad.y, dx.y, kc);
     }
     if (src.fbt(k) == SPHNJ_FREE_SURFACE && s.ph == SPHNJ_LIQUID && s.i != src.pid(k)) {
         if (sqn(dx) < 0.25f * R2) a.near = SPHNJ_HAS_NEAR_PARTICLE;
@@ -287,8 +306,8 @@ __device__ __forceinline__ void pair_particle(const sphnj_params &p, const DevSt
             const float kc = F::gw(p, sqn(dx));
             const float2 u_j = F::s_vel(d, j);
             riemann<F>(u_i, u_j, p_i, __ldg(&d.s_p[j]), rho_i, rho_i, cs, dx, kc, a);
-            a.grad.x += dx.x * kc;
-            a.grad.y += dx.y * kc;
+            mad_to<F>(a.grad.x, dx.x, kc);
+            mad_to<F>(a.grad.y, dx.y, kc);
             if (viscid) viscous<F>(p, u_i, u_j, rho_i, ph_i, dx, kc, a);
         }
         const int2 rv = __ldg(&d.rng_v[m]);
@@ -304,9 +323,9 @@ __device__ __forceinline__ void pair_particle(const sphnj_params &p, const DevSt
             // index; past the fluid count it is taken as LIQUID.
             const int ph_j = j < nf ? (int)__ldg(&d.f_phase[j]) : SPHNJ_LIQUID;
             if (!(ph_i == SPHNJ_LIQUID && ph_j == SPHNJ_GAS)) {
-                a.color += dot2(dx, dx) * kc;
-                a.grad.x += dx.x * kc;
-                a.grad.y += dx.y * kc;
+                mad_to<F>(a.color, dot2(dx, dx), kc);
+                mad_to<F>(a.grad.x, dx.x, kc);
+                mad_to<F>(a.grad.y, dx.y, kc);
             }
             if (viscid) viscous<F>(p, u_i, u_j, rho_i, ph_i, dx, kc, a);
         }
@@ -332,8 +351,8 @@ __device__ __forceinline__ float2 shift_particle(const sphnj_params &p, const De
             const float2 dx = sub2(src.x(src.key(t), sh), x_i);
             if (sqn(dx) < R2) {
                 const float kc = F::gw_shift(p, sqn(dx));
-                g.x += dx.x * kc;
-                g.y += dx.y * kc;
+                mad_to<F>(g.x, dx.x, kc);
+                mad_to<F>(g.y, dx.y, kc);
             }
         }
         const int2 rs = __ldg(&d.rng_s[m]);
@@ -341,8 +360,8 @@ __device__ __forceinline__ float2 shift_particle(const sphnj_params &p, const De
             const float2 dx = sub2(F::s_nbr(d, __ldg(&d.lst_s[t]), sh), x_i);
             if (sqn(dx) < R2) {
                 const float kc = F::gw_shift(p, sqn(dx));
-                g.x += dx.x * kc;
-                g.y += dx.y * kc;
+                mad_to<F>(g.x, dx.x, kc);
+                mad_to<F>(g.y, dx.y, kc);
             }
         }
         const int2 rv = __ldg(&d.rng_v[m]);
@@ -350,8 +369,8 @@ __device__ __forceinline__ float2 shift_particle(const sphnj_params &p, const De
             const float2 dx = sub2(F::v_nbr(d, __ldg(&d.lst_v[t]), sh), x_i);
             if (sqn(dx) < R2) {
                 const float kc = F::gw_shift(p, sqn(dx));
-                g.x += dx.x * kc;
-                g.y += dx.y * kc;
+                mad_to<F>(g.x, dx.x, kc);
+                mad_to<F>(g.y, dx.y, kc);
             }
         }
     }
@@ -497,8 +516,8 @@ __device__ __forceinline__ float2 shift_particle_listed(const sphnj_params &p, c
                 const float2 dx = sub2(x_j[e], x_i);
                 if (sqn(dx) < R2) {
                     const float kc = F::gw_shift(p, sqn(dx));
-                    g.x += dx.x * kc;
-                    g.y += dx.y * kc;
+                    mad_to<F>(g.x, dx.x, kc);
+                    mad_to<F>(g.y, dx.y, kc);
                 }
             }
         }
@@ -561,11 +580,18 @@ __device__ __forceinline__ unsigned int disp2(float2 a, float2 b) {
 
 // (I - n n^T) d with n = normalize(g), zeroed below EPS_FOR_SUM
 // (fluid.cu:394-397)
-__device__ __forceinline__ float2 project(float2 g, float2 disp) {
+// (the mixed form with round-to-nearest intrinsics, as mad_to)
+template <class F> __device__ __forceinline__ float2 project(float2 g, float2 disp) {
     float2 n = normalized(g);
     if (sqrtf(sqn(n)) < EPS_FOR_SUM) n = make_float2(0.f, 0.f);
-    float m00 = 1.0f - n.x * n.x, m10 = 0.0f - n.y * n.x, m01 = 0.0f - n.x * n.y, m11 = 1.0f - n.y * n.y;
-    return make_float2(m00 * disp.x + m01 * disp.y, m10 * disp.x + m11 * disp.y);
+    if constexpr (F::kMixed) {
+        const float m00 = __fsub_rn(1.0f, __fmul_rn(n.x, n.x)), m10 = -__fmul_rn(n.y, n.x),
+                    m01 = -__fmul_rn(n.x, n.y), m11 = __fsub_rn(1.0f, __fmul_rn(n.y, n.y));
+        return make_float2(sum2(m00, disp.x, m01, disp.y), sum2(m10, disp.x, m11, disp.y));
+    } else {
+        float m00 = 1.0f - n.x * n.x, m10 = 0.0f - n.y * n.x, m01 = 0.0f - n.x * n.y, m11 = 1.0f - n.y * n.y;
+        return make_float2(m00 * disp.x + m01 * disp.y, m10 * disp.x + m11 * disp.y);
+    }
 }
 
 // shiftDisplacementCalculate + correctionUpdate (fluid.cu:369-427) for
@@ -599,11 +625,11 @@ __device__ __forceinline__ unsigned int shift_update_particle(const sphnj_params
             dd = make_float2(0.f, 0.f);
         } else {
             bt = SPHNJ_FREE_SURFACE;
-            dd = project(g, disp);
+            dd = project<F>(g, disp);
         }
     } else if (color < 2.0f && near == SPHNJ_HAS_NEAR_PARTICLE) {
         bt = SPHNJ_VICINITY;
-        dd = project(g, disp);
+        dd = project<F>(g, disp);
     } else {
         bt = SPHNJ_INNER;
         dd = disp;
@@ -615,7 +641,7 @@ __device__ __forceinline__ unsigned int shift_update_particle(const sphnj_params
         float2 x = d.f_off[i], xc = d.f_offc[i], v = d.f_vel[i], vc = d.f_velc[i];
         const float2 x0 = x;
         kahan_add2(x, xc, sh);
-        kahan_add2(v, vc, make_float2(m.x * sh.x + m.z * sh.y, m.y * sh.x + m.w * sh.y));
+        kahan_add2(v, vc, make_float2(sum2(m.x, sh.x, m.z, sh.y), sum2(m.y, sh.x, m.w, sh.y)));
         d.f_x_alt[i] = x;
         d.f_offc[i] = xc;
         d.f_vel[i] = v;
