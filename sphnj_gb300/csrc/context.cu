@@ -603,7 +603,8 @@ int sphnj_upload_fields(sphnj_ctx *ctx, uint32_t mask, const sphnj_host_state *s
         if ((mask & SPHNJ_F_SOLID_KINEMATICS) &&
             (s->solid_position || s->solid_reference_position || s->solid_velocity))
             resplit |= 2;
-        launch_mixed_join(ctx->st, GroupOne{scene_of(ctx, ctx->parity), ctx->form});
+        // (a re-split fluid reads only the positions it is given)
+        launch_mixed_join(ctx->st, GroupOne{scene_of(ctx, ctx->parity), ctx->form}, resplit & 2);
         if ((mask & SPHNJ_F_FLUID_KINEMATICS) && s->fluid_velocity && !s->fluid_position)
             CK(cudaMemsetAsync(d.f_velc, 0, sizeof(float2) * (size_t)nf, ctx->st));
     }
@@ -766,9 +767,10 @@ int sphnj_download(sphnj_ctx *ctx, uint32_t mask, sphnj_host_state *s) {
     const int nf = p.fluid_number_total, ns = p.solid_number, nv = p.virt_number;
     const DevState &d = ctx->d;
     // mixed form: absolute positions and FP64 solid kinematics from the state
-    if (ctx->form == SPHNJ_FORM_MIXED && (mask & (SPHNJ_F_FLUID_KINEMATICS | SPHNJ_F_SOLID_KINEMATICS |
-                                                  SPHNJ_F_SOLID_DERIVED)))
-        launch_mixed_join(ctx->st, GroupOne{scene_of(ctx, ctx->parity), ctx->form});
+    if (ctx->form == SPHNJ_FORM_MIXED)
+        launch_mixed_join(ctx->st, GroupOne{scene_of(ctx, ctx->parity), ctx->form},
+                          ((mask & SPHNJ_F_FLUID_KINEMATICS) ? 1 : 0) |
+                              ((mask & (SPHNJ_F_SOLID_KINEMATICS | SPHNJ_F_SOLID_DERIVED)) ? 2 : 0));
     if (mask & SPHNJ_F_FLUID_KINEMATICS) {
         RET(d2h(ctx, s->fluid_position, d.f_pos, nf));
         RET(d2h(ctx, s->fluid_velocity, d.f_vel, nf));

@@ -209,7 +209,7 @@ template <class G> int launch_solid_update(cudaStream_t st, G &g, int sub);
 // fluid, bit 1 solid, bit 2 virtual), and mixed state -> host layout
 // (absolute positions, FP64 solid position / velocity / acceleration)
 void launch_mixed_split(cudaStream_t st, const GroupOne &g, int kinds);
-void launch_mixed_join(cudaStream_t st, const GroupOne &g);
+void launch_mixed_join(cudaStream_t st, const GroupOne &g, int kinds);  // bit 0 fluid, bit 1 solid
 
 // global diagnostics (kernels_diag.cu): kDiagBlocks x kDiagSlots doubles of
 // per-block partials, then the result in *out (device memory)

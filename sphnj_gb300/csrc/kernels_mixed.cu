@@ -16,20 +16,31 @@ namespace {
 
 constexpr int kBlock = 256;
 
+// The cell grid in FP64; iwx, iwy are 1 / width, computed on the host.
 struct Grid2 {
-    double x0, y0, wx, wy;
+    double x0, y0, wx, wy, iwx, iwy;
     int nx, ny;
 };
-__device__ __forceinline__ Grid2 grid_of(const sphnj_params &p) {
-    return {(double)p.cell_xmin[0], (double)p.cell_xmin[1], (double)p.interval[0], (double)p.interval[1],
+__device__ __forceinline__ Grid2 grid_of(const sphnj_params &p, double iwx = 0.0, double iwy = 0.0) {
+    return {(double)p.cell_xmin[0], (double)p.cell_xmin[1], (double)p.interval[0], (double)p.interval[1], iwx, iwy,
             p.cell_number[0], p.cell_number[1]};
+}
+
+// floor((x - x0) / w) without an FP64 division (slow on this GPU): the
+// product with the reciprocal, corrected by one step so that the corner
+// satisfies x0 + c w <= x < x0 + (c + 1) w as evaluated in FP64.
+__device__ __forceinline__ double cell_floor(double x, double x0, double w, double iw) {
+    double c = floor((x - x0) * iw);
+    if (x0 + c * w > x) c -= 1.0;
+    else if (x0 + (c + 1.0) * w <= x) c += 1.0;
+    return c;
 }
 
 // Cell (x, y) holding absolute position (x, y) and the FP32 offset from its
 // corner; positions outside the grid are reported and clamped into it.
 __device__ __forceinline__ int2 split_pos(const Grid2 &g, double x, double y, float2 &off, DevErr *err, int kind,
                                           int i) {
-    double fx = floor((x - g.x0) / g.wx), fy = floor((y - g.y0) / g.wy);
+    double fx = cell_floor(x, g.x0, g.wx, g.iwx), fy = cell_floor(y, g.y0, g.wy, g.iwy);
     if (!(fx >= 0.0 && fx < g.nx && fy >= 0.0 && fy < g.ny)) {
         raise_error(err, SPHNJ_ERR_OUT_OF_GRID, kind, i, -1);
         fx = fx == fx ? fmin(fmax(fx, 0.0), (double)(g.nx - 1)) : 0.0;
@@ -46,11 +57,11 @@ __device__ __forceinline__ float2 round_f2(double2 v, float2 &comp) {
 }
 
 // kinds: bit 0 fluid, bit 1 solid, bit 2 virtual
-__global__ void k_split(const __grid_constant__ One g, int kinds) {
+__global__ void k_split(const __grid_constant__ One g, int kinds, double iwx, double iwy) {
     const Scene &S = g.s;
     const sphnj_params &p = S.p;
     const DevState &d = S.d;
-    const Grid2 gr = grid_of(p);
+    const Grid2 gr = grid_of(p, iwx, iwy);
     const int nf = p.fluid_number_total, ns = p.solid_number, nv = p.virt_number;
     const long t = (long)blockIdx.x * blockDim.x + threadIdx.x;
     if (t < nf) {
@@ -89,7 +100,8 @@ __global__ void k_split(const __grid_constant__ One g, int kinds) {
     }
 }
 
-__global__ void k_join(const __grid_constant__ One g) {
+// kinds: bit 0 fluid, bit 1 solid
+__global__ void k_join(const __grid_constant__ One g, int kinds) {
     const Scene &S = g.s;
     const sphnj_params &p = S.p;
     const DevState &d = S.d;
@@ -97,6 +109,7 @@ __global__ void k_join(const __grid_constant__ One g) {
     const int nf = p.fluid_number_total, ns = p.solid_number;
     const long t = (long)blockIdx.x * blockDim.x + threadIdx.x;
     if (t < nf) {
+        if (!(kinds & 1)) return;
         const int i = (int)t;
         const int c = d.f_cell[i];
         const int cx = c / gr.ny, cy = c - cx * gr.ny;
@@ -104,6 +117,7 @@ __global__ void k_join(const __grid_constant__ One g) {
         d.f_pos[i] = make_float2((float)(gr.x0 + cx * gr.wx + ((double)off.x - (double)oc.x)),
                                  (float)(gr.y0 + cy * gr.wy + ((double)off.y - (double)oc.y)));
     } else if (t < (long)nf + ns) {
+        if (!(kinds & 2)) return;
         const int i = (int)(t - nf);
         const double2 X = d.s_ref[i];
         const float2 u = d.s_u[i], uc = d.s_uc[i], v = d.s_v[i], vc = d.s_vc[i], a = d.s_acc[i];
@@ -118,13 +132,15 @@ __global__ void k_join(const __grid_constant__ One g) {
 void launch_mixed_split(cudaStream_t st, const GroupOne &g, int kinds) {
     const sphnj_params &p = g.s.p;
     const long n = (long)p.fluid_number_total + p.solid_number + p.virt_number;
-    if (n > 0) k_split<<<grid_for(n, kBlock), kBlock, 0, st>>>(One{g.s}, kinds);
+    if (n > 0 && kinds)
+        k_split<<<grid_for(n, kBlock), kBlock, 0, st>>>(One{g.s}, kinds, 1.0 / (double)p.interval[0],
+                                                        1.0 / (double)p.interval[1]);
 }
 
-void launch_mixed_join(cudaStream_t st, const GroupOne &g) {
+void launch_mixed_join(cudaStream_t st, const GroupOne &g, int kinds) {
     const sphnj_params &p = g.s.p;
     const long n = (long)p.fluid_number_total + p.solid_number;
-    if (n > 0) k_join<<<grid_for(n, kBlock), kBlock, 0, st>>>(One{g.s});
+    if (n > 0 && kinds) k_join<<<grid_for(n, kBlock), kBlock, 0, st>>>(One{g.s}, kinds);
 }
 
 }  // namespace sphnj
