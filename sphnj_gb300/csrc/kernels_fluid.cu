@@ -39,6 +39,7 @@
 #include "kernels.h"
 
 #include <algorithm>
+#include <cmath>
 #include <type_traits>
 
 namespace sphnj {
@@ -48,6 +49,37 @@ namespace {
 constexpr int kPairBlock = 128;
 constexpr int kTileBlock = 256;  // tiled sweeps: ~208 particles per 16-cell tile
 constexpr int kListBlock = 128;  // shifting passes over an active-tile list
+
+// Block shape of the pair pass.  One-scene launches: 256 threads, 5 blocks per
+// SM (48 registers, no spills; unbounded it takes 64 and 4 blocks).  Batched
+// launches over tile lists: 128 threads (partly filled tiles leave fewer warps
+// waiting at the tile's barriers), 8 per SM where their staging fits
+// (pair_per_cell).  256-scene mixed sweep: 4.56 -> 4.46 ms/step.
+template <class G> struct PairShape {
+    static constexpr int threads = 256, min_blocks = 5;
+};
+template <> struct PairShape<GroupMany> {
+    static constexpr int threads = 128, min_blocks = 8;
+};
+constexpr int kMaxPerCell = 24;  // staged particles per cell at most
+
+// Particles per cell the pair pass stages (a tile with more falls back to the
+// unstaged sweep, without lists).  A scene swept alone: kMaxPerCell.  A batch:
+// 1.2 times the lattice count (cell area / particle area) of its densest
+// scene, at least 8, so that a typical batch's staging lets 7 or 8 blocks
+// share an SM (13 to 13.5 per cell at h = 1.2 dx: 16 or 17, 25 to 27 KB a
+// block; a 16-cell tile stages about 700 of its 864 to 918 entries).
+inline int pair_per_cell(const GroupOne &) { return kMaxPerCell; }
+inline int pair_per_cell(const GroupMany &g) {
+    double most = 0.0;
+    for (int k = 0; k < g.n; ++k) {
+        const sphnj_params &p = g.h_scenes[k].p;
+        if (p.fluid_number_total <= 0 || !(p.particle_diameter > 0.0f)) continue;
+        const double dx = p.particle_diameter;
+        most = std::max(most, (double)p.interval[0] * p.interval[1] / (dx * dx));
+    }
+    return std::min(kMaxPerCell, std::max(8, (int)std::ceil(1.2 * most)));
+}
 constexpr int kBlock = 256;
 constexpr int kFallbackBlocks = 304;  // 2 x 152 SMs, grid-stride
 
@@ -733,10 +765,9 @@ __device__ __forceinline__ Frame tile_frame(const sphnj_params &p, const DevStat
 // kList: the blocks loop over the scene's listed active tiles (batched
 // launches, and scenes that sweep_compacted() selects); otherwise block b
 // sweeps tile b, returning at once if it is empty.
-template <class G, class F, bool kList>
-// 5 blocks per SM: 48 registers, no spills (unbounded it takes 64 and 4 blocks)
-__global__ void __launch_bounds__(kTileBlock, 5) k_fluid_pair_tiled(const __grid_constant__ G gs, int tile_h, int cap,
-                                                                 int use_lists) {
+template <class G, class F, bool kList, int kThreads, int kMinBlocks>
+__global__ void __launch_bounds__(kThreads, kMinBlocks)
+    k_fluid_pair_tiled(const __grid_constant__ G gs, int tile_h, int cap, int use_lists) {
     SPHNJ_SCENE(gs);
     extern __shared__ __align__(16) unsigned char smem[];
     __shared__ int s_base[3], s_off[3];
@@ -945,7 +976,8 @@ template <class G, class F> __global__ void __launch_bounds__(kBlock) k_shift_co
     if (i < p.fluid_number_total) (F::kMixed ? d.f_off : d.f_pos)[i] = d.f_x_alt[i];
 }
 
-inline int tile_cap(int tile_h) { return 3 * (tile_h + 2) * 24; }
+// staged entries of a tile: three strips of tile_h + 2 cells at per_cell particles
+inline int tile_cap(int tile_h, int per_cell = kMaxPerCell) { return 3 * (tile_h + 2) * per_cell; }
 inline unsigned tile_blocks(const sphnj_params &p, int tile_h) {
     return (unsigned)p.cell_number[0] * (unsigned)((p.cell_number[1] + tile_h - 1) / tile_h);
 }
@@ -965,16 +997,21 @@ constexpr size_t kPairSmemPerEntry = 3 * sizeof(float2) + sizeof(int) + 1;
 }  // namespace
 
 cudaError_t configure_sweeps(const TileConfig &tc) {
-    const size_t smem = tile_cap(tc.tile_h) * kPairSmemPerEntry;  // above 48 KB needs an opt-in
-    if (smem <= 48 * 1024) return cudaSuccess;
+    using P1 = PairShape<GroupOne>;
+    using PM = PairShape<GroupMany>;
+    // dynamic shared memory above 48 KB needs an opt-in
     const int a = cudaFuncAttributeMaxDynamicSharedMemorySize;
-    const void *kernels[] = {
-        (const void *)k_fluid_pair_tiled<One, FormPlain, false>, (const void *)k_fluid_pair_tiled<One, FormPlain, true>,
-        (const void *)k_fluid_pair_tiled<Many, FormPlain, false>, (const void *)k_fluid_pair_tiled<Many, FormPlain, true>,
-        (const void *)k_fluid_pair_tiled<One, FormMixed, false>, (const void *)k_fluid_pair_tiled<One, FormMixed, true>,
-        (const void *)k_fluid_pair_tiled<Many, FormMixed, false>, (const void *)k_fluid_pair_tiled<Many, FormMixed, true>};
-    for (const void *k : kernels) {
-        const cudaError_t e = cudaFuncSetAttribute(k, (cudaFuncAttribute)a, (int)smem);
+    const size_t smem1 = tile_cap(tc.tile_h, kMaxPerCell) * kPairSmemPerEntry, smemM = smem1;
+    const std::pair<const void *, size_t> kernels[] = {
+        {(const void *)k_fluid_pair_tiled<One, FormPlain, false, P1::threads, P1::min_blocks>, smem1},
+        {(const void *)k_fluid_pair_tiled<One, FormPlain, true, P1::threads, P1::min_blocks>, smem1},
+        {(const void *)k_fluid_pair_tiled<One, FormMixed, false, P1::threads, P1::min_blocks>, smem1},
+        {(const void *)k_fluid_pair_tiled<One, FormMixed, true, P1::threads, P1::min_blocks>, smem1},
+        {(const void *)k_fluid_pair_tiled<Many, FormPlain, true, PM::threads, PM::min_blocks>, smemM},
+        {(const void *)k_fluid_pair_tiled<Many, FormMixed, true, PM::threads, PM::min_blocks>, smemM}};
+    for (const auto &k : kernels) {
+        if (k.second <= 48 * 1024) continue;
+        const cudaError_t e = cudaFuncSetAttribute(k.first, (cudaFuncAttribute)a, (int)k.second);
         if (e != cudaSuccess) return e;
     }
     return cudaSuccess;
@@ -1004,19 +1041,24 @@ template <class F, class G> int fluid_pair(cudaStream_t st, G &g, const TileConf
         return launch(
             g, site_key(SITE_PAIR_EACH), [](const Scene &s) { return grid_for(s.p.fluid_number_total, kPairBlock); },
             k_fluid_pair_each<D, F>, kPairBlock, 0, st, 0);
-    const int cap = tile_cap(tc.tile_h);
+    using Shape = PairShape<G>;
+    const int cap = tile_cap(tc.tile_h, pair_per_cell(g));
     const size_t smem = cap * kPairSmemPerEntry;
     // this step's active tiles (the cell lists are final), used by the pair
     // pass and every shifting pass of the step
     int n = launch_tile_compact(st, g, tc.tile_h, std::is_same<G, GroupMany>::value);
-    auto blocks = [&](const Scene &s) { return sweep_blocks(s.p, tc.tile_h); };
+    auto blocks = [&](const Scene &s) {
+        return std::min<unsigned>(tile_blocks(s.p, tc.tile_h),
+                                  sweep_blocks(s.p, tc.tile_h) * (kTileBlock / Shape::threads));
+    };
     const int lists = tc.lists ? 1 : 0;
+    const long long key = site_key(SITE_PAIR_TILED, tc.tile_h);
     if (use_tile_list(g, tc.tile_h))
-        n += launch(g, site_key(SITE_PAIR_TILED, tc.tile_h), blocks, k_fluid_pair_tiled<D, F, true>, kTileBlock, smem,
-                    st, tc.tile_h, cap, lists);
-    else
-        n += launch(g, site_key(SITE_PAIR_TILED, tc.tile_h), blocks, k_fluid_pair_tiled<D, F, false>, kTileBlock, smem,
-                    st, tc.tile_h, cap, lists);
+        n += launch(g, key, blocks, k_fluid_pair_tiled<D, F, true, Shape::threads, Shape::min_blocks>, Shape::threads,
+                    smem, st, tc.tile_h, cap, lists);
+    else if constexpr (!std::is_same<G, GroupMany>::value)  // batches always sweep their lists
+        n += launch(g, key, blocks, k_fluid_pair_tiled<D, F, false, Shape::threads, Shape::min_blocks>, Shape::threads,
+                    smem, st, tc.tile_h, cap, lists);
     n += launch(
         g, site_key(SITE_PAIR_FALLBACK), [](const Scene &s) { return fallback_blocks(s.p.fluid_number_total); },
         k_fluid_pair_each<D, F>, kPairBlock, 0, st, 1);
