@@ -126,6 +126,39 @@ __device__ __forceinline__ int neighbour_cell(int c, int n, int nx, int ny) {
     return i * ny + j;
 }
 
+// Calls fn(t, n) for every slot t of the CSR list `rng` in the nine cells
+// around cell c, in the order of the loop over neighbour slots n = 0..8.
+// Cells are numbered column-major and a list's ranges follow the cell order,
+// so rows cj-1..cj+1 of one column are one contiguous range of slots: three
+// ranges instead of nine, their bounds loaded together up front.  With kSlot
+// the slot n of each entry's cell is passed too (row cj starts at m1 and row
+// cj+1 at m2 in the column's range); otherwise n is 0.
+template <bool kSlot, class Fn>
+__device__ __forceinline__ void for_each_in_stencil(const int2 *rng, int c, int nx, int ny, Fn &&fn) {
+    const int ci = c / ny, cj = c - ci * ny;
+    const int r0 = max(cj - 1, 0), r1 = min(cj + 1, ny - 1);
+    int2 lo[3], mid[3], hi[3];
+#pragma unroll
+    for (int k = 0; k < 3; ++k) {
+        const int col = ci + k - 1;
+        lo[k] = mid[k] = hi[k] = make_int2(0, 0);
+        if (col >= 0 && col < nx) {
+            lo[k] = __ldg(&rng[col * ny + r0]);
+            hi[k] = __ldg(&rng[col * ny + r1]);
+            if constexpr (kSlot) mid[k] = __ldg(&rng[col * ny + cj]);
+        }
+    }
+#pragma unroll
+    for (int k = 0; k < 3; ++k) {
+        const int b = lo[k].x, e = hi[k].x + hi[k].y;
+        const int m1 = mid[k].x, m2 = cj + 1 < ny ? hi[k].x : e;
+        for (int t = b; t < e; ++t) {
+            if constexpr (kSlot) fn(t, 3 * k + (t >= m1) + (t >= m2));
+            else fn(t, 0);
+        }
+    }
+}
+
 // Gaussian kernel-gradient factor exp(-q^2) * Kd * C32 (fluid.cu:44-46)
 __device__ __forceinline__ float grad_w(const sphnj_params &p, float q2) {
     return expf(-q2) * p.kernel_differential * p.coefficient_3d_to_2d;

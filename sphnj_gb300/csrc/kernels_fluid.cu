@@ -570,10 +570,29 @@ __device__ __forceinline__ float2 shift_particle_listed(const sphnj_params &p, c
 // The lists of this step still hold every pair within the cutoff when twice
 // the summed per-update maximum displacement since the pair pass is inside
 // the skin (margin 0.9 for rounding).  `pass` shifting updates came before.
+// Lane k loads the maximum of update k, so the maxima arrive together rather
+// than one after another; the butterfly sum leaves the same bits in every
+// lane (each step adds the same two values).  Called by full warps.
 __device__ __forceinline__ bool lists_valid(const sphnj_params &p, const DevState &d, int pass) {
+    static_assert(kMaskShifts <= 32, "one lane per tracked update");
     if (pass >= kMaskShifts) return false;
-    float moved = 0.0f;
-    for (int k = 0; k <= pass; ++k) moved += sqrtf(__uint_as_float(d.disp2_bits[k]));
+    const int lane = threadIdx.x & 31;
+    float moved = lane <= pass ? sqrtf(__uint_as_float(__ldcg(&d.disp2_bits[lane]))) : 0.0f;
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) moved += __shfl_xor_sync(0xffffffffu, moved, o);
+    return 2.0f * moved < 0.9f * kSkin * sqrtf(p.impact_distance_square);
+}
+// The same test in two halves, for a kernel that issues the loads on entry
+// (list_moved_share) and sums only when it first needs the answer.
+__device__ __forceinline__ unsigned int list_moved_share(const DevState &d, int pass) {
+    const int lane = threadIdx.x & 31;
+    return pass < kMaskShifts && lane <= pass ? __ldcg(&d.disp2_bits[lane]) : 0u;
+}
+__device__ __forceinline__ bool lists_valid(const sphnj_params &p, unsigned int share, int pass) {
+    if (pass >= kMaskShifts) return false;
+    float moved = sqrtf(__uint_as_float(share));
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) moved += __shfl_xor_sync(0xffffffffu, moved, o);
     return 2.0f * moved < 0.9f * kSkin * sqrtf(p.impact_distance_square);
 }
 
@@ -830,11 +849,21 @@ __global__ void __launch_bounds__(kThreads, 2048 / kThreads)
     extern __shared__ __align__(16) unsigned char smem[];
     __shared__ int s_base[3], s_off[3];
     float2 *s_pos = reinterpret_cast<float2 *>(smem);
-    const bool use_list = lists_valid(p, d, pass);
+    // A block of a list launch, which sweeps several tiles, sums on its first
+    // tile with work, after that tile's setup has issued its loads; a block
+    // of one tile sums on entry (measured: each the faster of the two for its
+    // launch shape).
+    const bool entry_ok = kList ? false : lists_valid(p, d, pass);
+    [[maybe_unused]] const unsigned int moved_share = kList ? list_moved_share(d, pass) : 0u;
+    int first_ok = -1;
     unsigned int moved2 = 0u;
     auto sweep = [&](int tile) {
         TileGeom g;
         if (!tile_setup(p, d, tile, tile_h, s_base, s_off, g)) return;
+        // every thread of the block is here (tile_setup returns uniformly)
+        if constexpr (kList)
+            if (first_ok < 0) first_ok = lists_valid(p, moved_share, pass) ? 1 : 0;
+        const bool use_list = kList ? first_ok != 0 : entry_ok;
         const bool staged = g.total <= cap;
         if (staged) {
             for (int k = threadIdx.x; k < g.total; k += blockDim.x) {

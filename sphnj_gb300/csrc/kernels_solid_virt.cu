@@ -67,29 +67,22 @@ template <class G, class F> __global__ void __launch_bounds__(kBlock) k_virt_dat
     float2 vel = make_float2(0.f, 0.f);
     float pr = 0.f, sum = 0.f, nearest = LARGE_FLOAT;
     int phase = d.v_phase[i];
-    const int c = d.v_cell[i];
-    for (int n = 0; n < 9; ++n) {
-        const int m = neighbour_cell(c, n, nx, ny);
-        if (m < 0) continue;
-        const float2 sh = F::shift(p, fr, n);
-        const int2 rf = __ldg(&d.rng_f[m]);
-        for (int t = rf.x; t < rf.x + rf.y; ++t) {
-            const int j = __ldg(&d.lst_f[t]);
-            const float2 dx = sub2(F::f_nbr(d, j, sh), x_i);
-            const float d2 = sqn(dx);
-            if (!(d2 < R2)) continue;
-            const float kc = sw(p, d2 * hinv2);
-            sum += kc;
-            const float2 vj = __ldg(&d.f_vel[j]);
-            vel.x += vj.x * kc;
-            vel.y += vj.y * kc;
-            pr += (__ldg(&d.f_p[j]) - __ldg(&d.f_rho[j]) * (gx * dx.x + gy * dx.y)) * kc;
-            if (d2 < nearest) {
-                phase = __ldg(&d.f_phase[j]);
-                nearest = d2;
-            }
+    for_each_in_stencil<F::kMixed>(d.rng_f, d.v_cell[i], nx, ny, [&](int t, int n) {
+        const int j = __ldg(&d.lst_f[t]);
+        const float2 dx = sub2(F::f_nbr(d, j, F::shift(p, fr, n)), x_i);
+        const float d2 = sqn(dx);
+        if (!(d2 < R2)) return;
+        const float kc = sw(p, d2 * hinv2);
+        sum += kc;
+        const float2 vj = __ldg(&d.f_vel[j]);
+        vel.x += vj.x * kc;
+        vel.y += vj.y * kc;
+        pr += (__ldg(&d.f_p[j]) - __ldg(&d.f_rho[j]) * (gx * dx.x + gy * dx.y)) * kc;
+        if (d2 < nearest) {
+            phase = __ldg(&d.f_phase[j]);
+            nearest = d2;
         }
-    }
+    });
     float2 v;
     float pv;
     if (sum != 0.0f) {
@@ -126,30 +119,24 @@ template <class G, class F> __global__ void __launch_bounds__(kBlock) k_solid_co
     const float2 x_i = F::s_home(p, d, fr, i);
     float2 nrm = make_float2(0.f, 0.f);
     float pr = 0.f, sum = 0.f;
+    // fluid and solid neighbours feed separate sums, each in stencil order
     const int c = d.s_cell[i];
-    for (int n = 0; n < 9; ++n) {
-        const int m = neighbour_cell(c, n, nx, ny);
-        if (m < 0) continue;
-        const float2 sh = F::shift(p, fr, n);
-        const int2 rf = __ldg(&d.rng_f[m]);
-        for (int t = rf.x; t < rf.x + rf.y; ++t) {
-            const int j = __ldg(&d.lst_f[t]);
-            const float2 dx = sub2(F::f_nbr(d, j, sh), x_i);
-            if (!(sqn(dx) < R2)) continue;
-            const float kc = sw(p, sqn(dx) * hinv2);
-            sum += kc;
-            pr += __ldg(&d.f_p[j]) * kc;
-        }
-        const int2 rs = __ldg(&d.rng_s[m]);
-        for (int t = rs.x; t < rs.x + rs.y; ++t) {
-            const int j = __ldg(&d.lst_s[t]);
-            const float2 dx = sub2(F::s_nbr(d, j, sh), x_i);
-            if (!(sqn(dx) < R2)) continue;
-            const float kc = gw(p, sqn(dx) * hinv2);
-            nrm.x -= dx.x * kc;
-            nrm.y -= dx.y * kc;
-        }
-    }
+    for_each_in_stencil<F::kMixed>(d.rng_f, c, nx, ny, [&](int t, int n) {
+        const int j = __ldg(&d.lst_f[t]);
+        const float2 dx = sub2(F::f_nbr(d, j, F::shift(p, fr, n)), x_i);
+        if (!(sqn(dx) < R2)) return;
+        const float kc = sw(p, sqn(dx) * hinv2);
+        sum += kc;
+        pr += __ldg(&d.f_p[j]) * kc;
+    });
+    for_each_in_stencil<F::kMixed>(d.rng_s, c, nx, ny, [&](int t, int n) {
+        const int j = __ldg(&d.lst_s[t]);
+        const float2 dx = sub2(F::s_nbr(d, j, F::shift(p, fr, n)), x_i);
+        if (!(sqn(dx) < R2)) return;
+        const float kc = gw(p, sqn(dx) * hinv2);
+        nrm.x -= dx.x * kc;
+        nrm.y -= dx.y * kc;
+    });
     d.s_normal[i] = sqrtf(sqn(nrm)) < EPS_FOR_SUM ? make_float2(0.f, 0.f) : normalized(nrm);
     d.s_p[i] = sum != 0.0f ? fmaxf(pr / sum, p.min_pressure) : 0.0f;
 }
@@ -213,29 +200,23 @@ template <class G> __global__ void __launch_bounds__(kBlock) k_solid_deform(cons
     const int nx = p.cell_number[0], ny = p.cell_number[1];
     dmat2 L = {0, 0, 0, 0}, Ft = {0, 0, 0, 0};
     const double2 xr_i = d.s_ref[i], x_i = d.s_pos[i];
-    const int c = d.s_cell[i];
-    for (int n = 0; n < 9; ++n) {
-        const int m = neighbour_cell(c, n, nx, ny);
-        if (m < 0) continue;
-        const int2 rs = __ldg(&d.rng_s[m]);
-        for (int t = rs.x; t < rs.x + rs.y; ++t) {
-            const int j = __ldg(&d.lst_s[t]);
-            const double2 xr_j = d.s_ref[j];
-            const double2 dref = make_double2(xr_j.x - xr_i.x, xr_j.y - xr_i.y);
-            if (!ref_within(p, dref)) continue;
-            const double2 x_j = d.s_pos[j];
-            const double2 dx = make_double2(x_j.x - x_i.x, x_j.y - x_i.y);
-            const double kc = (double)gw(p, ref_q2(p, dref));
-            Ft.m00 += dx.x * dref.x * kc;
-            Ft.m10 += dx.y * dref.x * kc;
-            Ft.m01 += dx.x * dref.y * kc;
-            Ft.m11 += dx.y * dref.y * kc;
-            L.m00 += dref.x * dref.x * kc;
-            L.m10 += dref.y * dref.x * kc;
-            L.m01 += dref.x * dref.y * kc;
-            L.m11 += dref.y * dref.y * kc;
-        }
-    }
+    for_each_in_stencil<false>(d.rng_s, d.s_cell[i], nx, ny, [&](int t, int) {
+        const int j = __ldg(&d.lst_s[t]);
+        const double2 xr_j = d.s_ref[j];
+        const double2 dref = make_double2(xr_j.x - xr_i.x, xr_j.y - xr_i.y);
+        if (!ref_within(p, dref)) return;
+        const double2 x_j = d.s_pos[j];
+        const double2 dx = make_double2(x_j.x - x_i.x, x_j.y - x_i.y);
+        const double kc = (double)gw(p, ref_q2(p, dref));
+        Ft.m00 += dx.x * dref.x * kc;
+        Ft.m10 += dx.y * dref.x * kc;
+        Ft.m01 += dx.x * dref.y * kc;
+        Ft.m11 += dx.y * dref.y * kc;
+        L.m00 += dref.x * dref.x * kc;
+        L.m10 += dref.y * dref.x * kc;
+        L.m01 += dref.x * dref.y * kc;
+        L.m11 += dref.y * dref.y * kc;
+    });
     if (ddet(L) != 0.0) L = dinv(L);
     else L = {1.0, 0.0, 0.0, 1.0};
     const dmat2 F = dmul(Ft, L);
@@ -271,55 +252,51 @@ template <class G> __global__ void __launch_bounds__(kBlock) k_solid_force(const
     const float p_i = d.s_p[i];
     float2 couple = make_float2(0.f, 0.f);
     double2 acc = make_double2(0.0, 0.0);
+    // fluid (couple) and solid (acc) neighbours feed separate sums, each in
+    // stencil order
     const int c = d.s_cell[i];
-    for (int n = 0; n < 9; ++n) {
-        const int m = neighbour_cell(c, n, nx, ny);
-        if (m < 0) continue;
-        const int2 rf = __ldg(&d.rng_f[m]);
-        for (int t = rf.x; t < rf.x + rf.y; ++t) {  // solidFluidCouple, solid.cu:211-255
-            const int j = __ldg(&d.lst_f[t]);
-            const float2 dx = sub2(__ldg(&d.f_pos[j]), x_i);
-            if (!(sqn(dx) < R2)) continue;
-            const float kc = gw(p, sqn(dx) * hinv2);
-            const float p_j = __ldg(&d.f_p[j]);
-            const float cs = by_phase(p.sound_speed, __ldg(&d.f_phase[j]));
-            const float rho_j = __ldg(&d.f_rho[j]), rho_i = rho_j;
-            const float2 u_j = __ldg(&d.f_vel[j]);
-            float ps = fdiv(rho_i * p_j + rho_j * p_i, rho_i + rho_j);
-            float2 nn = sqn(dx) > 0.f ? make_float2(fdiv(dx.x, sqrtf(sqn(dx))), fdiv(dx.y, sqrtf(sqn(dx)))) : dx;
-            const float du = dot2(sub2(u_i, u_j), nn);
-            if (du >= 0.0f) ps += fdiv(rho_i * rho_j * du, rho_i + rho_j) * fminf(3.0f * du, cs);
-            const float am = fdiv(-2.0f * ps, rho_ref);
-            couple.x += am * dx.x * kc;
-            couple.y += am * dx.y * kc;
-        }
-        const int2 rs = __ldg(&d.rng_s[m]);
-        for (int t = rs.x; t < rs.x + rs.y; ++t) {  // solidSolidForce, solid.cu:257-305
-            const int j = __ldg(&d.lst_s[t]);
-            const double2 xr_j = d.s_ref[j];
-            const double2 dref = make_double2(xr_j.x - xr_i.x, xr_j.y - xr_i.y);
-            if (!ref_within(p, dref)) continue;
-            const double kc = (double)gw(p, ref_q2(p, dref));
-            const dmat2 PL = dmul(d.s_P[j], d.s_L[j]);
-            const dmat2 M = {PL.m00 + PL_i.m00, PL.m10 + PL_i.m10, PL.m01 + PL_i.m01, PL.m11 + PL_i.m11};
-            const double2 tv = dmv(M, dref);
-            acc.x += tv.x * kc / rho_ref_d;
-            acc.y += tv.y * kc / rho_ref_d;
-            const double2 x_j = d.s_pos[j], v_j = d.s_vel[j];
-            const double2 dx = make_double2(x_j.x - x_id.x, x_j.y - x_id.y);
-            const double2 dv = make_double2(v_j.x - v_id.x, v_j.y - v_id.y);
-            const float dvdx = __double2float_rn(dv.x * dx.x + dv.y * dx.y);
-            const float dis2 = __double2float_rn(dx.x * dx.x + dx.y * dx.y);
-            const float nuv = hs * dvdx / (dis2 + eps);
-            float visc = alpha * nuv * cs_s;
-            visc -= beta * nuv * nuv;
-            const double vd = (double)visc;
-            const dmat2 Fv = {F_i.m00 * vd, F_i.m10 * vd, F_i.m01 * vd, F_i.m11 * vd};
-            const double2 w = dmv(dmul(Fv, L_i), dref);
-            acc.x += w.x * kc;
-            acc.y += w.y * kc;
-        }
-    }
+    for_each_in_stencil<false>(d.rng_f, c, nx, ny, [&](int t, int) {  // solidFluidCouple, solid.cu:211-255
+        const int j = __ldg(&d.lst_f[t]);
+        const float2 dx = sub2(__ldg(&d.f_pos[j]), x_i);
+        if (!(sqn(dx) < R2)) return;
+        const float kc = gw(p, sqn(dx) * hinv2);
+        const float p_j = __ldg(&d.f_p[j]);
+        const float cs = by_phase(p.sound_speed, __ldg(&d.f_phase[j]));
+        const float rho_j = __ldg(&d.f_rho[j]), rho_i = rho_j;
+        const float2 u_j = __ldg(&d.f_vel[j]);
+        float ps = fdiv(rho_i * p_j + rho_j * p_i, rho_i + rho_j);
+        float2 nn = sqn(dx) > 0.f ? make_float2(fdiv(dx.x, sqrtf(sqn(dx))), fdiv(dx.y, sqrtf(sqn(dx)))) : dx;
+        const float du = dot2(sub2(u_i, u_j), nn);
+        if (du >= 0.0f) ps += fdiv(rho_i * rho_j * du, rho_i + rho_j) * fminf(3.0f * du, cs);
+        const float am = fdiv(-2.0f * ps, rho_ref);
+        couple.x += am * dx.x * kc;
+        couple.y += am * dx.y * kc;
+    });
+    for_each_in_stencil<false>(d.rng_s, c, nx, ny, [&](int t, int) {  // solidSolidForce, solid.cu:257-305
+        const int j = __ldg(&d.lst_s[t]);
+        const double2 xr_j = d.s_ref[j];
+        const double2 dref = make_double2(xr_j.x - xr_i.x, xr_j.y - xr_i.y);
+        if (!ref_within(p, dref)) return;
+        const double kc = (double)gw(p, ref_q2(p, dref));
+        const dmat2 PL = dmul(d.s_P[j], d.s_L[j]);
+        const dmat2 M = {PL.m00 + PL_i.m00, PL.m10 + PL_i.m10, PL.m01 + PL_i.m01, PL.m11 + PL_i.m11};
+        const double2 tv = dmv(M, dref);
+        acc.x += tv.x * kc / rho_ref_d;
+        acc.y += tv.y * kc / rho_ref_d;
+        const double2 x_j = d.s_pos[j], v_j = d.s_vel[j];
+        const double2 dx = make_double2(x_j.x - x_id.x, x_j.y - x_id.y);
+        const double2 dv = make_double2(v_j.x - v_id.x, v_j.y - v_id.y);
+        const float dvdx = __double2float_rn(dv.x * dx.x + dv.y * dx.y);
+        const float dis2 = __double2float_rn(dx.x * dx.x + dx.y * dx.y);
+        const float nuv = hs * dvdx / (dis2 + eps);
+        float visc = alpha * nuv * cs_s;
+        visc -= beta * nuv * nuv;
+        const double vd = (double)visc;
+        const dmat2 Fv = {F_i.m00 * vd, F_i.m10 * vd, F_i.m01 * vd, F_i.m11 * vd};
+        const double2 w = dmv(dmul(Fv, L_i), dref);
+        acc.x += w.x * kc;
+        acc.y += w.y * kc;
+    });
     d.s_couple[i] = couple;
     d.s_dudt[i] = make_double2(acc.x + (double)couple.x, acc.y + (double)couple.y);
 }
@@ -380,29 +357,23 @@ template <class G> __global__ void __launch_bounds__(kBlock) k_solid_deform_mixe
     const int2 rc_i = d.s_rc[i];
     const float2 ro_i = d.s_roff[i], u_i = d.s_u[i];
     float h00 = 0.f, h10 = 0.f, h01 = 0.f, h11 = 0.f, m00 = 0.f, m10 = 0.f, m01 = 0.f, m11 = 0.f;
-    const int c = d.s_cell[i];
-    for (int n = 0; n < 9; ++n) {
-        const int m = neighbour_cell(c, n, nx, ny);
-        if (m < 0) continue;
-        const int2 rs = __ldg(&d.rng_s[m]);
-        for (int t = rs.x; t < rs.x + rs.y; ++t) {
-            const int j = __ldg(&d.lst_s[t]);
-            const float2 dX = ref_delta(p, rc_i, ro_i, __ldg(&d.s_rc[j]), __ldg(&d.s_roff[j]));
-            const float q = sqn(dX);
-            if (!(q < R2)) continue;
-            const float kc = gw(p, q * hinv2);
-            const float2 du = sub2(__ldg(&d.s_u[j]), u_i);
-            const float ax = dX.x * kc, ay = dX.y * kc;
-            h00 += du.x * ax;
-            h10 += du.y * ax;
-            h01 += du.x * ay;
-            h11 += du.y * ay;
-            m00 += dX.x * ax;
-            m10 += dX.y * ax;
-            m01 += dX.x * ay;
-            m11 += dX.y * ay;
-        }
-    }
+    for_each_in_stencil<false>(d.rng_s, d.s_cell[i], nx, ny, [&](int t, int) {
+        const int j = __ldg(&d.lst_s[t]);
+        const float2 dX = ref_delta(p, rc_i, ro_i, __ldg(&d.s_rc[j]), __ldg(&d.s_roff[j]));
+        const float q = sqn(dX);
+        if (!(q < R2)) return;
+        const float kc = gw(p, q * hinv2);
+        const float2 du = sub2(__ldg(&d.s_u[j]), u_i);
+        const float ax = dX.x * kc, ay = dX.y * kc;
+        h00 += du.x * ax;
+        h10 += du.y * ax;
+        h01 += du.x * ay;
+        h11 += du.y * ay;
+        m00 += dX.x * ax;
+        m10 += dX.y * ax;
+        m01 += dX.x * ay;
+        m11 += dX.y * ay;
+    });
     const dmat2 M = {m00, m10, m01, m11};
     const dmat2 L = ddet(M) != 0.0 ? dinv(M) : dmat2{1.0, 0.0, 0.0, 1.0};
     const dmat2 H = dmul(dmat2{h00, h10, h01, h11}, L);
@@ -448,49 +419,44 @@ template <class G> __global__ void __launch_bounds__(kBlock) k_solid_force_mixed
     const float4 PL_i = d.s_PL[i], FL_i = d.s_FL[i];
     const float p_i = d.s_p[i];
     float2 couple = make_float2(0.f, 0.f), acc = make_float2(0.f, 0.f);
+    // fluid (couple) and solid (acc) neighbours feed separate sums, each in
+    // stencil order
     const int c = d.s_cell[i];
-    for (int n = 0; n < 9; ++n) {
-        const int m = neighbour_cell(c, n, nx, ny);
-        if (m < 0) continue;
-        const float2 sh = F::shift(p, fr, n);
-        const int2 rf = __ldg(&d.rng_f[m]);
-        for (int t = rf.x; t < rf.x + rf.y; ++t) {  // solidFluidCouple, solid.cu:211-255
-            const int j = __ldg(&d.lst_f[t]);
-            const float2 dx = sub2(F::f_nbr(d, j, sh), x_i);
-            if (!(sqn(dx) < R2)) continue;
-            const float kc = gw(p, sqn(dx) * hinv2);
-            const float p_j = __ldg(&d.f_p[j]);
-            const float cs = by_phase(p.sound_speed, __ldg(&d.f_phase[j]));
-            const float rho_j = __ldg(&d.f_rho[j]), rho_f = rho_j;
-            const float2 u_j = __ldg(&d.f_vel[j]);
-            float ps = fdiv(rho_f * p_j + rho_j * p_i, rho_f + rho_j);
-            float2 nn = sqn(dx) > 0.f ? make_float2(fdiv(dx.x, sqrtf(sqn(dx))), fdiv(dx.y, sqrtf(sqn(dx)))) : dx;
-            const float du = dot2(sub2(v_i, u_j), nn);
-            if (du >= 0.0f) ps += fdiv(rho_f * rho_j * du, rho_f + rho_j) * fminf(3.0f * du, cs);
-            const float am = fdiv(-2.0f * ps, rho_ref);
-            couple.x += am * dx.x * kc;
-            couple.y += am * dx.y * kc;
-        }
-        const int2 rs = __ldg(&d.rng_s[m]);
-        for (int t = rs.x; t < rs.x + rs.y; ++t) {  // solidSolidForce, solid.cu:257-305
-            const int j = __ldg(&d.lst_s[t]);
-            const float2 dX = ref_delta(p, rc_i, ro_i, __ldg(&d.s_rc[j]), __ldg(&d.s_roff[j]));
-            const float q = sqn(dX);
-            if (!(q < R2)) continue;
-            const float kc = gw(p, q * hinv2);
-            const float4 PL_j = __ldg(&d.s_PL[j]);
-            const float4 M = make_float4(PL_j.x + PL_i.x, PL_j.y + PL_i.y, PL_j.z + PL_i.z, PL_j.w + PL_i.w);
-            const float kr = kc * rinv;
-            acc.x += sum2(M.x, dX.x, M.z, dX.y) * kr;
-            acc.y += sum2(M.y, dX.x, M.w, dX.y) * kr;
-            const float2 dx = add2(dX, sub2(__ldg(&d.s_u[j]), u_i));
-            const float2 dv = sub2(__ldg(&d.s_v[j]), v_i);
-            const float nuv = hs * dot2(dv, dx) / (sqn(dx) + eps);
-            const float visc = sum2(alpha * nuv, cs_s, -beta * nuv, nuv) * kc;
-            acc.x += sum2(FL_i.x, dX.x, FL_i.z, dX.y) * visc;
-            acc.y += sum2(FL_i.y, dX.x, FL_i.w, dX.y) * visc;
-        }
-    }
+    for_each_in_stencil<true>(d.rng_f, c, nx, ny, [&](int t, int n) {  // solidFluidCouple, solid.cu:211-255
+        const int j = __ldg(&d.lst_f[t]);
+        const float2 dx = sub2(F::f_nbr(d, j, F::shift(p, fr, n)), x_i);
+        if (!(sqn(dx) < R2)) return;
+        const float kc = gw(p, sqn(dx) * hinv2);
+        const float p_j = __ldg(&d.f_p[j]);
+        const float cs = by_phase(p.sound_speed, __ldg(&d.f_phase[j]));
+        const float rho_j = __ldg(&d.f_rho[j]), rho_f = rho_j;
+        const float2 u_j = __ldg(&d.f_vel[j]);
+        float ps = fdiv(rho_f * p_j + rho_j * p_i, rho_f + rho_j);
+        float2 nn = sqn(dx) > 0.f ? make_float2(fdiv(dx.x, sqrtf(sqn(dx))), fdiv(dx.y, sqrtf(sqn(dx)))) : dx;
+        const float du = dot2(sub2(v_i, u_j), nn);
+        if (du >= 0.0f) ps += fdiv(rho_f * rho_j * du, rho_f + rho_j) * fminf(3.0f * du, cs);
+        const float am = fdiv(-2.0f * ps, rho_ref);
+        couple.x += am * dx.x * kc;
+        couple.y += am * dx.y * kc;
+    });
+    for_each_in_stencil<false>(d.rng_s, c, nx, ny, [&](int t, int) {  // solidSolidForce, solid.cu:257-305
+        const int j = __ldg(&d.lst_s[t]);
+        const float2 dX = ref_delta(p, rc_i, ro_i, __ldg(&d.s_rc[j]), __ldg(&d.s_roff[j]));
+        const float q = sqn(dX);
+        if (!(q < R2)) return;
+        const float kc = gw(p, q * hinv2);
+        const float4 PL_j = __ldg(&d.s_PL[j]);
+        const float4 M = make_float4(PL_j.x + PL_i.x, PL_j.y + PL_i.y, PL_j.z + PL_i.z, PL_j.w + PL_i.w);
+        const float kr = kc * rinv;
+        acc.x += sum2(M.x, dX.x, M.z, dX.y) * kr;
+        acc.y += sum2(M.y, dX.x, M.w, dX.y) * kr;
+        const float2 dx = add2(dX, sub2(__ldg(&d.s_u[j]), u_i));
+        const float2 dv = sub2(__ldg(&d.s_v[j]), v_i);
+        const float nuv = hs * dot2(dv, dx) / (sqn(dx) + eps);
+        const float visc = sum2(alpha * nuv, cs_s, -beta * nuv, nuv) * kc;
+        acc.x += sum2(FL_i.x, dX.x, FL_i.z, dX.y) * visc;
+        acc.y += sum2(FL_i.y, dX.x, FL_i.w, dX.y) * visc;
+    });
     d.s_couple[i] = couple;
     d.s_acc[i] = add2(acc, couple);
 }

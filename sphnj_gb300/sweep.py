@@ -1,10 +1,13 @@
 """Steps the scene sweep (cases.sweep_scene) as one batch and prints the time.
 
     python -m sphnj_gb300.sweep [--scenes N] [--form mixed|plain] [--warmup W] [--steps K]
+                                [--tile-h H | --autotune]
 
 Scenes 0..N-1 of the sweep are created in the chosen form and stepped
 together through sphnj_batch_step: W untimed steps, then K steps timed with
-CUDA events on the batch's stream.  It is the batched leg of `bench.py`'s
+CUDA events on the batch's stream.  --tile-h sets the cells per tile of
+the neighbour sweeps (16 by default); --autotune lets the batch's tuner
+choose the sweep configuration first and prints its choice.  It is the batched leg of `bench.py`'s
 sweep on its own, small enough to run under a profiler.
 """
 from __future__ import annotations
@@ -20,6 +23,8 @@ def main(argv=None) -> None:
     ap.add_argument("--form", choices=["mixed", "plain"], default="mixed")
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--steps", type=int, default=2)
+    ap.add_argument("--tile-h", type=int, default=16)
+    ap.add_argument("--autotune", action="store_true")
     args = ap.parse_args(argv)
     import torch
 
@@ -36,6 +41,9 @@ def main(argv=None) -> None:
     stream = torch.cuda.Stream()
     with Batch(sims) as b:
         b.set_stream(stream.cuda_stream)
+        b.set_tiling(True, args.tile_h)
+        if args.autotune:
+            print("autotune:", b.autotune())
         b.step(args.warmup)
         b.synchronize()
         e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
