@@ -2,10 +2,10 @@
 // its own arena, uploaded and downloaded on its own) advanced together.
 //
 // Every stage of a step is ONE launch over all scenes of the batch: a block
-// finds its scene in a per-launch block table (scene k owns blocks first[k]
-// .. first[k+1]-1, in proportion to its own particle / cell / tile counts)
-// and reads the scene's record - parameters, state pointers, cell lists and
-// scratch - from device memory.  So a batch of 256 small scenes costs the
+// finds its scene in a per-launch block table (scene k owns a run of
+// consecutive blocks, in proportion to its own particle / cell / tile
+// counts; one 16-byte entry per block) and reads the scene's record -
+// parameters, state pointers, cell lists and scratch - from device memory.  So a batch of 256 small scenes costs the
 // same ~30 launches per step as one large scene, every launch fills the GPU,
 // and scenes of uneven size share it in proportion to their work.  Each kind
 // of step is captured once as a CUDA graph and replayed.

@@ -263,30 +263,25 @@ struct One {
     }
 };
 
-// Many: one launch over many scenes.  Scene k owns the blocks
-// first[k] <= b < first[k + 1]; first[n] is the grid size, and a scene with
-// no work for this launch owns no block.  The block copies its scene's record
-// into shared memory, so that the kernel reads its fields with shared loads
-// at fixed addresses (as a one-scene launch reads them from parameter space)
-// rather than holding global addresses in registers.
+// Many: one launch over many scenes.  Each scene owns a run of consecutive
+// blocks (a scene with no work for this launch owns none); the launch's block
+// table gives block b its scene, its index within the scene's run and the
+// run's length in one 16-byte entry, so a block finds its scene with one
+// load.  The block copies its scene's record into shared memory, so that the
+// kernel reads its fields with shared loads at fixed addresses (as a
+// one-scene launch reads them from parameter space) rather than holding
+// global addresses in registers.
 struct Many {
     const Scene *scenes;
-    const int *first;  // [n + 1]
+    const int4 *blocks;  // [grid size]: {scene, blk, nblk, 0}
     int n;
     __device__ __forceinline__ const Scene *locate(int &blk, int &nblk) const {
         __shared__ __align__(16) Scene s_scene;
         static_assert(sizeof(Scene) % 16 == 0, "the record is copied in 16-byte words");
-        const int b = blockIdx.x;
-        int lo = 0, hi = n;  // first[lo] <= b < first[hi]
-        while (hi - lo > 1) {
-            const int mid = (lo + hi) >> 1;
-            if (__ldg(&first[mid]) <= b) lo = mid;
-            else hi = mid;
-        }
-        const int f0 = __ldg(&first[lo]);
-        blk = b - f0;
-        nblk = __ldg(&first[lo + 1]) - f0;
-        const int4 *src = reinterpret_cast<const int4 *>(scenes + lo);
+        const int4 t = __ldg(&blocks[blockIdx.x]);
+        blk = t.y;
+        nblk = t.z;
+        const int4 *src = reinterpret_cast<const int4 *>(scenes + t.x);
         int4 *dst = reinterpret_cast<int4 *>(&s_scene);
         for (int w = threadIdx.x; w < (int)(sizeof(Scene) / 16); w += blockDim.x) dst[w] = __ldg(&src[w]);
         __syncthreads();

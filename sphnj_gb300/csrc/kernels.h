@@ -6,9 +6,10 @@
 //   GroupOne   one scene; its record travels as a kernel parameter.
 //   GroupMany  a batch of independent scenes advanced by the same launches:
 //              the records live in device memory and each launch gets a
-//              per-scene block table (scene k owns blocks first[k] ..
-//              first[k+1]-1), so one launch covers every scene and a scene
-//              with no work for it owns no block.
+//              block table (scene k owns a run of consecutive blocks; each
+//              block's entry names its scene and its place in the run), so
+//              one launch covers every scene and a scene with no work for it
+//              owns no block.
 #pragma once
 
 #include <cuda_runtime.h>
@@ -79,7 +80,7 @@ struct GroupMany {
     // sequence is planned once before it is captured into a graph.
     bool planning = false;
     struct Table {
-        int *first;
+        int4 *blocks;  // per block: {scene, index within the scene's run, run length, 0}
         unsigned total;
     };
     std::map<long long, Table> tables;
@@ -91,23 +92,29 @@ struct GroupMany {
                 if (error == cudaSuccess) error = cudaErrorNotReady;  // launch not planned
                 return false;
             }
-            std::vector<int> first((size_t)n + 1, 0);
+            std::vector<unsigned> run((size_t)n, 0u);
             long long acc = 0;
             for (int k = 0; k < n; ++k) {
-                first[k] = (int)acc;
-                acc += blocks_of(h_scenes[k]);
+                run[k] = blocks_of(h_scenes[k]);
+                acc += run[k];
             }
-            first[n] = (int)acc;
             Table t{nullptr, (unsigned)acc};
             if (acc > 0x7fffffffLL) {
                 error = cudaErrorInvalidValue;
                 return false;
             }
-            cudaError_t e = cudaMalloc(&t.first, sizeof(int) * first.size());
-            if (e == cudaSuccess) e = cudaMemcpy(t.first, first.data(), sizeof(int) * first.size(),
-                                                 cudaMemcpyHostToDevice);
+            cudaError_t e = cudaSuccess;
+            if (acc > 0) {
+                std::vector<int4> table((size_t)acc);
+                size_t b = 0;
+                for (int k = 0; k < n; ++k)
+                    for (unsigned j = 0; j < run[k]; ++j) table[b++] = make_int4(k, (int)j, (int)run[k], 0);
+                e = cudaMalloc(&t.blocks, sizeof(int4) * table.size());
+                if (e == cudaSuccess)
+                    e = cudaMemcpy(t.blocks, table.data(), sizeof(int4) * table.size(), cudaMemcpyHostToDevice);
+            }
             if (e != cudaSuccess) {
-                if (t.first) cudaFree(t.first);
+                if (t.blocks) cudaFree(t.blocks);
                 error = e;
                 return false;
             }
@@ -116,7 +123,7 @@ struct GroupMany {
         if (planning) return false;
         blocks = it->second.total;
         dev.scenes = d_scenes + (exchanged ? n : 0);
-        dev.first = it->second.first;
+        dev.blocks = it->second.blocks;
         dev.n = n;
         return blocks > 0;
     }
@@ -126,7 +133,8 @@ struct GroupMany {
         return false;
     }
     void free_tables() {
-        for (auto &t : tables) cudaFree(t.second.first);
+        for (auto &t : tables)
+            if (t.second.blocks) cudaFree(t.second.blocks);
         tables.clear();
     }
 };
