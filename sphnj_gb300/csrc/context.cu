@@ -443,8 +443,13 @@ int sphnj_upload(sphnj_ctx *ctx, const sphnj_host_state *s) {
     bind_lists(ctx);
     // wall normals once before the loop (virtNormalCalculation, calculation.cu:28)
     GroupOne g{scene_of(ctx, ctx->parity), ctx->form};
-    if (s->virt_normal) RET(h2d(ctx, d.v_normal, s->virt_normal, nv));
-    else launch_virt_normal(st, g);
+    if (s->virt_normal) {
+        RET(h2d(ctx, d.v_normal, s->virt_normal, nv));
+    } else if (nv > 0) {
+        launch_virt_normal(st, g);
+        // the virtual lists it built go: the step starts from empty lists
+        CK(cudaMemsetAsync(ctx->lv.rng, 0, sizeof(int2) * C, st));
+    }
     // mixed form: cells + offsets, displacements and compensations
     if (ctx->form == SPHNJ_FORM_MIXED) launch_mixed_split(st, g, 7);
     CK(cudaGetLastError());

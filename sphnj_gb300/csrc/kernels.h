@@ -37,7 +37,7 @@ enum Site : int {
     SITE_REBUILD_CELLS, SITE_REBUILD_TILES, SITE_REBUILD_ONE, SITE_CAPACITY, SITE_COUPLE, SITE_VIRT_NORMAL,
     SITE_VIRT_DATA, SITE_PAIR_TILED, SITE_PAIR_EACH, SITE_PAIR_FALLBACK, SITE_FLUID_UPDATE, SITE_SOLID_DEFORM,
     SITE_SOLID_FORCE, SITE_SOLID_UPDATE, SITE_SHIFT_TILED, SITE_SHIFT_EACH, SITE_SHIFT_FALLBACK,
-    SITE_SHIFT_COPY_BACK, SITE_TILE_COMPACT, SITE_TILE_SUMS, SITE_TILE_SCATTER
+    SITE_SHIFT_COPY_BACK, SITE_TILE_COMPACT, SITE_TILE_SUMS, SITE_TILE_SCATTER, SITE_VIRT_BIN
 };
 inline long long site_key(int site, int arg = 0) { return ((long long)site << 32) | (unsigned)arg; }
 
@@ -177,6 +177,11 @@ template <class G> int launch_bin(cudaStream_t st, G &g, bool with_virt);
 // buffer `parity` (sort.cu:10-137)
 template <class G> int launch_sort_kind(cudaStream_t st, G &g, Kind k, int parity);
 
+// cell ids of the virtual particles and their per-cell index lists in
+// ascending order (ranges in lv.rng, indices in the sort scratch sc.sorted),
+// the arrays left in their order: the lists of the wall normals at upload
+template <class G> int launch_virt_index(cudaStream_t st, G &g);
+
 // incremental cell-list rebuild of one kind from list buffer parity ^ 1 into
 // list buffer `parity` (pair.cu:66-181)
 template <class G> int launch_rebuild_kind(cudaStream_t st, G &g, Kind k, int parity);
@@ -203,7 +208,9 @@ template <class G> int launch_fluid_update(cudaStream_t st, G &g);
 template <class G> int launch_shift_pass(cudaStream_t st, G &g, const TileConfig &tc, int pass);
 template <class G> int launch_shift_copy_back(cudaStream_t st, G &g);
 
-// virtual particles (virt.cu)
+// virtual particles (virt.cu).  launch_virt_normal builds the per-cell index
+// lists it reads (launch_virt_index: v_cell, lv.rng and the sort scratch);
+// the caller empties lv.rng again where the step expects empty lists.
 template <class G> int launch_virt_normal(cudaStream_t st, G &g);
 template <class G> int launch_virt_data(cudaStream_t st, G &g);
 

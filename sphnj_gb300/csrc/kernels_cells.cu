@@ -638,7 +638,27 @@ template <class G> int launch_bin(cudaStream_t st, G &g, bool with_virt) {
         k_bin<typename G::Dev>, kBlock, 0, st, with_virt ? 1 : 0);
 }
 
-template <class G> int launch_sort_kind(cudaStream_t st, G &g, Kind k, int parity) {
+// Cell ids of the virtual particles from their positions (the virtual part
+// of k_bin, with its out-of-grid check), for the cell lists of the wall
+// normals at upload.
+template <class G> __global__ void __launch_bounds__(kBlock) k_virt_bin(const __grid_constant__ G g) {
+    SPHNJ_SCENE(g);
+    const int i = blk * blockDim.x + threadIdx.x;
+    if (i >= p.virt_number) return;
+    const float2 x = d.v_pos[i];
+    int c = cell_of(p, x.x, x.y);
+    if (c < 0 || c >= p.cell_number_total) {
+        raise_error(d.err, SPHNJ_ERR_OUT_OF_GRID, 2, i, c);
+        c = c < 0 ? 0 : p.cell_number_total - 1;
+    }
+    d.v_cell[i] = c;
+}
+
+// Per-cell lists of kind k, the particle arrays not reordered: cell c's
+// particle indices in ascending order at sc.sorted[r.x .. r.x + r.y), r the
+// cell's range in list buffer `parity` (the sort's first stages; the list
+// entries themselves are written by the gathers that follow in a sort).
+template <class G> int launch_index_kind(cudaStream_t st, G &g, Kind k, int parity) {
     using D = typename G::Dev;
     auto has = [k](const Scene &s) { return count_of(s.p, k) > 0; };
     auto cells = [&](const Scene &s) { return has(s) ? grid_for(s.p.cell_number_total, kBlock) : 0u; };
@@ -654,6 +674,22 @@ template <class G> int launch_sort_kind(cudaStream_t st, G &g, Kind k, int parit
     n += launch(g, site_key(SITE_SORT_ONE, ki), one, k_scan_sums<D>, 1024, 0, st, k == KF ? 1 : 0, 0);
     n += launch(g, site_key(SITE_SORT_N, ki), parts, k_bucket<D>, kBlock, 0, st, ki);
     n += launch(g, site_key(SITE_SORT_CELLS32, ki), warps, k_cellsort<D>, kBlock, 0, st, ki, parity);
+    return n;
+}
+
+template <class G> int launch_virt_index(cudaStream_t st, G &g) {
+    int n = launch(
+        g, site_key(SITE_VIRT_BIN), [](const Scene &s) { return grid_for(s.p.virt_number, kBlock); },
+        k_virt_bin<typename G::Dev>, kBlock, 0, st);
+    return n + launch_index_kind(st, g, KV, 0);
+}
+
+template <class G> int launch_sort_kind(cudaStream_t st, G &g, Kind k, int parity) {
+    using D = typename G::Dev;
+    auto has = [k](const Scene &s) { return count_of(s.p, k) > 0; };
+    auto parts = [&](const Scene &s) { return has(s) ? grid_for(count_of(s.p, k), kBlock) : 0u; };
+    const int ki = (int)k;
+    int n = launch_index_kind(st, g, k, parity);
     if (k == KF) {
         n += launch(g, site_key(SITE_SORT_N, ki), parts, k_gather_fluid<D>, kBlock, 0, st, parity);
         n += launch(g, site_key(SITE_SORT_N, ki), parts, k_scatter_back_fluid<D>, kBlock, 0, st);
@@ -709,6 +745,7 @@ template <class G> int launch_capacity_check(cudaStream_t st, G &g) {
 
 SPHNJ_INSTANTIATE_GROUPS(launch_bin, bool);
 SPHNJ_INSTANTIATE_GROUPS(launch_sort_kind, Kind, int);
+SPHNJ_INSTANTIATE_GROUPS(launch_virt_index);
 SPHNJ_INSTANTIATE_GROUPS(launch_rebuild_kind, Kind, int);
 SPHNJ_INSTANTIATE_GROUPS(launch_capacity_check);
 SPHNJ_INSTANTIATE_GROUPS(launch_tile_compact, int, bool);

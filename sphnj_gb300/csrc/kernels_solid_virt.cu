@@ -2,9 +2,9 @@
 // virtual/fluid FP32, solid state FP64 with FP32 kernel weights
 // (include/particle.cuh:104-115, solid.cu:18-19,271-272).
 //
-//   k_virt_normal      getVirtNormal (virt.cu:8-48): O(N_v^2) wall normals
-//                      in index order (setup only), tiles of positions
-//                      staged in shared memory.
+//   k_virt_normal      getVirtNormal (virt.cu:8-48): wall normals (setup
+//                      only), the reference's index-order sum over the
+//                      per-cell lists of the nine stencil cells.
 //   k_virt_data        getVirtData + virtDataCalculate (virt.cu:61-149)
 //   k_solid_couple     solidCoupleUpdate (solid.cu:355-444)
 //   k_solid_deform     solidDeformationCalculate (solid.cu:7-23,169-209)
@@ -29,30 +29,57 @@ __device__ __forceinline__ float sw(const sphnj_params &p, float q2) {
 }
 __device__ __forceinline__ float by_phase(const float (&a)[2], int ph) { return ph ? a[1] : a[0]; }
 
-template <class G> __global__ void __launch_bounds__(256) k_virt_normal(const __grid_constant__ G g) {
+// The reference sums over every virtual particle j in index order, those
+// within the cutoff contributing.  All of them lie in the nine cells around
+// particle i (cells are at least a cutoff wide), and each cell's particles
+// are listed in ascending index order (launch_virt_index: ranges in lv.rng,
+// indices in the sort scratch sc.sorted), so a nine-way merge of those lists
+// visits the same j in the same order: the same sum, from about a hundred
+// candidates instead of N_v.
+template <class G> __global__ void __launch_bounds__(kBlock) k_virt_normal(const __grid_constant__ G g) {
     SPHNJ_SCENE(g);
-    __shared__ float2 tile[256];
-    const int nv = p.virt_number;
     const int i = blk * blockDim.x + threadIdx.x;
+    if (i >= p.virt_number) return;
+    const int nx = p.cell_number[0], ny = p.cell_number[1];
     const float R2 = p.impact_distance_square, hinv2 = p.smoothing_length_inverse_square;
-    const float2 x_i = i < nv ? d.v_pos[i] : make_float2(0.f, 0.f);
-    float2 nrm = make_float2(0.f, 0.f);
-    for (int base = 0; base < nv; base += 256) {
-        const int idx = base + threadIdx.x;
-        tile[threadIdx.x] = idx < nv ? d.v_pos[idx] : make_float2(0.f, 0.f);
-        __syncthreads();
-        const int cnt = min(256, nv - base);
-        for (int t = 0; t < cnt; ++t) {
-            const float2 dx = sub2(tile[t], x_i);
-            if (sqn(dx) < R2) {
-                const float kc = gw(p, sqn(dx) * hinv2);
-                nrm.x -= dx.x * kc;
-                nrm.y -= dx.y * kc;
-            }
-        }
-        __syncthreads();
+    const float2 x_i = d.v_pos[i];
+    const int2 *rng = S.lv.rng;
+    const int *lst = S.sc.sorted;
+    const int c = d.v_cell[i];
+    constexpr int kDone = 0x7fffffff;
+    int cur[9], end[9], head[9];  // per stencil cell: next slot, end slot, index at the next slot
+#pragma unroll
+    for (int n = 0; n < 9; ++n) {
+        const int m = neighbour_cell(c, n, nx, ny);
+        const int2 r = m >= 0 ? __ldg(&rng[m]) : make_int2(0, 0);
+        cur[n] = r.x;
+        end[n] = r.x + r.y;
+        head[n] = cur[n] < end[n] ? __ldg(&lst[cur[n]]) : kDone;
     }
-    if (i < nv) d.v_normal[i] = sqrtf(sqn(nrm)) < EPS_FOR_SUM ? make_float2(0.f, 0.f) : normalized(nrm);
+    float2 nrm = make_float2(0.f, 0.f);
+    for (;;) {
+        int j = kDone, nj = 0;
+#pragma unroll
+        for (int n = 0; n < 9; ++n)
+            if (head[n] < j) {
+                j = head[n];
+                nj = n;
+            }
+        if (j == kDone) break;
+        const float2 dx = sub2(__ldg(&d.v_pos[j]), x_i);
+        if (sqn(dx) < R2) {
+            const float kc = gw(p, sqn(dx) * hinv2);
+            nrm.x -= dx.x * kc;
+            nrm.y -= dx.y * kc;
+        }
+#pragma unroll
+        for (int n = 0; n < 9; ++n)  // advance the cell j came from (unrolled: the arrays stay in registers)
+            if (n == nj) {
+                ++cur[n];
+                head[n] = cur[n] < end[n] ? __ldg(&lst[cur[n]]) : kDone;
+            }
+    }
+    d.v_normal[i] = sqrtf(sqn(nrm)) < EPS_FOR_SUM ? make_float2(0.f, 0.f) : normalized(nrm);
 }
 
 template <class G, class F> __global__ void __launch_bounds__(kBlock) k_virt_data(const __grid_constant__ G g) {
@@ -496,9 +523,10 @@ template <class G> __global__ void __launch_bounds__(256) k_solid_update_mixed(c
 
 
 template <class G> int launch_virt_normal(cudaStream_t st, G &g) {
-    return launch(
-        g, site_key(SITE_VIRT_NORMAL), [](const Scene &s) { return grid_for(s.p.virt_number, 256); },
-        k_virt_normal<typename G::Dev>, 256, 0, st);
+    const int n = launch_virt_index(st, g);
+    return n + launch(
+                   g, site_key(SITE_VIRT_NORMAL), [](const Scene &s) { return grid_for(s.p.virt_number, kBlock); },
+                   k_virt_normal<typename G::Dev>, kBlock, 0, st);
 }
 template <class G> int launch_virt_data(cudaStream_t st, G &g) {
     using D = typename G::Dev;
