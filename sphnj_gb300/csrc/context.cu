@@ -192,6 +192,7 @@ size_t layout(sphnj_ctx *ctx, char *base) {
         d.s_v = a.take<float2>(ns); d.s_vc = a.take<float2>(ns); d.s_off = a.take<float2>(ns);
         d.s_acc = a.take<float2>(ns);
         d.s_PL = a.take<float4>(ns); d.s_FL = a.take<float4>(ns);
+        d.s_nbr = a.take<int>((size_t)kSolidNbrCap * ns); d.s_nbr_cnt = a.take<uint8_t>(ns);
         d.v_off = a.take<float2>(nv);
     }
     ctx->sc.cnt9 = a.take<int>((size_t)9 * C);

@@ -95,6 +95,12 @@ struct DevState {
     int2 *s_rc;
     float2 *s_roff, *s_u, *s_uc, *s_v, *s_vc, *s_off, *s_acc;
     float4 *s_PL, *s_FL;  // P L and F L of the last deformation pass (FP32, column-major)
+    // per solid particle, the solid neighbours that passed the deformation
+    // pass's reference-distance test, in its order (the force pass visits
+    // the same ones): entry k of particle i at s_nbr[k ns + i], their number
+    // in s_nbr_cnt (kNbrNone: more than kSolidNbrCap, walk the stencil)
+    int *s_nbr;
+    uint8_t *s_nbr_cnt;
     float2 *v_off;
 };
 
@@ -207,6 +213,7 @@ constexpr int kMaskShifts = 32;       // shifting passes tracked by disp2_bits
 constexpr float kSkin = 0.05f;        // list radius = cutoff * (1 + kSkin)
 constexpr int kNbrCap = 64;           // neighbour-list entries per particle
 constexpr int kNbrChunks = kNbrCap / 8;  // 16-byte chunks per list
+constexpr int kSolidNbrCap = 64;      // listed solid neighbours per solid particle (mixed form)
 constexpr uint8_t kNbrNone = 0xFF;
 constexpr float EPS_FOR_SUM = 0.1f;   // global.h:6
 constexpr float LARGE_FLOAT = 1.0E6f; // global.h:7

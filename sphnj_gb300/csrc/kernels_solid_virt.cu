@@ -384,11 +384,15 @@ template <class G> __global__ void __launch_bounds__(kBlock) k_solid_deform_mixe
     const int2 rc_i = d.s_rc[i];
     const float2 ro_i = d.s_roff[i], u_i = d.s_u[i];
     float h00 = 0.f, h10 = 0.f, h01 = 0.f, h11 = 0.f, m00 = 0.f, m10 = 0.f, m01 = 0.f, m11 = 0.f;
+    const int ns = p.solid_number;
+    int listed = 0;  // the neighbours that pass, recorded for the force pass
     for_each_in_stencil<false>(d.rng_s, d.s_cell[i], nx, ny, [&](int t, int) {
         const int j = __ldg(&d.lst_s[t]);
         const float2 dX = ref_delta(p, rc_i, ro_i, __ldg(&d.s_rc[j]), __ldg(&d.s_roff[j]));
         const float q = sqn(dX);
         if (!(q < R2)) return;
+        if (listed < kSolidNbrCap) d.s_nbr[(size_t)listed * ns + i] = j;
+        ++listed;
         const float kc = gw(p, q * hinv2);
         const float2 du = sub2(__ldg(&d.s_u[j]), u_i);
         const float ax = dX.x * kc, ay = dX.y * kc;
@@ -401,6 +405,7 @@ template <class G> __global__ void __launch_bounds__(kBlock) k_solid_deform_mixe
         m01 += dX.x * ay;
         m11 += dX.y * ay;
     });
+    d.s_nbr_cnt[i] = listed <= kSolidNbrCap ? (uint8_t)listed : kNbrNone;
     const dmat2 M = {m00, m10, m01, m11};
     const dmat2 L = ddet(M) != 0.0 ? dinv(M) : dmat2{1.0, 0.0, 0.0, 1.0};
     const dmat2 H = dmul(dmat2{h00, h10, h01, h11}, L);
@@ -466,8 +471,7 @@ template <class G> __global__ void __launch_bounds__(kBlock) k_solid_force_mixed
         couple.x += am * dx.x * kc;
         couple.y += am * dx.y * kc;
     });
-    for_each_in_stencil<false>(d.rng_s, c, nx, ny, [&](int t, int) {  // solidSolidForce, solid.cu:257-305
-        const int j = __ldg(&d.lst_s[t]);
+    auto solid_pair = [&](int j) {  // solidSolidForce, solid.cu:257-305
         const float2 dX = ref_delta(p, rc_i, ro_i, __ldg(&d.s_rc[j]), __ldg(&d.s_roff[j]));
         const float q = sqn(dX);
         if (!(q < R2)) return;
@@ -483,7 +487,18 @@ template <class G> __global__ void __launch_bounds__(kBlock) k_solid_force_mixed
         const float visc = sum2(alpha * nuv, cs_s, -beta * nuv, nuv) * kc;
         acc.x += sum2(FL_i.x, dX.x, FL_i.z, dX.y) * visc;
         acc.y += sum2(FL_i.y, dX.x, FL_i.w, dX.y) * visc;
-    });
+    };
+    // The solid neighbours this sub-step's deformation pass accepted, in its
+    // (stencil) order: each thread loops over its own ~40 rather than testing
+    // ~117 candidates with most lanes masked off; the cutoff test repeats on
+    // the same inputs, so the sum is the stencil walk's.
+    const int listed = d.s_nbr_cnt[i];
+    if (listed != kNbrNone) {
+        const int ns = p.solid_number;
+        for (int k = 0; k < listed; ++k) solid_pair(__ldg(&d.s_nbr[(size_t)k * ns + i]));
+    } else {
+        for_each_in_stencil<false>(d.rng_s, c, nx, ny, [&](int t, int) { solid_pair(__ldg(&d.lst_s[t])); });
+    }
     d.s_couple[i] = couple;
     d.s_acc[i] = add2(acc, couple);
 }
