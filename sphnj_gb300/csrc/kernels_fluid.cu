@@ -47,38 +47,47 @@ namespace sphnj {
 namespace {
 
 constexpr int kPairBlock = 128;
-constexpr int kTileBlock = 256;  // tiled sweeps: ~208 particles per 16-cell tile
-constexpr int kListBlock = 128;  // shifting passes over an active-tile list
+constexpr int kTileBlock = 256;   // tiled sweeps: ~208 particles per 16-cell tile
+constexpr int kListBlock = 128;   // shifting passes over an active-tile list
+constexpr int kDenseBlock = 128;  // shifting passes of a dense scene, one block per tile
 
-// Block shape of the pair pass.  One-scene launches: 256 threads, 5 blocks per
-// SM (48 registers, no spills; unbounded it takes 64 and 4 blocks).  Batched
-// launches over tile lists: 128 threads (partly filled tiles leave fewer warps
-// waiting at the tile's barriers), 8 per SM where their staging fits
-// (pair_per_cell).  256-scene mixed sweep: 4.56 -> 4.46 ms/step.
-template <class G> struct PairShape {
-    static constexpr int threads = 256, min_blocks = 5;
-};
-template <> struct PairShape<GroupMany> {
+// Block shape of the pair pass, by launch:
+//  - a dense scene swept alone (one block per tile) and batches (tile
+//    lists): 128 threads, 8 blocks per SM (64 registers, no spills), staging
+//    sized by pair_per_cell so that the 8 fit.  Smaller blocks leave fewer
+//    warps waiting at a tile's barriers.  256-scene mixed sweep 4.56 -> 4.46
+//    ms/step; 4.15M dam break 3.80 -> 3.74 (against 256 threads, 5 per SM);
+//  - a sparse scene swept alone (tile list): 256 threads, 5 per SM (48
+//    registers; unbounded it takes 64 and 4 blocks).
+template <class G, bool kList> struct PairShape {
     static constexpr int threads = 128, min_blocks = 8;
+};
+template <> struct PairShape<GroupOne, true> {
+    static constexpr int threads = 256, min_blocks = 5;
 };
 constexpr int kMaxPerCell = 24;  // staged particles per cell at most
 
 // Particles per cell the pair pass stages (a tile with more falls back to the
-// unstaged sweep, without lists).  A scene swept alone: kMaxPerCell.  A batch:
-// 1.2 times the lattice count (cell area / particle area) of its densest
-// scene, at least 8, so that a typical batch's staging lets 7 or 8 blocks
-// share an SM (13 to 13.5 per cell at h = 1.2 dx: 16 or 17, 25 to 27 KB a
-// block; a 16-cell tile stages about 700 of its 864 to 918 entries).
-inline int pair_per_cell(const GroupOne &) { return kMaxPerCell; }
-inline int pair_per_cell(const GroupMany &g) {
+// unstaged sweep, without lists): 1.2 times the lattice count (cell area /
+// particle area), at least 8 - of the scene, or of a batch's densest scene -
+// so that 7 or 8 blocks share an SM (13 to 13.5 per cell at h = 1.2 dx: 16
+// or 17, 25 to 27 KB a block; a 16-cell tile stages about 700 of its 864 to
+// 918 entries).  A sparse scene swept alone stages kMaxPerCell.
+inline double lattice_per_cell(const sphnj_params &p) {
+    if (p.fluid_number_total <= 0 || !(p.particle_diameter > 0.0f)) return 0.0;
+    const double dx = p.particle_diameter;
+    return (double)p.interval[0] * p.interval[1] / (dx * dx);
+}
+inline int staged_per_cell(double lattice) {
+    return std::min(kMaxPerCell, std::max(8, (int)std::ceil(1.2 * lattice)));
+}
+inline int pair_per_cell(const GroupOne &g, bool list) {
+    return list ? kMaxPerCell : staged_per_cell(lattice_per_cell(g.s.p));
+}
+inline int pair_per_cell(const GroupMany &g, bool) {
     double most = 0.0;
-    for (int k = 0; k < g.n; ++k) {
-        const sphnj_params &p = g.h_scenes[k].p;
-        if (p.fluid_number_total <= 0 || !(p.particle_diameter > 0.0f)) continue;
-        const double dx = p.particle_diameter;
-        most = std::max(most, (double)p.interval[0] * p.interval[1] / (dx * dx));
-    }
-    return std::min(kMaxPerCell, std::max(8, (int)std::ceil(1.2 * most)));
+    for (int k = 0; k < g.n; ++k) most = std::max(most, lattice_per_cell(g.h_scenes[k].p));
+    return staged_per_cell(most);
 }
 constexpr int kBlock = 256;
 constexpr int kFallbackBlocks = 304;  // 2 x 152 SMs, grid-stride
@@ -838,10 +847,10 @@ __global__ void __launch_bounds__(kThreads, kMinBlocks)
 // then its position update (shift_update_particle) by the same thread.
 // kThreads per block at full occupancy, 32 registers (a small spill): 32
 // registers at 8 blocks of 256 measured 4% faster than 40 at 6.  Batched
-// launches over the active-tile lists use blocks of kListBlock threads: their
-// tiles are often partly filled, and a smaller block leaves fewer warps
+// launches over the active-tile lists and dense scenes use blocks of 128
+// threads (kListBlock, kDenseBlock): a smaller block leaves fewer warps
 // waiting at the tile's barriers while the others work (256-scene mixed
-// sweep: 4.81 -> 4.52 ms/step).
+// sweep: 4.81 -> 4.52 ms/step; 4.15M dam break: 3.92 -> 3.80).
 template <class G, class F, bool kList, int kThreads>
 __global__ void __launch_bounds__(kThreads, 2048 / kThreads)
     k_shift_gradient_tiled(const __grid_constant__ G gs, int tile_h, int cap, int pass) {
@@ -1026,18 +1035,20 @@ constexpr size_t kPairSmemPerEntry = 3 * sizeof(float2) + sizeof(int) + 1;
 }  // namespace
 
 cudaError_t configure_sweeps(const TileConfig &tc) {
-    using P1 = PairShape<GroupOne>;
-    using PM = PairShape<GroupMany>;
-    // dynamic shared memory above 48 KB needs an opt-in
+    using PD = PairShape<GroupOne, false>;
+    using PL = PairShape<GroupOne, true>;
+    using PM = PairShape<GroupMany, true>;
+    // dynamic shared memory above 48 KB needs an opt-in (every launch stages
+    // at most kMaxPerCell per cell)
     const int a = cudaFuncAttributeMaxDynamicSharedMemorySize;
-    const size_t smem1 = tile_cap(tc.tile_h, kMaxPerCell) * kPairSmemPerEntry, smemM = smem1;
+    const size_t smem = tile_cap(tc.tile_h, kMaxPerCell) * kPairSmemPerEntry;
     const std::pair<const void *, size_t> kernels[] = {
-        {(const void *)k_fluid_pair_tiled<One, FormPlain, false, P1::threads, P1::min_blocks>, smem1},
-        {(const void *)k_fluid_pair_tiled<One, FormPlain, true, P1::threads, P1::min_blocks>, smem1},
-        {(const void *)k_fluid_pair_tiled<One, FormMixed, false, P1::threads, P1::min_blocks>, smem1},
-        {(const void *)k_fluid_pair_tiled<One, FormMixed, true, P1::threads, P1::min_blocks>, smem1},
-        {(const void *)k_fluid_pair_tiled<Many, FormPlain, true, PM::threads, PM::min_blocks>, smemM},
-        {(const void *)k_fluid_pair_tiled<Many, FormMixed, true, PM::threads, PM::min_blocks>, smemM}};
+        {(const void *)k_fluid_pair_tiled<One, FormPlain, false, PD::threads, PD::min_blocks>, smem},
+        {(const void *)k_fluid_pair_tiled<One, FormPlain, true, PL::threads, PL::min_blocks>, smem},
+        {(const void *)k_fluid_pair_tiled<One, FormMixed, false, PD::threads, PD::min_blocks>, smem},
+        {(const void *)k_fluid_pair_tiled<One, FormMixed, true, PL::threads, PL::min_blocks>, smem},
+        {(const void *)k_fluid_pair_tiled<Many, FormPlain, true, PM::threads, PM::min_blocks>, smem},
+        {(const void *)k_fluid_pair_tiled<Many, FormMixed, true, PM::threads, PM::min_blocks>, smem}};
     for (const auto &k : kernels) {
         if (k.second <= 48 * 1024) continue;
         const cudaError_t e = cudaFuncSetAttribute(k.first, (cudaFuncAttribute)a, (int)k.second);
@@ -1070,24 +1081,31 @@ template <class F, class G> int fluid_pair(cudaStream_t st, G &g, const TileConf
         return launch(
             g, site_key(SITE_PAIR_EACH), [](const Scene &s) { return grid_for(s.p.fluid_number_total, kPairBlock); },
             k_fluid_pair_each<D, F>, kPairBlock, 0, st, 0);
-    using Shape = PairShape<G>;
-    const int cap = tile_cap(tc.tile_h, pair_per_cell(g));
+    const bool list = use_tile_list(g, tc.tile_h);
+    const int cap = tile_cap(tc.tile_h, pair_per_cell(g, list));
     const size_t smem = cap * kPairSmemPerEntry;
     // this step's active tiles (the cell lists are final), used by the pair
     // pass and every shifting pass of the step
     int n = launch_tile_compact(st, g, tc.tile_h, std::is_same<G, GroupMany>::value);
+    // list launches: about one block per tile the fluid can fill, twice that
+    // at 128 threads; a dense scene: one block per tile
     auto blocks = [&](const Scene &s) {
         return std::min<unsigned>(tile_blocks(s.p, tc.tile_h),
-                                  sweep_blocks(s.p, tc.tile_h) * (kTileBlock / Shape::threads));
+                                  sweep_blocks(s.p, tc.tile_h) * (kTileBlock / PairShape<G, true>::threads));
     };
     const int lists = tc.lists ? 1 : 0;
     const long long key = site_key(SITE_PAIR_TILED, tc.tile_h);
-    if (use_tile_list(g, tc.tile_h))
+    if (list) {
+        using Shape = PairShape<G, true>;
         n += launch(g, key, blocks, k_fluid_pair_tiled<D, F, true, Shape::threads, Shape::min_blocks>, Shape::threads,
                     smem, st, tc.tile_h, cap, lists);
-    else if constexpr (!std::is_same<G, GroupMany>::value)  // batches always sweep their lists
-        n += launch(g, key, blocks, k_fluid_pair_tiled<D, F, false, Shape::threads, Shape::min_blocks>, Shape::threads,
-                    smem, st, tc.tile_h, cap, lists);
+    } else if constexpr (!std::is_same<G, GroupMany>::value) {  // batches always sweep their lists
+        using Shape = PairShape<G, false>;
+        n += launch(
+            g, key, [&](const Scene &s) { return tile_blocks(s.p, tc.tile_h); },
+            k_fluid_pair_tiled<D, F, false, Shape::threads, Shape::min_blocks>, Shape::threads, smem, st, tc.tile_h,
+            cap, lists);
+    }
     n += launch(
         g, site_key(SITE_PAIR_FALLBACK), [](const Scene &s) { return fallback_blocks(s.p.fluid_number_total); },
         k_fluid_pair_each<D, F>, kPairBlock, 0, st, 1);
@@ -1130,7 +1148,9 @@ template <class F, class G> int shift_pass(cudaStream_t st, G &g, const TileConf
     // batched list launches: blocks of kListBlock threads, kTileBlock / kListBlock
     // times as many (a sparse scene swept alone, one short launch, keeps the
     // larger blocks: measured 116 against 132 ms/step on the sweep's scenes
-    // stepped one by one)
+    // stepped one by one).  A dense scene: one block of kDenseBlock threads
+    // per tile (4.15M dam break 3.92 -> 3.80 ms/step against 256 threads;
+    // 64 threads: 4.39, 512: 4.73).
     constexpr int kT = std::is_same<G, GroupMany>::value ? kListBlock : kTileBlock;
     auto list_blocks = [&](const Scene &s) {
         return active(s) ? std::min<unsigned>(tile_blocks(s.p, tc.tile_h), sweep_blocks(s.p, tc.tile_h) * (kTileBlock / kT))
@@ -1138,7 +1158,7 @@ template <class F, class G> int shift_pass(cudaStream_t st, G &g, const TileConf
     };
     int n = use_tile_list(g, tc.tile_h)
                 ? launch(g, key, list_blocks, k_shift_gradient_tiled<D, F, true, kT>, kT, smem, st, tc.tile_h, cap, pass)
-                : launch(g, key, blocks, k_shift_gradient_tiled<D, F, false, kTileBlock>, kTileBlock, smem, st,
+                : launch(g, key, blocks, k_shift_gradient_tiled<D, F, false, kDenseBlock>, kDenseBlock, smem, st,
                          tc.tile_h, cap, pass);
     n += launch(
         g, site_key(SITE_SHIFT_FALLBACK, pass),
