@@ -79,18 +79,18 @@ def bytes_per_step(nf: int, ns: int, nv: int, shifts: int, substeps: int) -> flo
 # DRAM traffic (dram__bytes_read.sum + dram__bytes_write.sum) per fluid
 # particle of one launch of the tiled neighbour sweeps, from one ncu capture of
 # the 2,083,750-particle gas-liquid dam break (plain form, tiles of 16 cells,
-# stored neighbour lists, fused shifting pass); it grows in proportion to the
+# stored neighbour lists, fused shifting pass, 128-thread blocks); it grows in proportion to the
 # particle count (same tile shape, same list length per particle).  Well above
 # the compulsory bytes above: the pair pass writes the per-step neighbour lists
 # and every shifting pass reads them back.
 MEASURED_TRAFFIC_PER_PARTICLE = {
-    "fluid_pair": 146.6,
-    "shift_pass": 156.4,
+    "fluid_pair": 149.0,
+    "shift_pass": 157.4,
 }
 # the same capture of the mixed form
 MEASURED_TRAFFIC_PER_PARTICLE_MIXED = {
-    "fluid_pair": 148.0,
-    "shift_pass": 186.8,
+    "fluid_pair": 149.4,
+    "shift_pass": 187.3,
 }
 
 
