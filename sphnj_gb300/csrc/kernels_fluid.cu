@@ -52,15 +52,20 @@ constexpr int kListBlock = 128;   // shifting passes over an active-tile list
 constexpr int kDenseBlock = 128;  // shifting passes of a dense scene, one block per tile
 
 // Block shape of the pair pass, by launch:
-//  - a dense scene swept alone (one block per tile) and batches (tile
-//    lists): 128 threads, 8 blocks per SM (64 registers, no spills), staging
-//    sized by pair_per_cell so that the 8 fit.  Smaller blocks leave fewer
-//    warps waiting at a tile's barriers.  256-scene mixed sweep 4.56 -> 4.46
-//    ms/step; 4.15M dam break 3.80 -> 3.74 (against 256 threads, 5 per SM);
+//  - batches (tile lists): 128 threads, 8 blocks per SM (64 registers, no
+//    spills), staging sized by pair_per_cell so that the 8 fit.  Smaller
+//    blocks leave fewer warps waiting at a tile's barriers (256-scene mixed
+//    sweep 4.56 -> 4.46 ms/step);
+//  - a dense scene swept alone (one block per tile): 128 threads, 7 per SM
+//    (up to 73 registers).  4.15M dam break 3.80 -> 3.74 ms/step at 8 per SM
+//    against 256 threads at 5; 7 per SM 3.77 -> 3.69, 6 per SM 3.76;
 //  - a sparse scene swept alone (tile list): 256 threads, 5 per SM (48
 //    registers; unbounded it takes 64 and 4 blocks).
 template <class G, bool kList> struct PairShape {
     static constexpr int threads = 128, min_blocks = 8;
+};
+template <> struct PairShape<GroupOne, false> {
+    static constexpr int threads = 128, min_blocks = 7;
 };
 template <> struct PairShape<GroupOne, true> {
     static constexpr int threads = 256, min_blocks = 5;
