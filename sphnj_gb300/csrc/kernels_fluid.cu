@@ -56,18 +56,20 @@ constexpr int kDenseBlock = 128;  // shifting passes of a dense scene, one block
 //    spills), staging sized by pair_per_cell so that the 8 fit.  Smaller
 //    blocks leave fewer warps waiting at a tile's barriers (256-scene mixed
 //    sweep 4.56 -> 4.46 ms/step);
-//  - a dense scene swept alone (one block per tile): 128 threads, 7 per SM
-//    (up to 73 registers).  4.15M dam break 3.80 -> 3.74 ms/step at 8 per SM
-//    against 256 threads at 5; 7 per SM 3.77 -> 3.69, 6 per SM 3.76;
+//  - a dense scene swept alone (one block per tile): 128 threads, 8 per SM
+//    in the plain form, 7 in the mixed form.  4.15M dam break 3.80 -> 3.74
+//    ms/step at 8 per SM against 256 threads at 5; then, measured on one box,
+//    mixed 3.737 at 8 against 3.660 at 7, plain 4.214 at 8 against 4.267 at 7
+//    (6 per SM: 3.76);
 //  - a sparse scene swept alone (tile list): 256 threads, 5 per SM (48
 //    registers; unbounded it takes 64 and 4 blocks).
-template <class G, bool kList> struct PairShape {
+template <class G, bool kList, class F> struct PairShape {
     static constexpr int threads = 128, min_blocks = 8;
 };
-template <> struct PairShape<GroupOne, false> {
+template <> struct PairShape<GroupOne, false, FormMixed> {
     static constexpr int threads = 128, min_blocks = 7;
 };
-template <> struct PairShape<GroupOne, true> {
+template <class F> struct PairShape<GroupOne, true, F> {
     static constexpr int threads = 256, min_blocks = 5;
 };
 constexpr int kMaxPerCell = 24;  // staged particles per cell at most
@@ -1040,20 +1042,23 @@ constexpr size_t kPairSmemPerEntry = 3 * sizeof(float2) + sizeof(int) + 1;
 }  // namespace
 
 cudaError_t configure_sweeps(const TileConfig &tc) {
-    using PD = PairShape<GroupOne, false>;
-    using PL = PairShape<GroupOne, true>;
-    using PM = PairShape<GroupMany, true>;
+    using PDp = PairShape<GroupOne, false, FormPlain>;
+    using PDm = PairShape<GroupOne, false, FormMixed>;
+    using PLp = PairShape<GroupOne, true, FormPlain>;
+    using PLm = PairShape<GroupOne, true, FormMixed>;
+    using PMp = PairShape<GroupMany, true, FormPlain>;
+    using PMm = PairShape<GroupMany, true, FormMixed>;
     // dynamic shared memory above 48 KB needs an opt-in (every launch stages
     // at most kMaxPerCell per cell)
     const int a = cudaFuncAttributeMaxDynamicSharedMemorySize;
     const size_t smem = tile_cap(tc.tile_h, kMaxPerCell) * kPairSmemPerEntry;
     const std::pair<const void *, size_t> kernels[] = {
-        {(const void *)k_fluid_pair_tiled<One, FormPlain, false, PD::threads, PD::min_blocks>, smem},
-        {(const void *)k_fluid_pair_tiled<One, FormPlain, true, PL::threads, PL::min_blocks>, smem},
-        {(const void *)k_fluid_pair_tiled<One, FormMixed, false, PD::threads, PD::min_blocks>, smem},
-        {(const void *)k_fluid_pair_tiled<One, FormMixed, true, PL::threads, PL::min_blocks>, smem},
-        {(const void *)k_fluid_pair_tiled<Many, FormPlain, true, PM::threads, PM::min_blocks>, smem},
-        {(const void *)k_fluid_pair_tiled<Many, FormMixed, true, PM::threads, PM::min_blocks>, smem}};
+        {(const void *)k_fluid_pair_tiled<One, FormPlain, false, PDp::threads, PDp::min_blocks>, smem},
+        {(const void *)k_fluid_pair_tiled<One, FormPlain, true, PLp::threads, PLp::min_blocks>, smem},
+        {(const void *)k_fluid_pair_tiled<One, FormMixed, false, PDm::threads, PDm::min_blocks>, smem},
+        {(const void *)k_fluid_pair_tiled<One, FormMixed, true, PLm::threads, PLm::min_blocks>, smem},
+        {(const void *)k_fluid_pair_tiled<Many, FormPlain, true, PMp::threads, PMp::min_blocks>, smem},
+        {(const void *)k_fluid_pair_tiled<Many, FormMixed, true, PMm::threads, PMm::min_blocks>, smem}};
     for (const auto &k : kernels) {
         if (k.second <= 48 * 1024) continue;
         const cudaError_t e = cudaFuncSetAttribute(k.first, (cudaFuncAttribute)a, (int)k.second);
@@ -1096,16 +1101,16 @@ template <class F, class G> int fluid_pair(cudaStream_t st, G &g, const TileConf
     // at 128 threads; a dense scene: one block per tile
     auto blocks = [&](const Scene &s) {
         return std::min<unsigned>(tile_blocks(s.p, tc.tile_h),
-                                  sweep_blocks(s.p, tc.tile_h) * (kTileBlock / PairShape<G, true>::threads));
+                                  sweep_blocks(s.p, tc.tile_h) * (kTileBlock / PairShape<G, true, F>::threads));
     };
     const int lists = tc.lists ? 1 : 0;
     const long long key = site_key(SITE_PAIR_TILED, tc.tile_h);
     if (list) {
-        using Shape = PairShape<G, true>;
+        using Shape = PairShape<G, true, F>;
         n += launch(g, key, blocks, k_fluid_pair_tiled<D, F, true, Shape::threads, Shape::min_blocks>, Shape::threads,
                     smem, st, tc.tile_h, cap, lists);
     } else if constexpr (!std::is_same<G, GroupMany>::value) {  // batches always sweep their lists
-        using Shape = PairShape<G, false>;
+        using Shape = PairShape<G, false, F>;
         n += launch(
             g, key, [&](const Scene &s) { return tile_blocks(s.p, tc.tile_h); },
             k_fluid_pair_tiled<D, F, false, Shape::threads, Shape::min_blocks>, Shape::threads, smem, st, tc.tile_h,
