@@ -48,10 +48,8 @@ def parse():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--dx", type=float, default=0.0017)
-    ap.add_argument("--cpu-dx", type=float, default=0.0068,
-                    help="dx of the bounded CPU sample (same geometry, 1/16 of the particles)")
-    ap.add_argument("--cpu-steps", type=int, default=150,
-                    help="timed oracle steps of the CPU sample (~10 s on 16 host cores)")
+    ap.add_argument("--cpu-steps", type=int, default=10,
+                    help="timed oracle steps of the CPU baseline on the workload (~10 s on 16 host cores)")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--untiled", action="store_true", help="one thread per particle in the neighbour sweeps")
@@ -121,55 +119,120 @@ def make_case(dx):
     return cases.dam_break_gas(dx=dx)
 
 
-def cpu_rate(case, p, steps, normals=None):
-    """Oracle (reference precision, all host threads) particle-steps/s on a
-    case; setup (upload, wall normals) is outside the timed region."""
+def cpu_model() -> str:
+    """The host CPU's model name (x86 'model name', or lscpu's 'Model name'
+    on Arm, where /proc/cpuinfo lists only part numbers)."""
+    try:
+        for line in Path("/proc/cpuinfo").read_text().splitlines():
+            if line.lower().startswith("model name"):
+                return line.split(":", 1)[1].strip()
+    except OSError:
+        pass
+    try:
+        out = subprocess.run(["lscpu"], capture_output=True, text=True, timeout=10).stdout
+        for line in out.splitlines():
+            if line.strip().lower().startswith("model name"):
+                return line.split(":", 1)[1].strip()
+    except (OSError, subprocess.SubprocessError):
+        pass
+    return "unknown"
+
+
+def next_sort_step(step: int, every: int) -> int:
+    """Steps to take from step counter `step` so that the next step taken is
+    a sort step ((i - 1) mod sort_every_step == 0, SimTime::isSort)."""
+    return (-step) % every
+
+
+def oracle_sim(case, threads=0):
+    """The oracle (reference precision) uploaded with the case; its
+    parameters derived by the oracle itself, so that the product library is
+    never loaded on this path."""
     import oracle
 
-    arr = case.arrays()
-    if normals is not None:
-        arr["virt_normal"] = normals
-    o = oracle.OracleSim(p, oracle.REFERENCE_PRECISION, threads=0)
-    o.upload(arr)
-    o.step(1)  # first step sorts; keep it out of the timing like the GPU warm-up
+    p = oracle.params_for(case)
+    if threads:
+        oracle.set_threads(threads)
+    o = oracle.OracleSim(p, oracle.REFERENCE_PRECISION, threads=threads)
+    o.upload(case.arrays())
+    return o, p
+
+
+def oracle_timed(o, p, warm, steps, align):
+    """Times `steps` oracle steps after `warm` untimed ones; with `align` the
+    step counter is moved on (untimed, no work) so that the timed steps start
+    with a sort step, as the GPU arm's do.  Returns seconds."""
+    import oracle  # noqa: F401
+
+    o.step(warm)
+    if align:
+        o.set_step(o.step_index + next_sort_step(o.step_index, p.sort_every_step))
     t0 = time.perf_counter()
     o.step(steps)
-    dt = time.perf_counter() - t0
-    o.close()
-    return (p.fluid_number_total + p.solid_number) * steps / dt, oracle.max_threads(), dt
+    return time.perf_counter() - t0
+
+
+RECORDS = ROOT / "tests" / "records"
+
+
+def error_records() -> dict:
+    """The errors against the FP64 oracle that the GPU tests measured and
+    recorded (tests/records/*.json, written by tests/test_gpu_fp64_error.py
+    with SPHNJ_RECORD_DIR set): per record, its case and the largest errors of
+    each form."""
+    out = {}
+    for f in sorted(RECORDS.glob("fp64_*.json")):
+        try:
+            rec = json.loads(f.read_text())
+        except (OSError, ValueError):
+            continue
+        out[f.stem] = rec.get("summary", rec)
+    return out or {"missing": "no error records under tests/records"}
 
 
 def run_reference(args):
+    """The reference's CPU implementation of the path on this host: the
+    reference has only a CUDA implementation, so this is its CPU restatement
+    (the oracle port, OpenMP over particles) on the same workload as the GPU
+    arm - the 4.15M-particle dam break - with every host thread; W warm-up
+    steps, then K timed steps that start with a sort step.  A 1-thread step
+    is timed beside it."""
     rank, world, _ = dist_env()
     if rank != 0:
         return 0
     import oracle
 
     oracle.build()
-    case = make_case(args.cpu_dx)
-    p = case.params()
-    arr = case.arrays()
-    o = oracle.OracleSim(p, oracle.REFERENCE_PRECISION, threads=0)
-    o.upload(arr)
-    o.step(max(args.warmup, 1))
+    case = make_case(args.dx)
     t0 = time.perf_counter()
-    o.step(args.steps)
-    dt = time.perf_counter() - t0
+    o, p = oracle_sim(case)
+    setup = time.perf_counter() - t0
     n = p.fluid_number_total + p.solid_number
+    threads = oracle.max_threads()
+    dt = oracle_timed(o, p, max(args.warmup, 1), args.steps, align=True)
     v = n * args.steps / dt
-    sample = (f"gas-liquid dam break at dx={args.cpu_dx} ({n} particles, same geometry, h/dx and 10 shifts "
-              f"as the dx={args.dx} workload), {args.steps} full steps")
+    oracle.set_threads(1)
+    t1 = time.perf_counter()
+    o.step(1)
+    dt1 = time.perf_counter() - t1
+    oracle.set_threads(threads)
+    o.close()
+    sample = (f"the full workload ({n} particles), {args.warmup} warm-up steps, then {args.steps} timed steps "
+              f"starting with a sort step, {threads} threads; 1 thread: {n / dt1:.4g} particle-steps/s over one "
+              f"step")
     line = {
         "impl": "reference", "metric": METRIC, "value": v, "unit": UNIT, "n_gpus": args.gpus,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": dt * 1e3 / args.steps,
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
         "data": "synthetic (lattice dam break generated in-process)",
-        "config": {"workload": f"gas-liquid dam break, dx={args.dx}", "particles": n},
-        "cpu_baseline": {"value": v, "unit": UNIT, "cores": oracle.max_threads(), "kind": "port",
-                         "sample": sample},
+        "config": {"workload": f"gas-liquid dam break, 1.0x2.0 m water in a 4.0x3.0 m air-filled tank, dx={args.dx}",
+                   "particles": n, "n_fluid": p.fluid_number_total, "n_virt": p.virt_number,
+                   "shift_per_step": p.shift_per_step, "sort_every_step": p.sort_every_step},
+        "cpu_baseline": {"value": v, "unit": UNIT, "cores": threads, "kind": "port", "sample": sample,
+                         "one_thread": n / dt1, "cpu": cpu_model(), "setup_s": setup},
         "e2e": {"value": v, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
         "note": "the reference has no CPU implementation of the path (CUDA only); this arm is its CPU "
-                "restatement in oracle/, built with OpenMP",
+                "restatement in oracle/ (OpenMP), with parameters derived by the oracle itself",
     }
     print(json.dumps(line), flush=True)
     return 0
@@ -309,9 +372,14 @@ def run_ours(args):
         if world > 1:
             torch.distributed.barrier()
 
-    # warm-up
+    # warm-up, then on to the step before a sort step, so that the timed
+    # steps start with a sort (sort_every_step = 50: one sort in K = 20 timed
+    # steps over-weights it; the amortised rate over one whole sort period is
+    # measured below as "sort_period")
     sim.step(args.warmup)
+    sim.step(next_sort_step(sim.step_index, p.sort_every_step))
     sim.synchronize()
+    first_timed = sim.step_index + 1
 
     # ---- timed region: inputs resident in HBM (state 0.3 GB > 129 MB L2) ---
     l0 = sim.launches()
@@ -332,6 +400,19 @@ def run_ours(args):
         torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
         ms = float(t.item())
     value = units * world * args.steps / (ms / 1e3)
+
+    # ---- one whole sort period (sort_every_step steps from a sort step) ------
+    sim.step(next_sort_step(sim.step_index, p.sort_every_step))
+    sim.synchronize()
+    q0, q1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    q0.record(stream)
+    sim.step(p.sort_every_step)
+    q1.record(stream)
+    torch.cuda.synchronize()
+    ms_period = q0.elapsed_time(q1)
+    sort_period = {"steps": p.sort_every_step, "ms_per_step": ms_period / p.sort_every_step,
+                   "value": units * world * p.sort_every_step / (ms_period / 1e3),
+                   "what": "one sort step and the incremental steps up to the next sort, timed together"}
 
     # ---- per-stage device times (CUDA events on the launching stream) -------
     sim.profile_enable(True)
@@ -355,8 +436,7 @@ def run_ours(args):
                 "frac": achieved / peak,
                 "traffic": byte_model.measured_traffic_per_launch(dom, nf, mixed) if args.tile_h == 16 and not args.untiled
                 else None,
-                "traffic_source": "ncu dram bytes of one launch at 2.08M particles, scaled by particle count "
-                                  "(profiles/k_fluid_pair_tiled_k_shift_gradient_tiled_dam_break_gas_2M.md)",
+                "traffic_source": "ncu dram bytes of one launch at 2.08M particles, scaled by particle count",
                 "peak_source": "MEASURED_PEAKS.json hbm_gbs (measured)" if peaks else "fallback 6.8 TB/s",
                 "bytes_per_launch": bpl, "avg_launch_ms": avg_ms,
                 "stage_share": {k: round(v[0] / total_ms, 4) for k, v in prof.items() if v[1]}}
@@ -424,9 +504,7 @@ def run_ours(args):
              names[other]: {"value": units * world * args.steps / (ms_other / 1e3),
                             "ms_per_step": ms_other / args.steps}}
     forms["mixed_over_plain"] = forms["plain"]["ms_per_step"] / forms["mixed"]["ms_per_step"]
-    forms["error_vs_fp64_oracle"] = ("water dam break front after 2,000 steps: mixed 4.2e-7, plain 1.2e-5 "
-                                     "(relative); cantilever tip over a quarter period: mixed 1.1e-7, plain "
-                                     "3.4e-10 of amplitude (tests/test_gpu_mixed.py)")
+    forms["error_vs_fp64_oracle"] = error_records()
 
     sweep = None
     if not args.no_sweep:
@@ -434,13 +512,22 @@ def run_ours(args):
 
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
-        ccase = make_case(args.cpu_dx)
-        cp = ccase.params()
-        v, cores, dt = cpu_rate(ccase, cp, args.cpu_steps)
-        cpu = {"value": v, "unit": UNIT, "cores": cores, "kind": "port",
-               "sample": f"oracle (reference precision, OpenMP) on the same dam break at dx={args.cpu_dx} "
-                         f"({cp.fluid_number_total} particles, same geometry, h/dx and shifts), {args.cpu_steps} "
-                         f"steps after one sort step, {dt:.1f} s"}
+        import oracle
+
+        o, cp = oracle_sim(case)
+        cores = oracle.max_threads()
+        dt = oracle_timed(o, cp, 1, args.cpu_steps, align=False)
+        v = units * args.cpu_steps / dt
+        oracle.set_threads(1)
+        t1 = time.perf_counter()
+        o.step(1)
+        dt1 = time.perf_counter() - t1
+        oracle.set_threads(cores)
+        o.close()
+        cpu = {"value": v, "unit": UNIT, "cores": cores, "kind": "port", "cpu": cpu_model(), "one_thread": units / dt1,
+               "sample": f"oracle (reference precision, OpenMP) on this workload ({units} particles), one sort "
+                         f"step untimed, then {args.cpu_steps} steps ({dt:.1f} s); one_thread: one more step on 1 "
+                         f"thread ({dt1:.1f} s)"}
 
     if world > 1:
         torch.distributed.destroy_process_group()
@@ -466,6 +553,8 @@ def run_ours(args):
         "cpu_baseline": cpu,
         "e2e": e2e,
         "gpu_launches": launches,
+        "timed_steps": f"{first_timed}..{first_timed + args.steps - 1} (starts with a sort step)",
+        "sort_period": sort_period,
         "clocks": clk.summary(),
         "forms": forms,
         "batched_sweep": sweep,

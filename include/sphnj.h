@@ -421,18 +421,26 @@ int  sphnj_stat_launches(const sphnj_ctx *ctx, uint64_t *launches);
  * lists in the reference's order.
  *
  * All pointers are device pointers owned by the caller:
- *   cell_id     [n_particles]       new cell id of each particle (0..nx*ny-1)
+ *   cell_id     [n_particles]       new cell id of each particle; every id
+ *                                   must lie in 0..nx*ny-1 (not checked: an
+ *                                   id outside it corrupts list_out)
  *   prev_range  [2*nx*ny]           previous {start, count} per cell (8-byte aligned)
  *   prev_list   [sum of counts]     previous lists, a valid CSR over 0..n_particles-1
  *   range_out   [2*nx*ny]           new {start, count} per cell (8-byte aligned)
  *   list_out    [n_particles]       new lists
+ * As in the reference, a particle whose new cell is not one of the nine
+ * around its previous cell (it moved more than one cell since the lists were
+ * built) is dropped until the next sort: list_out then holds fewer than
+ * n_particles entries (the sum of the new counts).
  * stream is a cudaStream_t (NULL = legacy default stream); the call only
  * enqueues work.  It allocates nothing: its scratch is a static device array
  * for at most SPHNJ_NOALLOC_MAX_CELLS cells (about 2.6 MB, held by every GPU
  * that loads the library until the process exits).  nx*ny above that limit
- * returns SPHNJ_ERR_UNSUPPORTED.  The first call on a device looks up that
- * array's device address (cudaGetSymbolAddress); make that first call before
- * any stream capture.  All calls share the one array, so calls that overlap
+ * returns SPHNJ_ERR_UNSUPPORTED.  Each call outside a stream capture looks up
+ * that array's device address in the current context (cudaGetSymbolAddress);
+ * a call during a capture uses the address the last such call found on that
+ * device, so make the first call on a device before any stream capture (a
+ * first call inside a capture returns SPHNJ_ERR_ARG).  All calls share the one array, so calls that overlap
  * on the GPU (different streams, or different host threads) race and must
  * be serialised by the caller. */
 #define SPHNJ_NOALLOC_MAX_CELLS 65536

@@ -65,6 +65,25 @@ def max_threads() -> int:
     return lib().oracle_max_threads()
 
 
+def set_threads(n: int) -> int:
+    """OpenMP threads of later oracle steps (n <= 0 keeps the current
+    number); returns the number in use."""
+    return lib().oracle_set_threads(int(n))
+
+
+def params_for(case) -> Params:
+    """Parameters of a sphnj_gb300.cases.Case derived by the oracle itself
+    from the case's input.ini text and particle counts (the reference's
+    Parameter::readParameter and initiate restated in oracle/sph_oracle.cpp),
+    without the product library."""
+    p = Params()
+    counts = (C.c_int32 * 4)(case.n_liquid, case.n_gas, case.n_solid, case.n_virt)
+    rc = lib().oracle_params_from_ini(case.ini_text().encode(), counts, C.byref(p))
+    if rc:
+        raise OracleError(f"oracle_params_from_ini: {abi.ERROR_NAMES.get(rc, rc)}")
+    return p
+
+
 class OracleError(RuntimeError):
     pass
 

@@ -32,11 +32,19 @@ from pathlib import Path
 HERE = Path(__file__).resolve().parent
 OUT = HERE.parent / "_ref"
 STAGED = OUT / "src"
-REFERENCE = Path("/root/reference")
+# the reference checkout: SPHNJ_REFERENCE, else where the development
+# container mounts it
+REFERENCE = Path(os.environ.get("SPHNJ_REFERENCE", "/root/reference"))
 BIN = OUT / "harness"
 
 FLAGS = ["-std=c++17", "-rdc=true", "-gencode", "arch=compute_103a,code=sm_103a", "-O3", "-use_fast_math",
          "-Xptxas", "-O3,-dlcm=cg", "-w"]
+
+
+def reference_present() -> bool:
+    """True where the reference tree itself is readable (the development
+    container), so that build() compiles the harness from it."""
+    return (REFERENCE / "src" / "fluid.cu").exists()
 
 
 def source_root() -> Path:

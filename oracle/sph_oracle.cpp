@@ -1181,6 +1181,171 @@ struct oracle_ctx {
     oracle::Base *impl;
 };
 
+namespace oracle {
+
+// key -> value of a flat ini text: '#' starts a comment, '[section]' lines
+// carry no keys, a later key replaces an earlier one (Config, config.cpp:59-129
+// and config.h:122-159, for the files this project writes).
+struct Ini {
+    std::vector<std::pair<std::string, std::string>> kv;
+    explicit Ini(const char *text) {
+        std::string all(text ? text : ""), line;
+        size_t a = 0;
+        while (a <= all.size()) {
+            size_t b = all.find('\n', a);
+            if (b == std::string::npos) b = all.size();
+            line = all.substr(a, b - a);
+            a = b + 1;
+            const size_t hash = line.find('#');
+            if (hash != std::string::npos) line.resize(hash);
+            const size_t eq = line.find('=');
+            if (eq == std::string::npos || line.find('[') != std::string::npos) continue;
+            auto trim = [](std::string t) {
+                const size_t f = t.find_first_not_of(" \t\r"), l = t.find_last_not_of(" \t\r");
+                return f == std::string::npos ? std::string() : t.substr(f, l - f + 1);
+            };
+            const std::string k = trim(line.substr(0, eq)), v = trim(line.substr(eq + 1));
+            if (!k.empty()) kv.emplace_back(k, v);
+        }
+    }
+    const std::string *find(const char *key) const {
+        for (auto it = kv.rbegin(); it != kv.rend(); ++it)
+            if (it->first == key) return &it->second;
+        return nullptr;
+    }
+    float f(const char *key, float dflt) const {
+        const std::string *v = find(key);
+        return v ? std::strtof(v->c_str(), nullptr) : dflt;
+    }
+    double d(const char *key, double dflt) const {
+        const std::string *v = find(key);
+        return v ? std::strtod(v->c_str(), nullptr) : dflt;
+    }
+    int i(const char *key, int dflt) const {
+        const std::string *v = find(key);
+        return v ? (int)std::strtol(v->c_str(), nullptr, 10) : dflt;
+    }
+    bool b(const char *key, bool dflt) const {
+        const std::string *v = find(key);
+        if (!v) return dflt;
+        return *v == "true" || *v == "1" || *v == "yes" || *v == "on" || *v == "True" || *v == "TRUE";
+    }
+};
+
+// Parameter::readParameter + Parameter::initiate in the reference's float
+// arithmetic: the ini reads with their defaults (physics.cpp:12-17,
+// properties.cpp:37-49,120-149, domain.cpp:10-18, sim_time.cpp:10-16,
+// kernel.cpp:11-14) and the derived constants (properties.cpp:53-89,
+// kernel.cpp:25-41 with the truncated-Gaussian constants of global.h:11-13,
+// domain.cpp:37-49).
+static int params_from_ini(const char *text, const int counts[4], sphnj_params *p) {
+    const Ini c(text);
+    std::memset(p, 0, sizeof *p);
+    p->gravity[0] = 0.0f;
+    p->gravity[1] = -c.f("gravity", 9.81f);
+    p->transient_type = c.b("is_steady", false) ? SPHNJ_STEADY : SPHNJ_TRANSIENT;
+    p->fluid_number[0] = counts[0];
+    p->fluid_number[1] = counts[1];
+    p->fluid_number_total = counts[0] + counts[1];
+    p->solid_number = counts[2];
+    p->virt_number = counts[3];
+    p->particle_shift_coef = c.f("particle_shift_coef", 0.4f);
+    p->is_fluid_viscid = c.b("is_viscid", false) ? 1 : 0;
+    p->min_pressure = c.f("min_pressure", -1.013e5f);
+    const char *phase[2] = {"liquid", "gas"};
+    const float cs0[2] = {1500.0f, 340.0f}, rho0[2] = {1000.0f, 1.29f}, g0[2] = {7.0f, 1.4f},
+                mu0[2] = {1.01e-3f, 17.9e-6f};
+    for (int k = 0; k < 2; ++k) {
+        const std::string pre(phase[k]);
+        p->sound_speed[k] = c.f((pre + "_sound_speed").c_str(), cs0[k]);
+        p->reference_density[k] = c.f((pre + "_density").c_str(), rho0[k]);
+        p->gamma[k] = c.f((pre + "_gamma").c_str(), g0[k]);
+        p->viscosity[k] = c.f((pre + "_viscosity").c_str(), mu0[k]);
+        // FluidProperties::initiate
+        p->coefficient_p2rho[k] = p->gamma[k] * powf(p->sound_speed[k], -2.0f) / p->reference_density[k];
+        p->coefficient_rho2p[k] = 1.0f / p->coefficient_p2rho[k];
+        p->gamma_inv[k] = 1.0f / p->gamma[k];
+        p->reference_density_inverse[k] = 1.0f / p->reference_density[k];
+        p->min_density[k] = (1.0f - 0.4f) * p->reference_density[k];
+    }
+    p->solid_reference_density = c.f("solid_density", 2700.0f);
+    p->youngs_modulus = c.f("youngs_modulus", 67.5e9f);
+    p->poisson_ratio = c.f("poisson_ratio", 0.34f);
+    p->artificial_viscosity[0] = c.f("arti_vis_alpha", 2.5f);
+    p->artificial_viscosity[1] = c.f("arti_vis_beta", 2.5f);
+    p->fixed_speed[0] = c.d("solid_fixed_speed_x", 0.0);
+    p->fixed_speed[1] = c.d("solid_fixed_speed_y", 0.0);
+    p->constitution_type = c.b("is_2D_strain", false) ? SPHNJ_STRAIN_2D : SPHNJ_STRESS_2D;
+    p->plastic_type = c.b("is_plastic", false) ? SPHNJ_PLASTIC : SPHNJ_HYPER_ELASTIC;
+    p->auxetic_density = c.f("auxetic_density", 636.0f);
+    p->auxetic_modulus = c.f("auxetic_modulus", 0.0f);
+    p->auxetic_poisson_ratio = c.f("auxetic_poisson_ratio", -0.2f);
+    p->yield_strain = c.f("yield_strain", 0.0f);
+    p->yield_stress = c.f("yield_stress", 2.0e7f);
+    p->harden_strain = c.f("harden_strain", 0.5f);
+    p->harden_coef = c.f("harden_coef", 100.0f);
+    // one of the auxetic modulus and the yield strain follows from the
+    // other and the yield stress (properties.cpp:150-158)
+    if (p->auxetic_modulus == 0.0f && p->yield_strain == 0.0f) return SPHNJ_ERR_CONFIG;
+    if (p->yield_strain != 0.0f) p->auxetic_modulus = p->yield_stress / p->yield_strain;
+    else p->yield_strain = p->yield_stress / p->auxetic_modulus;
+    // SolidProperties::initiate
+    const float E = p->youngs_modulus, nu = p->poisson_ratio, aE = p->auxetic_modulus, anu = p->auxetic_poisson_ratio;
+    const bool strain = p->constitution_type == SPHNJ_STRAIN_2D;
+    p->lambda = E * nu / (strain ? 1.0f - 2.0f * nu : 1.0f - nu) / (1.0f + nu);
+    p->nu = E / (1.0f + nu) / 2.0f;
+    p->auxetic_lambda = aE * anu / (strain ? 1.0f - 2.0f * anu : 1.0f - anu) / (1.0f + anu);
+    p->auxetic_nu = aE / (1.0f + anu) / 2.0f;
+    p->bulk_modulus = E / (3.0f * (1.0f - 2.0f * nu));
+    p->solid_sound_speed = sqrtf(p->bulk_modulus / p->solid_reference_density);
+    // Domain
+    p->cell_xmin[0] = c.f("cell_xmin", 0.0f);
+    p->cell_xmin[1] = c.f("cell_ymin", 0.0f);
+    p->cell_xmax[0] = c.f("cell_xmax", 0.0f);
+    p->cell_xmax[1] = c.f("cell_ymax", 0.0f);
+    p->domain_xmin[0] = c.f("domain_xmin", 0.0f);
+    p->domain_xmin[1] = c.f("domain_ymin", 0.0f);
+    p->domain_xmax[0] = c.f("domain_xmax", 0.0f);
+    p->domain_xmax[1] = c.f("domain_ymax", 0.0f);
+    // SimTime
+    p->dt = c.f("dt", 0.0f);
+    p->istart = c.i("istart", 0);
+    p->iend = c.i("iend", 0);
+    p->solid_sub_step = c.i("solid_sub_step", 1);
+    p->result_interval = c.i("result_interval", 1);
+    p->sort_every_step = c.i("sort_every_step", 1);
+    p->shift_per_step = c.i("shift_per_step", 1);
+    // Kernel
+    p->smoothing_length = c.f("smoothing_length", 0.0f);
+    p->particle_diameter = c.f("particle_diameter", 0.0f);
+    p->impact_length_hsml_ratio = c.f("impact_length_hsml_ratio", 3.0f);
+    p->thread_num = c.i("thread_num", 32);
+    const float h = p->smoothing_length, dd = p->particle_diameter, R = p->impact_length_hsml_ratio;
+    if (h <= 0.0f || dd <= 0.0f) return SPHNJ_ERR_CONFIG;
+    p->particle_volume = powf(dd, 3.0f);
+    p->diameter_square = powf(dd, 2.0f);
+    p->smoothing_length_square = powf(h, 2.0f);
+    p->smoothing_length_inverse = 1.0f / h;
+    p->smoothing_length_inverse_square = powf(p->smoothing_length_inverse, 2.0f);
+    p->impact_distance_square = powf(R, 2.0f) * powf(h, 2.0f);
+    const float tg2 = 5.551921f;  // global.h:12
+    p->kernel_coefficient_1 = expf(-powf(R, 2.0f));
+    p->kernel_coefficient_2 = 1.0f / tg2 * powf(h / dd, -3.0f);
+    p->kernel_differential = 2.0f / tg2 * powf(h / dd, -3.0f) * powf(h, -2.0f);
+    p->coefficient_3d_to_2d = 2.120729f;  // global.h:13
+    for (int k = 0; k < 2; ++k) {
+        const float span = p->cell_xmax[k] - p->cell_xmin[k];
+        if (span == 0.0f) return SPHNJ_ERR_CONFIG;
+        p->cell_number[k] = (int)(span / (R * h));
+        p->interval[k] = span / (float)p->cell_number[k];
+        p->interval_inv[k] = 1.0f / p->interval[k];
+    }
+    p->cell_number_total = p->cell_number[0] * p->cell_number[1];
+    return SPHNJ_OK;
+}
+
+}  // namespace oracle
+
 extern "C" {
 
 // precision: 0 = reference precision (fluid FP32, solid FP64), 1 = FP64.
@@ -1227,6 +1392,22 @@ int oracle_debug_set_step(oracle_ctx *c, int s) {
     if (!c) return SPHNJ_ERR_ARG;
     c->impl->set_step(s);
     return SPHNJ_OK;
+}
+// Parameters of a case from its input.ini text and its particle counts
+// (n_liquid, n_gas, n_solid, n_virt), derived by the oracle itself.
+int oracle_params_from_ini(const char *ini_text, const int32_t *counts, sphnj_params *out) {
+    if (!ini_text || !counts || !out) return SPHNJ_ERR_ARG;
+    const int c[4] = {counts[0], counts[1], counts[2], counts[3]};
+    return oracle::params_from_ini(ini_text, c, out);
+}
+int oracle_set_threads(int threads) {
+#ifdef _OPENMP
+    if (threads > 0) omp_set_num_threads(threads);
+    return omp_get_max_threads();
+#else
+    (void)threads;
+    return 1;
+#endif
 }
 int oracle_max_threads(void) {
 #ifdef _OPENMP

@@ -269,6 +269,10 @@ def declare(lib: C.CDLL, prefix: str) -> None:
         g("error").restype = C.c_int
         g("max_threads").argtypes = []
         g("max_threads").restype = C.c_int
+        g("set_threads").argtypes = [C.c_int]
+        g("set_threads").restype = C.c_int
+        g("params_from_ini").argtypes = [C.c_char_p, PI, C.POINTER(Params)]
+        g("params_from_ini").restype = C.c_int
     g("create").restype = C.c_int
     g("upload").argtypes = [vp, C.POINTER(HostState)]
     g("upload").restype = C.c_int

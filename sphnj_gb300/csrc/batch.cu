@@ -225,8 +225,9 @@ int sphnj_batch_step(sphnj_batch *b, int n) {
             if (!c->uploaded || c->step != c0->step || c->parity != c0->parity)
                 return bfail(b, SPHNJ_ERR_ARG, "batch scenes are not at the same step");
         StepKind k{};
+        std::vector<StepKind> kinds(b->scenes.size());
         for (size_t i = 0; i < b->scenes.size(); ++i) {
-            const StepKind ki = advance(b->scenes[i]);
+            const StepKind ki = kinds[i] = next_kind(b->scenes[i]);
             if (i == 0) {
                 k = ki;
             } else {
@@ -267,6 +268,8 @@ int sphnj_batch_step(sphnj_batch *b, int n) {
             }
         }
         BCK(cudaGetLastError());
+        // the step is issued: only now does every scene's step state move
+        for (size_t i = 0; i < b->scenes.size(); ++i) commit_step(b->scenes[i], kinds[i]);
     }
     return SPHNJ_OK;
 }

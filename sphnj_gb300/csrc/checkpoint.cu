@@ -87,6 +87,8 @@ int sphnj_checkpoint_save(sphnj_ctx *ctx, void *buffer, uint64_t bytes) {
 
 int sphnj_checkpoint_load(sphnj_ctx *ctx, const void *buffer, uint64_t bytes) {
     if (!ctx || !buffer) return SPHNJ_ERR_ARG;
+    // a batch steps its scenes in lockstep: one scene's step cannot move alone
+    if (ctx->batch) return ck_fail(ctx, SPHNJ_ERR_ARG, "the scene is in a batch: load before batching it");
     if (bytes < sizeof(CkHeader)) return ck_fail(ctx, SPHNJ_ERR_IO, "checkpoint shorter than its header");
     CkHeader h;
     std::memcpy(&h, buffer, sizeof h);

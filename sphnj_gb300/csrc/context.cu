@@ -260,6 +260,9 @@ int device_error_status(sphnj_ctx *ctx) {
         snprintf(buf, sizeof buf, "particle outside the cell grid (kind %d, index %d, cell id %d)", e.info[0],
                  e.info[1], e.info[2]);
         break;
+    case SPHNJ_ERR_NONFINITE:
+        snprintf(buf, sizeof buf, "non-finite state (kind %d, index %d) after an update", e.info[0], e.info[1]);
+        break;
     case SPHNJ_ERR_CELL_OVERFLOW:
         snprintf(buf, sizeof buf, "cell %d holds %d particles, more than the reference's %d slots", e.info[0],
                  e.info[1], SPHNJ_CELL_SIZE);
@@ -519,23 +522,27 @@ template <class G> int issue_step(G &g, const StepKind &k, cudaStream_t st, cons
 template int issue_step<GroupOne>(GroupOne &, const StepKind &, cudaStream_t, const TileConfig &, Profiler *);
 template int issue_step<GroupMany>(GroupMany &, const StepKind &, cudaStream_t, const TileConfig &, Profiler *);
 
-StepKind advance(sphnj_ctx *ctx) {
+StepKind next_kind(const sphnj_ctx *ctx) {
     const sphnj_params &p = ctx->p;
-    ctx->step++;
+    const int step = ctx->step + 1;
     StepKind k;
-    k.is_sort = ((ctx->step - 1) % p.sort_every_step) == 0;  // SimTime::isSort
+    k.is_sort = ((step - 1) % p.sort_every_step) == 0;  // SimTime::isSort
     // virtual particles are binned until their first sort (and once after an
     // upload); afterwards their ids never change.  After their first sort
     // their order and lists stay as they are (a stable sort of sorted keys is
     // the identity), so they are sorted once.
     k.bin_virt = !ctx->virt_sorted || !ctx->virt_cells_valid;
     k.sort_virt = k.is_sort && p.virt_number > 0 && !ctx->virt_sorted;
-    if (!k.is_sort) ctx->parity ^= 1;
-    k.parity = ctx->parity;
+    k.parity = k.is_sort ? ctx->parity : ctx->parity ^ 1;
+    return k;
+}
+
+void commit_step(sphnj_ctx *ctx, const StepKind &k) {
+    ctx->step++;
+    ctx->parity = k.parity;
     ctx->virt_cells_valid = true;
     if (k.sort_virt) ctx->virt_sorted = true;
     bind_lists(ctx);
-    return k;
 }
 
 }  // namespace sphnj
@@ -552,10 +559,11 @@ void drop_graphs(sphnj_ctx *ctx) {
 extern "C" int sphnj_step(sphnj_ctx *ctx, int n) {
     if (!ctx || n < 0) return SPHNJ_ERR_ARG;
     if (!ctx->uploaded) return fail(ctx, SPHNJ_ERR_ARG, "sphnj_step before sphnj_upload");
+    if (ctx->batch) return fail(ctx, SPHNJ_ERR_ARG, "the scene is in a batch: step the batch");
     cudaSetDevice(ctx->device);
     cudaStream_t st = ctx->st;
     for (int it = 0; it < n; ++it) {
-        const StepKind k = advance(ctx);
+        const StepKind k = next_kind(ctx);
         GroupOne g{scene_of(ctx, k.parity), ctx->form};
         if (ctx->use_graphs && !ctx->prof.on) {
             auto it_g = ctx->graphs.find(k.key());
@@ -576,6 +584,7 @@ extern "C" int sphnj_step(sphnj_ctx *ctx, int n) {
             ctx->launches += (uint64_t)issue_step(g, k, st, ctx->tiles, ctx->prof.on ? &ctx->prof : nullptr);
         }
         CK(cudaGetLastError());
+        commit_step(ctx, k);
     }
     return SPHNJ_OK;
 }

@@ -89,9 +89,14 @@ namespace sphnj {
 
 // The scene record of ctx with the cell lists of buffer `parity` bound.
 Scene scene_of(const sphnj_ctx *ctx, int parity);
-// Advances the host-side step state of ctx by one step and returns the kind
-// of launch sequence that step needs.
-StepKind advance(sphnj_ctx *ctx);
+// The kind of launch sequence the next step of ctx needs, from its host-side
+// step state, which is left unchanged.
+StepKind next_kind(const sphnj_ctx *ctx);
+// Advances the host-side step state of ctx past a step of kind k (its
+// next_kind), once that step's launches have been issued: a step whose
+// capture or launch fails leaves the state where it was, so a retry repeats
+// the same step.
+void commit_step(sphnj_ctx *ctx, const StepKind &k);
 // Copies the device error record of ctx to the host (synchronising its
 // stream) and turns it into a status and message.
 int check_device_error(sphnj_ctx *ctx);

@@ -112,6 +112,13 @@ __device__ __forceinline__ void raise_error(DevErr *e, int code, int a = 0, int 
     }
 }
 
+// Non-finite state: the update kernels raise SPHNJ_ERR_NONFINITE (kind,
+// particle index) for the first particle whose updated position, velocity or
+// density is NaN or infinite.  The reference steps on silently; values are
+// left as they are, so the check changes no result.
+__device__ __forceinline__ bool finite2(float2 a) { return isfinite(a.x) && isfinite(a.y); }
+__device__ __forceinline__ bool finite2(double2 a) { return isfinite(a.x) && isfinite(a.y); }
+
 // findPositionCell, pair.cu:8-18: x-major cell id from the float position,
 // (y - ymin) * inv_dy truncated toward zero plus the column index times ny.
 // Explicit round-to-nearest intrinsics keep the result independent of

@@ -1004,6 +1004,7 @@ template <class G, class F> __global__ void __launch_bounds__(kBlock) k_fluid_up
         d.f_rho[i] = rho;
         d.f_p[i] = density_to_pressure(p, rho, ph);
         d.f_vel[i] = v;
+        if (!(finite2(x) && finite2(v) && isfinite(rho))) raise_error(d.err, SPHNJ_ERR_NONFINITE, KF, i);
         float s2 = __fadd_rn(__fmul_rn(v.x, v.x), __fmul_rn(v.y, v.y));
         if (s2 == s2) sp2 = __float_as_uint(s2);  // NaN never wins, as on the host
         moved2 = disp2(x0, x);

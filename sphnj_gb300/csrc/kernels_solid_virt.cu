@@ -354,6 +354,7 @@ template <class G> __global__ void __launch_bounds__(256) k_solid_update(const _
     }
     d.s_pos[i] = x;
     d.s_vel[i] = v;
+    if (!(finite2(x) && finite2(v))) raise_error(d.err, SPHNJ_ERR_NONFINITE, KS, i);
 }
 
 // ---- mixed form -------------------------------------------------------------
@@ -531,6 +532,7 @@ template <class G> __global__ void __launch_bounds__(256) k_solid_update_mixed(c
     d.s_uc[i] = uc;
     d.s_v[i] = v;
     d.s_vc[i] = vc;
+    if (!(finite2(u) && finite2(v))) raise_error(d.err, SPHNJ_ERR_NONFINITE, KS, i);
     d.s_off[i] = solid_offset(p, d.s_rc[i], d.s_roff[i], u, d.s_cell[i]);
 }
 

@@ -34,14 +34,26 @@ constexpr int kMaxDevices = 64;
 std::mutex g_mu;
 int *g_scratch_ptr[kMaxDevices] = {};
 
-// Device address of g_rebuild_scratch for the current device.  In host code
-// the array's name is only a host-side stand-in, so the address must come
-// from cudaGetSymbolAddress, once per device, with that device current.
-int scratch_for_current_device(int **out) {
+// Device address of g_rebuild_scratch in the current context.  In host code
+// the array's name is only a host-side stand-in, so the address comes from
+// cudaGetSymbolAddress, called with the device current.  Outside a stream
+// capture it is looked up on every call, so that a caller on another context
+// of the same device, or after a cudaDeviceReset (which reloads the module),
+// gets the address of its own context; during a capture, where the lookup
+// could load the module, the address cached per device by an earlier call
+// is used (the first call on a device must therefore come before any
+// capture, as the header states).
+int scratch_for_current_device(cudaStream_t st, int **out) {
     int dev = 0;
     if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= kMaxDevices) return SPHNJ_ERR_NO_DEVICE;
+    cudaStreamCaptureStatus cap = cudaStreamCaptureStatusNone;
+    if (cudaStreamIsCapturing(st, &cap) != cudaSuccess) {
+        cudaGetLastError();
+        return SPHNJ_ERR_CUDA;
+    }
     std::lock_guard<std::mutex> lk(g_mu);
-    if (!g_scratch_ptr[dev]) {
+    if (cap == cudaStreamCaptureStatusNone || !g_scratch_ptr[dev]) {
+        if (cap != cudaStreamCaptureStatusNone) return SPHNJ_ERR_ARG;  // first call inside a capture
         void *ptr = nullptr;
         cudaError_t e = cudaGetSymbolAddress(&ptr, g_rebuild_scratch);
         if (e != cudaSuccess || !ptr) {
@@ -65,11 +77,11 @@ extern "C" int sphnj_rebuild_cell_lists_noalloc(int nx, int ny, int n_particles,
         return SPHNJ_ERR_ARG;
     if ((reinterpret_cast<uintptr_t>(prev_range) | reinterpret_cast<uintptr_t>(range_out)) & 7u)
         return SPHNJ_ERR_ARG;  // {start, count} pairs are read as 8-byte int2
+    cudaStream_t st = static_cast<cudaStream_t>(stream);
     int *scratch = nullptr;
-    int rc = scratch_for_current_device(&scratch);
+    int rc = scratch_for_current_device(st, &scratch);
     if (rc) return rc;
     const int C = nx * ny;
-    cudaStream_t st = static_cast<cudaStream_t>(stream);
     if (n_particles == 0) {
         // no particles: every cell starts at 0 and holds none
         cudaError_t e = cudaMemsetAsync(range_out, 0, sizeof(int32_t) * 2 * (size_t)C, st);

@@ -34,6 +34,9 @@ FIXTURES = {
     "gas": ("dam_break_gas", dict(dx=0.05, iend=200), 200, [0, 1, 51, 52], 10),
     "beam": ("beam", dict(dx=0.002, iend=2000, cfl=0.25), 2000, [0, 1, 51, 52], 10),
     "gate": ("gate", dict(dx=0.002, gas=False, layers=3, substeps=4, iend=200), 200, [0, 1, 51, 52], 10),
+    # the hydroelastic gate with air at 1000:1 (gas-liquid-solid coupling:
+    # fluidSolidCalculate with gas fluid, solidFluidCouple from gas)
+    "gate_air": ("gate", dict(dx=0.002, gas=True, layers=3, substeps=4, iend=200), 200, [0, 1, 51, 52], 10),
     "auxetic": ("auxetic_block", dict(dx=0.002, n=20, iend=200), 200, [0, 1, 51, 52, 200], 5),
 }
 

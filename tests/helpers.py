@@ -130,3 +130,17 @@ def golden_case(name):
     case = cases.by_name(gen, **kw)
     assert case.ini_text() == str(g["ini"]), f"{name}: generator output changed since the fixture was made"
     return case, g
+
+
+def record(name: str, payload: dict):
+    """Writes payload as <name>.json into $SPHNJ_RECORD_DIR when that is set
+    (the measured errors of the long comparisons, kept beside the numbers
+    they support); does nothing otherwise."""
+    import json
+    import os
+
+    out = os.environ.get("SPHNJ_RECORD_DIR")
+    if not out:
+        return
+    Path(out).mkdir(parents=True, exist_ok=True)
+    (Path(out) / f"{name}.json").write_text(json.dumps(payload, indent=1, sort_keys=True) + "\n")

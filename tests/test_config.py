@@ -170,3 +170,65 @@ def test_solid_boundary_column_is_optional(tmp_path):
     f.write_text("\n".join([rows[0]] + [" ".join(r.split()[:7]) for r in rows[1:]]) + "\n")
     p, arr = S.load_case(tmp_path / "b")
     assert np.all(arr["solid_boundary_type"] == 0)
+
+
+# order of the derived parameters the reference-build harness dumps
+# (oracle/ref/harness.cu `param_f` / `param_i`)
+PARAM_F = ["smoothing_length_square", "smoothing_length_inverse_square", "impact_distance_square",
+           "kernel_coefficient_1", "kernel_coefficient_2", "kernel_differential", "coefficient_3d_to_2d",
+           ("interval", 0), ("interval", 1), ("interval_inv", 0), ("interval_inv", 1),
+           ("coefficient_p2rho", 0), ("coefficient_p2rho", 1), ("coefficient_rho2p", 0),
+           ("coefficient_rho2p", 1), ("gamma_inv", 0), ("gamma_inv", 1), ("min_density", 0), ("min_density", 1),
+           "lambda_", "nu", "bulk_modulus", "solid_sound_speed", "dt", ("gravity", 1),
+           ("reference_density_inverse", 0), ("reference_density_inverse", 1)]
+PARAM_I = [("cell_number", 0), ("cell_number", 1), "cell_number_total", "fluid_number_total", "solid_number",
+           "virt_number"]
+
+
+def _field(p, f):
+    return getattr(p, f[0])[f[1]] if isinstance(f, tuple) else getattr(p, f)
+
+
+@pytest.mark.parametrize("name", ["water", "gas", "beam", "gate", "auxetic", "gate_air"])
+def test_derived_parameters_equal_the_reference_builds(name):
+    """The constants sphnj_params_derive gives (from the case's input.ini and
+    particle counts, through the library's own ini reader) are bit-identical
+    to the ones the reference's own build derived for the same case
+    (Parameter::initiate: kernel.cpp:25-41, properties.cpp:53-89,
+    domain.cpp:37-49), as its harness dumped them in the golden fixture."""
+    from helpers import golden, golden_case
+
+    if golden(name) is None:
+        pytest.skip("fixture not generated")
+    case, gz = golden_case(name)
+    p = case.params()
+    ref_f = np.asarray(gz["s0/param_f"], np.float32)
+    ref_i = np.asarray(gz["s0/param_i"], np.int32)
+    assert len(ref_f) == len(PARAM_F) and len(ref_i) == len(PARAM_I) + 1
+    got_f = np.array([_field(p, f) for f in PARAM_F], np.float32)
+    got_i = np.array([_field(p, f) for f in PARAM_I], np.int32)
+    bad = [(PARAM_F[k], float(got_f[k]), float(ref_f[k])) for k in range(len(PARAM_F))
+           if got_f[k].view(np.int32) != ref_f[k].view(np.int32)]
+    assert not bad, f"{name}: derived constants differ from the reference build's: {bad}"
+    assert np.array_equal(got_i, ref_i[:len(PARAM_I)]), (got_i, ref_i)
+
+
+@pytest.mark.parametrize("name", ["water", "gas", "beam", "gate", "auxetic", "gate_air"])
+def test_oracle_derives_the_same_parameters(name):
+    """The oracle's own ini reading and derivation (used where the product
+    library must not be loaded, e.g. the reference arm of the benchmark)
+    gives the library's parameters bit for bit, so both sides of every
+    comparison start from the reference build's constants."""
+    import oracle
+    from helpers import golden, golden_case
+
+    if golden(name) is None:
+        pytest.skip("fixture not generated")
+    case, gz = golden_case(name)
+    a, b = case.params(), oracle.params_for(case)
+    differ = [f for f, _ in abi.Params._fields_ if bytes(a)[getattr(abi.Params, f).offset:][:getattr(abi.Params, f).size]
+              != bytes(b)[getattr(abi.Params, f).offset:][:getattr(abi.Params, f).size]]
+    assert not differ, f"{name}: the oracle's parameters differ from the library's in {differ}"
+    ref_f = np.asarray(gz["s0/param_f"], np.float32)
+    got_f = np.array([_field(b, f) for f in PARAM_F], np.float32)
+    assert np.array_equal(got_f.view(np.int32), ref_f.view(np.int32))

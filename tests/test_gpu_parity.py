@@ -65,6 +65,8 @@ LOCKSTEP_CASES = {
     "gas": lambda: cases.dam_break_gas(dx=0.05),
     "beam": lambda: cases.beam(dx=0.002, cfl=0.25),
     "gate": lambda: cases.gate(dx=0.002, gas=False, layers=3, substeps=4),
+    # gas-liquid-solid: air at 1000:1 around the gate
+    "gate_air": lambda: cases.gate(dx=0.002, gas=True, layers=3, substeps=4),
     "auxetic": lambda: cases.auxetic_block(dx=0.002, n=20),
 }
 
@@ -105,7 +107,8 @@ def test_wall_normals_match_oracle():
         assert np.max(np.abs(a["virt_normal"] - b["virt_normal"])) < 1e-5
 
 
-@pytest.mark.parametrize("name,steps,tol", [("water", 200, 2e-3), ("gate", 100, 2e-3), ("beam", 200, 1e-3)])
+@pytest.mark.parametrize("name,steps,tol", [("water", 200, 2e-3), ("gate", 100, 2e-3), ("gate_air", 100, 2e-3),
+                                           ("beam", 200, 1e-3)])
 def test_free_run_against_oracle(name, steps, tol):
     """Independent runs from the same .dat input; differences grow with the
     step count, so the bound is looser than one step's."""
@@ -204,7 +207,7 @@ def test_sorted_order_and_partition():
 
 # ---- against the reference's own CUDA build ---------------------------------
 
-GOLDEN_NAMES = ["water", "gas", "beam", "gate", "auxetic"]
+GOLDEN_NAMES = ["water", "gas", "beam", "gate", "gate_air", "auxetic"]
 
 
 @pytest.mark.parametrize("name", GOLDEN_NAMES)
@@ -288,3 +291,48 @@ def test_cell_overflow_is_reported():
         with pytest.raises(S.SphnjError) as e:
             g.synchronize()
         assert e.value.code == abi.ERR_CELL_OVERFLOW
+
+
+@pytest.mark.parametrize("form", [abi.FORM_PLAIN, abi.FORM_MIXED])
+def test_nonfinite_fluid_state_is_reported(form):
+    """A NaN velocity injected on the host into an uploaded state: the
+    reference steps on silently; here the fluid update flags it and the next
+    synchronising call returns SPHNJ_ERR_NONFINITE (no device fault)."""
+    case = cases.dam_break_water(dx=0.05)
+    case.fluid_velocity[11] = [np.nan, 0.0]
+    p, arr = load(case)
+    with S.Simulation(p, form) as g:
+        g.upload(arr)
+        g.step(1)
+        with pytest.raises(S.SphnjError) as e:
+            g.synchronize()
+        assert e.value.code == abi.ERR_NONFINITE
+
+
+@pytest.mark.parametrize("form", [abi.FORM_PLAIN, abi.FORM_MIXED])
+def test_nonfinite_solid_state_is_reported(form):
+    case = cases.beam(dx=0.004)
+    case.solid_velocity[40] = [0.0, np.inf]
+    p, arr = load(case)
+    with S.Simulation(p, form) as g:
+        g.upload(arr)
+        g.step(1)
+        with pytest.raises(S.SphnjError) as e:
+            g.synchronize()
+        assert e.value.code == abi.ERR_NONFINITE
+
+
+def test_scene_in_a_batch_is_stepped_only_by_the_batch():
+    """sphnj_step on a scene that belongs to a batch is refused (its step
+    would move away from the batch's other scenes)."""
+    p, arr = load(cases.dam_break_water(dx=0.05))
+    with S.Simulation(p) as a, S.Simulation(p) as b:
+        a.upload(arr)
+        b.upload(arr)
+        with S.Batch([a, b]) as bt:
+            with pytest.raises(S.SphnjError) as e:
+                a.step(1)
+            assert e.value.code == abi.ERR_ARG
+            bt.step(2)
+            bt.synchronize()
+            assert a.step_index == b.step_index == 2

@@ -13,7 +13,7 @@ from sphnj_gb300.diagnostics import diagnostics
 from helpers import (CELL_IDS, FLUID_FIELDS, SOLID_FIELDS, VIRT_FIELDS, field_errors, golden, golden_case,
                      golden_cells, golden_state, load, nonempty)
 
-GOLDEN_NAMES = ["water", "gas", "beam", "gate", "auxetic"]
+GOLDEN_NAMES = ["water", "gas", "beam", "gate", "gate_air", "auxetic"]
 
 # oracle (IEEE float, no contraction) vs the reference build (-use_fast_math),
 # one step from an identical state; relative to each field's scale
@@ -106,6 +106,7 @@ def test_max_speed_matches_reference():
 @pytest.mark.parametrize("name,steps,cols,tol", [
     ("water", 200, ["front", "mom_x", "mom_y", "ek", "rho_sum"], 2e-3),
     ("beam", 2000, ["tip_x", "tip_y", "eks", "eps"], 2e-2),
+    ("gate_air", 200, ["front", "mom_x", "mom_y", "ek", "rho_sum", "eks", "eps"], 2e-3),
 ])
 def test_trajectory_matches_reference(name, steps, cols, tol):
     """Free-running oracle against the reference's own diagnostics."""
