@@ -61,6 +61,8 @@ def parse():
                          "form the metric names (default), or plain, the reference's precision")
     ap.add_argument("--no-sweep", action="store_true", help="skip the 256-scene batched sweep")
     ap.add_argument("--sweep-steps", type=int, default=20, help="timed steps of the 256-scene sweep")
+    ap.add_argument("--no-autotune", action="store_true",
+                    help="batched sweep: keep --tile-h and the default block sizes instead of autotuning")
     return ap.parse_args()
 
 
@@ -313,6 +315,9 @@ def run_sweep(args, stream):
         b.set_stream(stream.cuda_stream)
         b.set_tiling(True, args.tile_h)
         b.step(args.warmup)
+        # the launch shape and each size class's tile height chosen by the
+        # library's autotuner on this state (the state is put back)
+        tuned = None if args.no_autotune else b.autotune(steps=3)
         l0 = b.launches()
         ms = timed(lambda: b.step(K))
         launches = b.launches() - l0
@@ -325,7 +330,7 @@ def run_sweep(args, stream):
         for sim in sims:
             sim.close()
         total = sum(v[0] for v in prof.values())
-        out[name] = dict(rate(ms), launches_per_step=launches / K,
+        out[name] = dict(rate(ms), launches_per_step=launches / K, autotuned=tuned,
                          stage_share={k: round(v[0] / total, 4) for k, v in prof.items() if v[1]})
         out[name + "_over_plain"] = ms_plain / ms
     return {
@@ -367,6 +372,12 @@ def run_ours(args):
     sim.set_tiling(not args.untiled, args.tile_h)
     sim.set_graphs(not args.no_graphs)
     sim.upload(arr)
+    # launch shape chosen by the library's autotuner on the first step's state
+    # (tile height, lists, block sizes; the state is put back)
+    tuned = None
+    if not args.no_autotune and not args.untiled:
+        sim.step(1)
+        tuned = sim.autotune(steps=3)
 
     def barrier():
         if world > 1:
@@ -484,6 +495,10 @@ def run_ours(args):
         o.set_tiling(not args.untiled, args.tile_h)
         o.set_graphs(not args.no_graphs)
         o.upload(arr)
+        tuned_other = None
+        if not args.no_autotune and not args.untiled:
+            o.step(1)
+            tuned_other = o.autotune(steps=3)
         o.step(args.warmup)
         o.synchronize()
         barrier()
@@ -500,9 +515,9 @@ def run_ours(args):
         torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
         ms_other = float(t.item())
     names = {abi.FORM_PLAIN: "plain", abi.FORM_MIXED: "mixed"}
-    forms = {names[form]: {"value": value, "ms_per_step": ms / args.steps},
+    forms = {names[form]: {"value": value, "ms_per_step": ms / args.steps, "autotuned": tuned},
              names[other]: {"value": units * world * args.steps / (ms_other / 1e3),
-                            "ms_per_step": ms_other / args.steps}}
+                            "ms_per_step": ms_other / args.steps, "autotuned": tuned_other}}
     forms["mixed_over_plain"] = forms["plain"]["ms_per_step"] / forms["mixed"]["ms_per_step"]
     forms["error_vs_fp64_oracle"] = error_records()
 
@@ -541,7 +556,11 @@ def run_ours(args):
         "config": {"workload": f"gas-liquid dam break, 1.0x2.0 m water in a 4.0x3.0 m air-filled tank, dx={args.dx}",
                    "form": "plain (reference precision and cell-list order)" if form == abi.FORM_PLAIN else
                            "mixed (FP32 pair loops, cell + offset positions with Kahan integration)",
-                   "sweeps": "per-particle" if args.untiled else f"tiled, {args.tile_h} cells per tile",
+                   "sweeps": "per-particle" if args.untiled else
+                             (f"tiled, {args.tile_h} cells per tile" if tuned is None else
+                              f"tiled, autotuned: {tuned['tile_h']} cells per tile, lists {tuned['lists']}, "
+                              f"blocks {tuned['shift_block'] or 'default'} (shifting) / "
+                              f"{tuned['pair_block'] or 'default'} (pair)"),
                    "launch": "direct" if args.no_graphs else "one CUDA graph per kind of step", "n_fluid": nf, "n_liquid": p.fluid_number[0],
                    "n_solid": ns, "n_virt": nv, "cells": p.cell_number_total, "shift_per_step": p.shift_per_step,
                    "sort_every_step": p.sort_every_step, "dt": p.dt,

@@ -338,6 +338,13 @@ int  sphnj_set_tiling(sphnj_ctx *ctx, int tiled, int tile_h);
  * (sphnj_profile_enable) always launches individually. */
 int  sphnj_set_graphs(sphnj_ctx *ctx, int on);
 
+/* on != 0 (default): the kernels of a step are launched with programmatic
+ * stream serialisation (programmatic dependent launch), so that each kernel's
+ * blocks are scheduled while the previous kernel's last blocks still run and
+ * wait on the device for its results; 0 launches them plainly, one after the
+ * other.  Results are identical. */
+int  sphnj_set_launch_chaining(sphnj_ctx *ctx, int on);
+
 /* Tiled sweeps: on != 0 (default) stores per-step neighbour lists in the pair
  * pass for the shifting passes of the same step; 0 walks the 3x3 stencil in
  * every pass.  Results are identical.  sphnj_get_sweeps reports the current
@@ -345,16 +352,33 @@ int  sphnj_set_graphs(sphnj_ctx *ctx, int on);
 int  sphnj_set_neighbour_lists(sphnj_ctx *ctx, int on);
 int  sphnj_get_sweeps(const sphnj_ctx *ctx, int *tiled, int *tile_h, int *lists);
 
+/* Threads per block of the tiled sweeps: the shifting passes (64, 128 or
+ * 256) and the pair pass (128 or 256); 0 keeps each launch kind's default
+ * (128 for a dense scene's shifting passes and pair pass, 256 for a sparse
+ * scene's, 128 in batches).  Results are identical for every choice. */
+int  sphnj_set_block_sizes(sphnj_ctx *ctx, int shift_threads, int pair_threads);
+int  sphnj_get_block_sizes(const sphnj_ctx *ctx, int *shift_threads, int *pair_threads);
+
 /* Autotuner of the sweep configuration (no counterpart in the reference,
- * whose launch shape is fixed at thread_num = 32).  Candidates: one thread
- * per particle; tiles of 8, 12, 16, 24, 32 cells with stored neighbour lists;
- * tiles of 8, 16, 32 cells without.  Each runs `steps` steps from a device
- * copy of the current state (once to capture its graphs, once timed with CUDA
- * events); the state is put back after each trial, so tuning does not advance
- * or change the run.  The fastest candidate is installed and reported. */
+ * whose launch shape is fixed at thread_num = 32).  Coordinate search over:
+ * one thread per particle, or tiles of 8, 12, 16, 24, 32 cells with stored
+ * neighbour lists and of 8, 16, 32 cells without; then the shifting passes'
+ * block size (64, 128, 256 threads); then the pair pass's (128, 256).  For a
+ * batch (sphnj_batch_autotune) the scenes with fluid are then split at their
+ * median particle count into two size classes, and each class's tile height
+ * is tuned with the other's fixed.  Each candidate runs `steps` steps from a
+ * device copy of the current state (once to capture its graphs, once timed
+ * with CUDA events); the state is put back after each trial, so tuning does
+ * not advance or change the run.  The fastest candidate is installed and
+ * reported: tile_h / lists are those of class 0 (the only class of a single
+ * scene); class_split is the fluid particle count at which class 1 starts
+ * (0 with one class). */
 typedef struct sphnj_tuning {
     int32_t tiled, tile_h, lists, candidates;
     double  ms_per_step;
+    int32_t shift_block, pair_block;
+    int32_t size_classes, class_split;
+    int32_t class_tile_h[2], class_lists[2];
 } sphnj_tuning;
 int  sphnj_autotune(sphnj_ctx *ctx, int steps, sphnj_tuning *out);
 
@@ -471,8 +495,17 @@ int  sphnj_batch_set_stream(sphnj_batch *b, void *cuda_stream);
 /* As sphnj_set_tiling / sphnj_set_graphs, for every scene of the batch. */
 int  sphnj_batch_set_tiling(sphnj_batch *b, int tiled, int tile_h);
 int  sphnj_batch_set_graphs(sphnj_batch *b, int on);
+int  sphnj_batch_set_launch_chaining(sphnj_batch *b, int on);
 int  sphnj_batch_set_neighbour_lists(sphnj_batch *b, int on);
 int  sphnj_batch_get_sweeps(const sphnj_batch *b, int *tiled, int *tile_h, int *lists);
+/* One scene's own sweep shape inside the batch (scene = its index in the
+ * array given to sphnj_batch_create): the cells per tile and the list switch
+ * of that scene; the batch's launches are shared, each scene sweeps tiles of
+ * its own height.  Results are identical for every choice. */
+int  sphnj_batch_set_scene_tiling(sphnj_batch *b, int scene, int tile_h, int lists);
+int  sphnj_batch_get_scene_tiling(const sphnj_batch *b, int scene, int *tile_h, int *lists);
+/* As sphnj_set_block_sizes, for the batch's launches. */
+int  sphnj_batch_set_block_sizes(sphnj_batch *b, int shift_threads, int pair_threads);
 /* As sphnj_autotune, over the whole batch (every scene copied and put back). */
 int  sphnj_batch_autotune(sphnj_batch *b, int steps, sphnj_tuning *out);
 /* Advances every scene n fluid steps (asynchronous, as sphnj_step). */

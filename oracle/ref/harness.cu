@@ -9,11 +9,21 @@
 // per-particle array, the Cell lists and the derived Parameter values - in a
 // small binary format read by tests/golden/make_fixtures.py.
 //
-// usage (run directory prepared by oracle/ref/run_reference.py):
+// usage (run directory prepared by oracle/ref/build_ref.py):
 //   harness dump  <nsteps> <step,step,...> <out_prefix> [diag_every]
 //   harness time  <warmup> <steps>
+//   harness run   <global,global,...>
+// `run` is DeviceCalculation::calculation (calculation.cu:20-48) with its
+// outputs: per step Output::outputData, then the named global writers of
+// output.cu ("default" = Output::outputGlobalData, or any of edge,
+// total_force, wedge_disp, middle_position, end_position, tank_beam_end,
+// total_energy, crush_force, von_mises_stress, mean_pressure), then the
+// stages; a final outputData after the loop.  The reference's Windows paths
+// ("..\\..\\out\\...") become file names containing backslashes in the run
+// directory.
 #include "calculation.cuh"
 #include "function.cuh"
+#include "output.cuh"
 #include "memory_copy.cuh"
 #include "sim.cuh"
 
@@ -28,6 +38,8 @@
 #include <sstream>
 #include <string>
 #include <vector>
+
+#include <windows.h>
 
 namespace {
 
@@ -295,6 +307,44 @@ int main(int argc, char **argv) {
             }
             if (ms_log) std::fclose(ms_log);
             if (dg) std::fclose(dg);
+        } else if (mode == "run") {
+            std::vector<std::string> globals;
+            std::stringstream ss(argc > 2 ? argv[2] : "default");
+            std::string tok;
+            while (std::getline(ss, tok, ','))
+                if (!tok.empty()) globals.push_back(tok);
+            const std::string gpath = "..\\..\\out\\global";
+            SimTime *time = Sim::parameter.getTime();
+            while (time->addStep()) {
+                Output::outputData(sim);
+                CreateDirectory(gpath.c_str(), NULL);
+                for (const std::string &g : globals) {
+                    if (g == "default") Output::outputGlobalData(sim);
+                    else if (g == "edge") Output::outputEdge(sim, gpath);
+                    else if (g == "total_force") Output::outputTotalForce(sim, gpath);
+                    else if (g == "wedge_disp") Output::outputWedgeDisp(sim, gpath);
+                    else if (g == "middle_position") Output::outputMiddlePosition(sim, gpath);
+                    else if (g == "end_position") Output::outputEndPosition(sim, gpath);
+                    else if (g == "tank_beam_end") Output::outputTankBeamEnd(sim, gpath);
+                    else if (g == "total_energy") Output::outputTotalEnergy(sim, gpath);
+                    else if (g == "crush_force") Output::outputCrushForce(sim, gpath);
+                    else if (g == "von_mises_stress") Output::outputVonMisesStress(sim, gpath);
+                    else if (g == "mean_pressure") Output::outputMeanPressure(sim, gpath);
+                    else {
+                        std::fprintf(stderr, "unknown global writer %s\n", g.c_str());
+                        return 2;
+                    }
+                }
+                DeviceCalculation::particleCellUpdate();
+                DeviceCalculation::sortParticle(sim);
+                DeviceCalculation::fillCell();
+                DeviceCalculation::coupleCalculation();
+                DeviceCalculation::virtUpdate();
+                DeviceCalculation::fluidCalculation();
+                DeviceCalculation::solidCalculation(sim);
+                DeviceCalculation::fluidCorrection(sim);
+            }
+            Output::outputData(sim);
         } else if (mode == "time") {
             int warm = std::atoi(argv[2]), steps = std::atoi(argv[3]);
             for (int s = 0; s < warm; ++s) one_step(sim, nullptr);

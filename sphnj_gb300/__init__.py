@@ -176,6 +176,21 @@ class Simulation:
     def set_graphs(self, on: bool = True):
         self._check(self._lib.sphnj_set_graphs(self._h, 1 if on else 0), "set_graphs")
 
+    def set_launch_chaining(self, on: bool = True):
+        """Programmatic dependent launch between the kernels of a step
+        (sphnj_set_launch_chaining)."""
+        self._check(self._lib.sphnj_set_launch_chaining(self._h, 1 if on else 0), "set_launch_chaining")
+
+    def set_block_sizes(self, shift_threads: int = 0, pair_threads: int = 0):
+        """Threads per block of the tiled shifting passes and pair pass (0: the
+        launch kind's default; sphnj_set_block_sizes)."""
+        self._check(self._lib.sphnj_set_block_sizes(self._h, int(shift_threads), int(pair_threads)), "block_sizes")
+
+    def block_sizes(self) -> tuple:
+        a, b = C.c_int(), C.c_int()
+        self._check(self._lib.sphnj_get_block_sizes(self._h, C.byref(a), C.byref(b)), "block_sizes")
+        return a.value, b.value
+
     def set_neighbour_lists(self, on: bool = True):
         self._check(self._lib.sphnj_set_neighbour_lists(self._h, 1 if on else 0), "set_neighbour_lists")
 
@@ -337,6 +352,24 @@ class Batch:
 
     def set_graphs(self, on: bool = True):
         self._check(self._lib.sphnj_batch_set_graphs(self._h, 1 if on else 0), "set_graphs")
+
+    def set_launch_chaining(self, on: bool = True):
+        self._check(self._lib.sphnj_batch_set_launch_chaining(self._h, 1 if on else 0), "set_launch_chaining")
+
+    def set_block_sizes(self, shift_threads: int = 0, pair_threads: int = 0):
+        self._check(self._lib.sphnj_batch_set_block_sizes(self._h, int(shift_threads), int(pair_threads)),
+                    "block_sizes")
+
+    def set_scene_tiling(self, scene: int, tile_h: int, lists: bool = True):
+        """One scene's own tile height and list switch (sphnj_batch_set_scene_tiling)."""
+        self._check(self._lib.sphnj_batch_set_scene_tiling(self._h, int(scene), int(tile_h), 1 if lists else 0),
+                    "scene_tiling")
+
+    def scene_tiling(self, scene: int) -> tuple:
+        a, b = C.c_int(), C.c_int()
+        self._check(self._lib.sphnj_batch_get_scene_tiling(self._h, int(scene), C.byref(a), C.byref(b)),
+                    "scene_tiling")
+        return a.value, bool(b.value)
 
     def set_neighbour_lists(self, on: bool = True):
         self._check(self._lib.sphnj_batch_set_neighbour_lists(self._h, 1 if on else 0), "set_neighbour_lists")

@@ -141,11 +141,16 @@ INPUT_FIELDS = {
 class Tuning(C.Structure):
     """sphnj_tuning: the sweep configuration the autotuner chose."""
     _fields_ = [("tiled", C.c_int32), ("tile_h", C.c_int32), ("lists", C.c_int32), ("candidates", C.c_int32),
-                ("ms_per_step", C.c_double)]
+                ("ms_per_step", C.c_double), ("shift_block", C.c_int32), ("pair_block", C.c_int32),
+                ("size_classes", C.c_int32), ("class_split", C.c_int32), ("class_tile_h", C.c_int32 * 2),
+                ("class_lists", C.c_int32 * 2)]
 
     def as_dict(self) -> dict:
         return {"tiled": bool(self.tiled), "tile_h": self.tile_h, "lists": bool(self.lists),
-                "candidates": self.candidates, "ms_per_step": self.ms_per_step}
+                "candidates": self.candidates, "ms_per_step": self.ms_per_step,
+                "shift_block": self.shift_block, "pair_block": self.pair_block,
+                "size_classes": self.size_classes, "class_split": self.class_split,
+                "class_tile_h": list(self.class_tile_h), "class_lists": [bool(x) for x in self.class_lists]}
 
 
 class Diag(C.Structure):
@@ -235,6 +240,19 @@ def declare(lib: C.CDLL, prefix: str) -> None:
         g("batch_set_stream").argtypes = [vp, vp]
         g("batch_set_tiling").argtypes = [vp, C.c_int, C.c_int]
         g("batch_set_graphs").argtypes = [vp, C.c_int]
+        PIi_ = C.POINTER(C.c_int)
+        g("set_block_sizes").argtypes = [vp, C.c_int, C.c_int]
+        g("get_block_sizes").argtypes = [vp, PIi_, PIi_]
+        g("batch_set_block_sizes").argtypes = [vp, C.c_int, C.c_int]
+        g("batch_set_scene_tiling").argtypes = [vp, C.c_int, C.c_int, C.c_int]
+        g("batch_get_scene_tiling").argtypes = [vp, C.c_int, PIi_, PIi_]
+        for n in ("set_block_sizes", "get_block_sizes", "batch_set_block_sizes", "batch_set_scene_tiling",
+                  "batch_get_scene_tiling"):
+            g(n).restype = C.c_int
+        g("set_launch_chaining").argtypes = [vp, C.c_int]
+        g("set_launch_chaining").restype = C.c_int
+        g("batch_set_launch_chaining").argtypes = [vp, C.c_int]
+        g("batch_set_launch_chaining").restype = C.c_int
         g("batch_step").argtypes = [vp, C.c_int]
         g("batch_synchronize").argtypes = [vp]
         g("batch_profile_enable").argtypes = [vp, C.c_int]

@@ -34,6 +34,7 @@ struct sphnj_batch {
     Scene *d_recs[2] = {nullptr, nullptr};
     TileConfig tiles;
     bool use_graphs = true;
+    bool pdl = true;  // programmatic dependent launch between the kernels of a step
     std::map<int, StepGraph> graphs;
     std::set<int> planned;             // step kinds whose block tables exist
     Profiler prof;
@@ -82,6 +83,38 @@ void set_scene_streams(sphnj_batch *b, cudaStream_t st) {
     for (sphnj_ctx *c : b->scenes) c->st = st;
 }
 
+// The device records of every scene, list buffer 0 / 1 bound: the n scenes,
+// then the same with their position buffers exchanged.
+cudaError_t write_records(sphnj_batch *b) {
+    const int n = (int)b->scenes.size();
+    for (int par = 0; par < 2; ++par) {
+        b->recs[par].clear();
+        b->recs[par].reserve(2 * (size_t)n);
+        for (sphnj_ctx *c : b->scenes) b->recs[par].push_back(scene_of(c, par));
+        for (int k = 0; k < n; ++k) {
+            Scene s = b->recs[par][k];
+            exchange_positions(s, b->g.form);
+            b->recs[par].push_back(s);
+        }
+        if (!b->d_recs[par]) {
+            cudaError_t e = cudaMalloc(&b->d_recs[par], sizeof(Scene) * 2 * n);
+            if (e != cudaSuccess) return e;
+        }
+        cudaError_t e = cudaMemcpy(b->d_recs[par], b->recs[par].data(), sizeof(Scene) * 2 * n, cudaMemcpyHostToDevice);
+        if (e != cudaSuccess) return e;
+    }
+    return cudaSuccess;
+}
+
+// After a scene's sweep shape changed: new records, new block tables, new graphs.
+int refresh_records(sphnj_batch *b) {
+    drop_graphs(b);
+    b->planned.clear();
+    b->g.free_tables();
+    BCK(write_records(b));
+    return SPHNJ_OK;
+}
+
 }  // namespace
 
 extern "C" {
@@ -116,28 +149,18 @@ int sphnj_batch_create(sphnj_ctx *const *scenes, int n, sphnj_batch **out) {
         return SPHNJ_ERR_CUDA;
     }
     b->st = b->own;
-    for (int par = 0; par < 2; ++par) {
-        b->recs[par].reserve(2 * (size_t)n);
-        for (sphnj_ctx *c : b->scenes) b->recs[par].push_back(scene_of(c, par));
-        for (int k = 0; k < n; ++k) {
-            Scene s = b->recs[par][k];
-            exchange_positions(s, c0->form);
-            b->recs[par].push_back(s);
-        }
-        cudaError_t e = cudaMalloc(&b->d_recs[par], sizeof(Scene) * 2 * n);
-        if (e == cudaSuccess)
-            e = cudaMemcpy(b->d_recs[par], b->recs[par].data(), sizeof(Scene) * 2 * n, cudaMemcpyHostToDevice);
-        if (e != cudaSuccess) {
-            cudaGetLastError();
-            for (Scene *r : b->d_recs)
-                if (r) cudaFree(r);
-            cudaStreamDestroy(b->own);
-            delete b;
-            return SPHNJ_ERR_CUDA;
-        }
-    }
     b->g.n = n;
     b->g.form = c0->form;
+    // the batch's launch shape starts as its first scene's
+    b->tiles = c0->tiles;
+    if (write_records(b) != cudaSuccess) {
+        cudaGetLastError();
+        for (Scene *r : b->d_recs)
+            if (r) cudaFree(r);
+        cudaStreamDestroy(b->own);
+        delete b;
+        return SPHNJ_ERR_CUDA;
+    }
     if (configure_sweeps(b->tiles) != cudaSuccess) {
         cudaGetLastError();
         for (Scene *r : b->d_recs) cudaFree(r);
@@ -183,10 +206,12 @@ int sphnj_batch_set_tiling(sphnj_batch *b, int tiled, int tile_h) {
     BCK(cudaStreamSynchronize(b->st));
     b->tiles.tiled = tiled != 0;
     b->tiles.tile_h = tile_h;
-    drop_graphs(b);
-    b->planned.clear();  // tiled launches have their own tables
+    for (sphnj_ctx *c : b->scenes) {  // every scene takes the batch's shape
+        c->tiles.tiled = b->tiles.tiled;
+        c->tiles.tile_h = tile_h;
+    }
     BCK(configure_sweeps(b->tiles));
-    return SPHNJ_OK;
+    return refresh_records(b);
 }
 
 int sphnj_batch_set_neighbour_lists(sphnj_batch *b, int on) {
@@ -194,8 +219,40 @@ int sphnj_batch_set_neighbour_lists(sphnj_batch *b, int on) {
     cudaSetDevice(b->device);
     BCK(cudaStreamSynchronize(b->st));
     b->tiles.lists = on != 0;
-    drop_graphs(b);
+    for (sphnj_ctx *c : b->scenes) c->tiles.lists = b->tiles.lists;
+    return refresh_records(b);
+}
+
+int sphnj_batch_set_scene_tiling(sphnj_batch *b, int scene, int tile_h, int lists) {
+    if (!b || scene < 0 || scene >= (int)b->scenes.size() || tile_h < 1 || tile_h > 64) return SPHNJ_ERR_ARG;
+    cudaSetDevice(b->device);
+    BCK(cudaStreamSynchronize(b->st));
+    b->scenes[scene]->tiles.tile_h = tile_h;
+    b->scenes[scene]->tiles.lists = lists != 0;
+    return refresh_records(b);
+}
+
+int sphnj_batch_get_scene_tiling(const sphnj_batch *b, int scene, int *tile_h, int *lists) {
+    if (!b || scene < 0 || scene >= (int)b->scenes.size()) return SPHNJ_ERR_ARG;
+    if (tile_h) *tile_h = b->scenes[scene]->tiles.tile_h;
+    if (lists) *lists = b->scenes[scene]->tiles.lists ? 1 : 0;
     return SPHNJ_OK;
+}
+
+int sphnj_batch_set_block_sizes(sphnj_batch *b, int shift_threads, int pair_threads) {
+    if (!b) return SPHNJ_ERR_ARG;
+    if (!(shift_threads == 0 || shift_threads == 64 || shift_threads == 128 || shift_threads == 256) ||
+        !(pair_threads == 0 || pair_threads == 128 || pair_threads == 256))
+        return bfail(b, SPHNJ_ERR_ARG, "block sizes: shifting pass 0, 64, 128 or 256; pair pass 0, 128 or 256");
+    cudaSetDevice(b->device);
+    BCK(cudaStreamSynchronize(b->st));
+    b->tiles.shift_block = shift_threads;
+    b->tiles.pair_block = pair_threads;
+    for (sphnj_ctx *c : b->scenes) {
+        c->tiles.shift_block = shift_threads;
+        c->tiles.pair_block = pair_threads;
+    }
+    return refresh_records(b);
 }
 
 int sphnj_batch_get_sweeps(const sphnj_batch *b, int *tiled, int *tile_h, int *lists) {
@@ -203,6 +260,15 @@ int sphnj_batch_get_sweeps(const sphnj_batch *b, int *tiled, int *tile_h, int *l
     if (tiled) *tiled = b->tiles.tiled ? 1 : 0;
     if (tile_h) *tile_h = b->tiles.tile_h;
     if (lists) *lists = b->tiles.lists ? 1 : 0;
+    return SPHNJ_OK;
+}
+
+int sphnj_batch_set_launch_chaining(sphnj_batch *b, int on) {
+    if (!b) return SPHNJ_ERR_ARG;
+    cudaSetDevice(b->device);
+    BCK(cudaStreamSynchronize(b->st));
+    b->pdl = on != 0;
+    drop_graphs(b);
     return SPHNJ_OK;
 }
 
@@ -238,6 +304,7 @@ int sphnj_batch_step(sphnj_batch *b, int n) {
             }
         }
         GroupMany &g = b->g;
+        g.pdl = b->pdl;
         g.h_scenes = b->recs[k.parity].data();
         g.d_scenes = b->d_recs[k.parity];
         int rc = plan(b, k);
@@ -324,10 +391,22 @@ const char *sphnj_batch_last_error(const sphnj_batch *b) { return b ? b->msg.c_s
 
 namespace {
 
-int apply_batch(void *o, const TileConfig &t) {
+// Installs a candidate: the launch shape for the batch, and each scene its
+// size class's tile height and list switch (one record refresh).
+int apply_batch(void *o, const Tuned &t) {
     sphnj_batch *b = static_cast<sphnj_batch *>(o);
-    int rc = sphnj_batch_set_tiling(b, t.tiled ? 1 : 0, t.tile_h);
-    return rc ? rc : sphnj_batch_set_neighbour_lists(b, t.lists ? 1 : 0);
+    cudaSetDevice(b->device);
+    BCK(cudaStreamSynchronize(b->st));
+    b->tiles = t.launch;
+    for (size_t k = 0; k < b->scenes.size(); ++k) {
+        TileConfig &c = b->scenes[k]->tiles;
+        const int cls = k < t.cls.size() ? t.cls[k] : 0;
+        c = t.launch;
+        c.tile_h = t.tile_h[cls];
+        c.lists = t.lists[cls];
+    }
+    BCK(configure_sweeps(b->tiles));
+    return refresh_records(b);
 }
 int step_batch(void *o, int n) { return sphnj_batch_step(static_cast<sphnj_batch *>(o), n); }
 
@@ -340,15 +419,9 @@ int sphnj_batch_autotune(sphnj_batch *b, int steps, sphnj_tuning *out) {
     cudaSetDevice(b->device);
     BCK(cudaStreamSynchronize(b->st));
     TuneResult r{};
-    const int rc = tune_sweeps(b->scenes, b->st, steps, apply_batch, step_batch, b, &r);
+    const int rc = tune_sweeps(b->scenes, b->st, steps, true, apply_batch, step_batch, b, &r);
     if (rc) return rc == SPHNJ_ERR_CUDA ? bfail(b, rc, "batch autotune: CUDA error") : rc;
-    if (out) {
-        out->tiled = r.best.tiled ? 1 : 0;
-        out->tile_h = r.best.tile_h;
-        out->lists = r.best.lists ? 1 : 0;
-        out->candidates = r.tried;
-        out->ms_per_step = r.ms_per_step;
-    }
+    tuning_out(r, out);
     return SPHNJ_OK;
 }
 

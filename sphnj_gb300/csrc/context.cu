@@ -242,6 +242,8 @@ Scene scene_of(const sphnj_ctx *ctx, int parity) {
     s.sc = ctx->sc;
     s.payload = static_cast<char *>(ctx->payload);
     s.f_listed_total = ctx->f_listed_total;
+    s.tile_h = ctx->tiles.tile_h;
+    s.lists = ctx->tiles.lists ? 1 : 0;
     return s;
 }
 
@@ -565,6 +567,7 @@ extern "C" int sphnj_step(sphnj_ctx *ctx, int n) {
     for (int it = 0; it < n; ++it) {
         const StepKind k = next_kind(ctx);
         GroupOne g{scene_of(ctx, k.parity), ctx->form};
+        g.pdl = ctx->pdl;
         if (ctx->use_graphs && !ctx->prof.on) {
             auto it_g = ctx->graphs.find(k.key());
             if (it_g == ctx->graphs.end()) {
@@ -590,6 +593,15 @@ extern "C" int sphnj_step(sphnj_ctx *ctx, int n) {
 }
 
 extern "C" {
+
+int sphnj_set_launch_chaining(sphnj_ctx *ctx, int on) {
+    if (!ctx) return SPHNJ_ERR_ARG;
+    cudaSetDevice(ctx->device);
+    CK(cudaStreamSynchronize(ctx->st));
+    ctx->pdl = on != 0;
+    drop_graphs(ctx);
+    return SPHNJ_OK;
+}
 
 int sphnj_set_graphs(sphnj_ctx *ctx, int on) {
     if (!ctx) return SPHNJ_ERR_ARG;
@@ -728,6 +740,26 @@ int sphnj_set_neighbour_lists(sphnj_ctx *ctx, int on) {
     CK(cudaStreamSynchronize(ctx->st));
     ctx->tiles.lists = on != 0;
     drop_graphs(ctx);  // the pair pass takes the switch as a launch argument
+    return SPHNJ_OK;
+}
+
+int sphnj_set_block_sizes(sphnj_ctx *ctx, int shift_threads, int pair_threads) {
+    if (!ctx) return SPHNJ_ERR_ARG;
+    if (!(shift_threads == 0 || shift_threads == 64 || shift_threads == 128 || shift_threads == 256) ||
+        !(pair_threads == 0 || pair_threads == 128 || pair_threads == 256))
+        return fail(ctx, SPHNJ_ERR_ARG, "block sizes: shifting pass 0, 64, 128 or 256; pair pass 0, 128 or 256");
+    cudaSetDevice(ctx->device);
+    CK(cudaStreamSynchronize(ctx->st));
+    ctx->tiles.shift_block = shift_threads;
+    ctx->tiles.pair_block = pair_threads;
+    drop_graphs(ctx);
+    return SPHNJ_OK;
+}
+
+int sphnj_get_block_sizes(const sphnj_ctx *ctx, int *shift_threads, int *pair_threads) {
+    if (!ctx) return SPHNJ_ERR_ARG;
+    if (shift_threads) *shift_threads = ctx->tiles.shift_block;
+    if (pair_threads) *pair_threads = ctx->tiles.pair_block;
     return SPHNJ_OK;
 }
 

@@ -80,6 +80,7 @@ struct sphnj_ctx {
     int probe_cap = 0;
     sphnj::TileConfig tiles;
     bool use_graphs = true;  // replay each kind of step as a captured CUDA graph
+    bool pdl = true;         // programmatic dependent launch between the kernels of a step
     std::map<int, sphnj::StepGraph> graphs;
     sphnj_batch *batch = nullptr;  // the batch this scene belongs to, if any
     std::string msg = "ok";
@@ -107,13 +108,23 @@ int device_error_status(sphnj_ctx *ctx);
 // of the contexts' complete state, each candidate runs `steps` steps twice
 // (the first captures its graphs), the second timed with CUDA events on `st`;
 // the state is put back after every trial and at the end.  `apply` installs a
-// candidate, `step` advances every context; returns the fastest candidate.
+// candidate, `step` advances every context; with `classes` the scenes are
+// split into two size classes whose tile heights are tuned apart.  Returns
+// the fastest candidate.
+struct Tuned {
+    TileConfig launch;              // tiled switch and block sizes
+    int tile_h[2] = {16, 16};       // per size class
+    bool lists[2] = {true, true};
+    int split = 0;                  // fluid count at which class 1 starts (0: one class)
+    std::vector<int> cls;           // class of each context
+};
 struct TuneResult {
-    TileConfig best;
+    Tuned best;
     double ms_per_step;
     int tried;
 };
-int tune_sweeps(const std::vector<sphnj_ctx *> &ctxs, cudaStream_t st, int steps,
-                int (*apply)(void *, const TileConfig &), int (*step)(void *, int), void *obj, TuneResult *out);
+int tune_sweeps(const std::vector<sphnj_ctx *> &ctxs, cudaStream_t st, int steps, bool classes,
+                int (*apply)(void *, const Tuned &), int (*step)(void *, int), void *obj, TuneResult *out);
+void tuning_out(const TuneResult &r, sphnj_tuning *out);
 
 }  // namespace sphnj

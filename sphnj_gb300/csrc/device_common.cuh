@@ -259,6 +259,10 @@ struct Scene {
     ListScratch sc;
     char *payload;        // sort payload staging
     int *f_listed_total;  // fluid particles in the current lists (written by the list scans)
+    // sweep shape of this scene: cells per tile of the tiled neighbour sweeps
+    // and whether its pair pass stores neighbour lists (the scenes of a batch
+    // may have different shapes, chosen by size)
+    int tile_h, lists, pad_[2];
 };
 
 // Where a block finds its scene.  Every kernel of the step is a template over
@@ -303,9 +307,23 @@ struct Many {
     }
 };
 
+// Programmatic dependent launch: every kernel of a step is launched with
+// programmatic stream serialisation (when the context has it on), so that its
+// blocks can be scheduled while the previous kernel's last blocks still run.
+// Before a kernel reads anything an earlier kernel wrote it waits for the
+// previous grid to complete and its writes to be visible
+// (griddepcontrol.wait; a no-op in a launch without the attribute); then it
+// lets the next kernel's blocks be scheduled.  Only the block's scene lookup
+// (constant records and block tables) comes before the wait.
+__device__ __forceinline__ void pdl_enter() {
+    asm volatile("griddepcontrol.wait;" ::: "memory");
+    asm volatile("griddepcontrol.launch_dependents;" ::: "memory");
+}
+
 #define SPHNJ_SCENE(g)                                   \
     int blk, nblk;                                       \
     const ::sphnj::Scene &S = *(g).locate(blk, nblk);    \
+    ::sphnj::pdl_enter();                                \
     const sphnj_params &p = S.p;                         \
     const ::sphnj::DevState &d = S.d;                    \
     (void)nblk;                                          \

@@ -24,11 +24,16 @@ namespace sphnj {
 
 // How the fluid neighbour sweeps are launched: tiled (a block per column
 // segment of tile_h cells, neighbours staged in shared memory) or one thread
-// per particle.  Both give identical results.
+// per particle, and the block sizes of the tiled sweeps.  Every choice gives
+// identical results.  tile_h and lists are a scene's own (copied into its
+// record, so the scenes of a batch may differ); tiled and the block sizes
+// belong to a launch.
 struct TileConfig {
     bool tiled = true;
     int tile_h = 16;
-    bool lists = true;  // tiled: store per-step neighbour lists (else walk the stencil in every pass)
+    bool lists = true;    // tiled: store per-step neighbour lists (else walk the stencil in every pass)
+    int shift_block = 0;  // threads per block of the tiled shifting passes: 64, 128, 256 (0: per launch kind)
+    int pair_block = 0;   // threads per block of the tiled pair pass: 128, 256 (0: per launch kind)
 };
 
 // Launch sites: a batch keeps one block table per (site, argument).
@@ -56,6 +61,7 @@ struct GroupOne {
     using Dev = One;
     Scene s;
     int form = SPHNJ_FORM_PLAIN;
+    bool pdl = false;  // launch with programmatic stream serialisation
     template <class F> bool prepare(long long, F &&blocks_of, unsigned &blocks, Dev &dev) {
         blocks = blocks_of(s);
         dev.s = s;
@@ -70,6 +76,7 @@ struct GroupMany {
     const Scene *h_scenes = nullptr;  // host copies of the first n records of d_scenes
     int n = 0;
     int form = SPHNJ_FORM_PLAIN;      // every scene of a group has the same form
+    bool pdl = false;                 // launch with programmatic stream serialisation
     // device records of the current list parity: n records, then the same n
     // with their position buffers exchanged
     const Scene *d_scenes = nullptr;
@@ -147,7 +154,23 @@ int launch(G &g, long long key, F &&blocks_of, void (*kern)(typename G::Dev, P..
     unsigned blocks = 0;
     typename G::Dev dev;
     if (!g.prepare(key, blocks_of, blocks, dev)) return 0;
-    kern<<<blocks, threads, smem, st>>>(dev, std::forward<A>(a)...);
+    if (g.pdl) {
+        // programmatic dependent launch: the kernel waits for its predecessor
+        // in pdl_enter (SPHNJ_SCENE), so its blocks may be scheduled early
+        cudaLaunchAttribute at[1];
+        at[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+        at[0].val.programmaticStreamSerializationAllowed = 1;
+        cudaLaunchConfig_t cfg = {};
+        cfg.gridDim = dim3(blocks);
+        cfg.blockDim = dim3(threads);
+        cfg.dynamicSmemBytes = smem;
+        cfg.stream = st;
+        cfg.attrs = at;
+        cfg.numAttrs = 1;
+        cudaLaunchKernelEx(&cfg, kern, dev, std::forward<A>(a)...);  // errors: cudaGetLastError of the caller
+    } else {
+        kern<<<blocks, threads, smem, st>>>(dev, std::forward<A>(a)...);
+    }
     return 1;
 }
 
@@ -186,10 +209,10 @@ template <class G> int launch_virt_index(cudaStream_t st, G &g);
 // list buffer `parity` (pair.cu:66-181)
 template <class G> int launch_rebuild_kind(cudaStream_t st, G &g, Kind k, int parity);
 
-// this step's active tiles of the tiled sweeps (tile height tile_h) into
-// d.tile_list / d.tile_count, in tile order: for every scene with fluid
-// (all_scenes) or for the scenes that sweep_compacted() selects
-template <class G> int launch_tile_compact(cudaStream_t st, G &g, int tile_h, bool all_scenes);
+// this step's active tiles of the tiled sweeps (each scene's own tile
+// height) into d.tile_list / d.tile_count, in tile order: for every scene
+// with fluid (all_scenes) or for the scenes that sweep_compacted() selects
+template <class G> int launch_tile_compact(cudaStream_t st, G &g, bool all_scenes);
 
 // per-cell capacity check against the reference's 64 slots
 template <class G> int launch_capacity_check(cudaStream_t st, G &g);

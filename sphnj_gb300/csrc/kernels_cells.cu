@@ -217,16 +217,16 @@ __global__ void __launch_bounds__(kBlock) k_scan_tile(const __grid_constant__ G 
 }
 
 // In-place exclusive scan of the tile sums (<= SCAN_MAX_TILES) by one block:
-// of the cell scans (sweep_tile_h == 0: one sum per 1024 cells) or of the
-// sweep-tile compaction (one sum per 1024 sweep tiles of height sweep_tile_h).
+// of the cell scans (sweep_tiles == 0: one sum per 1024 cells) or of the
+// sweep-tile compaction (one sum per 1024 sweep tiles of the scene's tile
+// height).
 // The grand total goes to the scene's listed-particle count (total_to 1), its
 // active-tile count (2) or nowhere (0).
 template <class G>
-__global__ void __launch_bounds__(1024) k_scan_sums(const __grid_constant__ G g, int total_to, int sweep_tile_h) {
+__global__ void __launch_bounds__(1024) k_scan_sums(const __grid_constant__ G g, int total_to, int sweep_tiles_) {
     SPHNJ_SCENE(g);
     __shared__ int ws[33];
-    const int units = sweep_tile_h > 0 ? p.cell_number[0] * ((p.cell_number[1] + sweep_tile_h - 1) / sweep_tile_h)
-                                       : p.cell_number_total;
+    const int units = sweep_tiles_ ? sweep_tiles(p, S.tile_h) : p.cell_number_total;
     const int ntiles = (units + SCAN_TILE - 1) / SCAN_TILE;
     int *sums = S.sc.sums;
     int *total = total_to == 1 ? S.f_listed_total : total_to == 2 ? d.tile_count : nullptr;
@@ -282,8 +282,9 @@ __device__ __forceinline__ bool tile_active(const sphnj_params &p, const DevStat
     return h1.x + h1.y > h0.x;
 }
 
-template <class G> __global__ void __launch_bounds__(kBlock) k_tile_flag_scan(const __grid_constant__ G g, int tile_h) {
+template <class G> __global__ void __launch_bounds__(kBlock) k_tile_flag_scan(const __grid_constant__ G g) {
     SPHNJ_SCENE(g);
+    const int tile_h = S.tile_h;
     const int nt = sweep_tiles(p, tile_h);
     const ListScratch &sc = S.sc;
     const int t0 = blk * SCAN_TILE + threadIdx.x * 4;
@@ -304,8 +305,9 @@ template <class G> __global__ void __launch_bounds__(kBlock) k_tile_flag_scan(co
     if (threadIdx.x == 0) sc.sums[blk] = total;
 }
 
-template <class G> __global__ void k_tile_scatter(const __grid_constant__ G g, int tile_h) {
+template <class G> __global__ void k_tile_scatter(const __grid_constant__ G g) {
     SPHNJ_SCENE(g);
+    const int tile_h = S.tile_h;
     const int t = blk * blockDim.x + threadIdx.x;
     if (t < sweep_tiles(p, tile_h) && tile_active(p, d, t, tile_h))
         d.tile_list[cell_start(S.sc.local, S.sc.sums, t)] = t;
@@ -718,22 +720,22 @@ template <class G> int launch_rebuild_kind(cudaStream_t st, G &g, Kind k, int pa
     return n;
 }
 
-template <class G> int launch_tile_compact(cudaStream_t st, G &g, int tile_h, bool all_scenes) {
+template <class G> int launch_tile_compact(cudaStream_t st, G &g, bool all_scenes) {
     using D = typename G::Dev;
-    auto has = [tile_h, all_scenes](const Scene &s) {
-        return all_scenes ? s.p.fluid_number_total > 0 : sweep_compacted(s.p, tile_h);
+    auto has = [all_scenes](const Scene &s) {
+        return all_scenes ? s.p.fluid_number_total > 0 : sweep_compacted(s.p, s.tile_h);
     };
     int n = launch(
-        g, site_key(SITE_TILE_COMPACT, tile_h),
-        [&](const Scene &s) { return has(s) ? grid_for(sweep_tiles(s.p, tile_h), SCAN_TILE) : 0u; },
-        k_tile_flag_scan<D>, kBlock, 0, st, tile_h);
+        g, site_key(SITE_TILE_COMPACT),
+        [&](const Scene &s) { return has(s) ? grid_for(sweep_tiles(s.p, s.tile_h), SCAN_TILE) : 0u; },
+        k_tile_flag_scan<D>, kBlock, 0, st);
     n += launch(
-        g, site_key(SITE_TILE_SUMS, tile_h), [&](const Scene &s) { return has(s) ? 1u : 0u; }, k_scan_sums<D>, 1024, 0,
-        st, 2, tile_h);
+        g, site_key(SITE_TILE_SUMS), [&](const Scene &s) { return has(s) ? 1u : 0u; }, k_scan_sums<D>, 1024, 0, st, 2,
+        1);
     n += launch(
-        g, site_key(SITE_TILE_SCATTER, tile_h),
-        [&](const Scene &s) { return has(s) ? grid_for(sweep_tiles(s.p, tile_h), kBlock) : 0u; }, k_tile_scatter<D>,
-        kBlock, 0, st, tile_h);
+        g, site_key(SITE_TILE_SCATTER),
+        [&](const Scene &s) { return has(s) ? grid_for(sweep_tiles(s.p, s.tile_h), kBlock) : 0u; }, k_tile_scatter<D>,
+        kBlock, 0, st);
     return n;
 }
 
@@ -748,6 +750,6 @@ SPHNJ_INSTANTIATE_GROUPS(launch_sort_kind, Kind, int);
 SPHNJ_INSTANTIATE_GROUPS(launch_virt_index);
 SPHNJ_INSTANTIATE_GROUPS(launch_rebuild_kind, Kind, int);
 SPHNJ_INSTANTIATE_GROUPS(launch_capacity_check);
-SPHNJ_INSTANTIATE_GROUPS(launch_tile_compact, int, bool);
+SPHNJ_INSTANTIATE_GROUPS(launch_tile_compact, bool);
 
 }  // namespace sphnj

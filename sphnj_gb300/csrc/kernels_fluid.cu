@@ -72,6 +72,16 @@ template <> struct PairShape<GroupOne, false, FormMixed> {
 template <class F> struct PairShape<GroupOne, true, F> {
     static constexpr int threads = 256, min_blocks = 5;
 };
+// The block shapes an autotuner may choose instead (TileConfig::pair_block):
+// 128 threads at 8 blocks per SM (7 in the mixed form's dense launch) or 256
+// at 4 (5 in a list launch, whose kernel holds 48 registers).
+template <class F, bool kList, int kT> struct PairBlock;
+template <class F, bool kList> struct PairBlock<F, kList, 128> {
+    static constexpr int threads = 128, min_blocks = (!kList && F::kMixed) ? 7 : 8;
+};
+template <class F, bool kList> struct PairBlock<F, kList, 256> {
+    static constexpr int threads = 256, min_blocks = kList ? 5 : 4;
+};
 constexpr int kMaxPerCell = 24;  // staged particles per cell at most
 
 // Particles per cell the pair pass stages (a tile with more falls back to the
@@ -802,8 +812,9 @@ __device__ __forceinline__ Frame tile_frame(const sphnj_params &p, const DevStat
 // sweeps tile b, returning at once if it is empty.
 template <class G, class F, bool kList, int kThreads, int kMinBlocks>
 __global__ void __launch_bounds__(kThreads, kMinBlocks)
-    k_fluid_pair_tiled(const __grid_constant__ G gs, int tile_h, int cap, int use_lists) {
+    k_fluid_pair_tiled(const __grid_constant__ G gs, int cap) {
     SPHNJ_SCENE(gs);
+    const int tile_h = S.tile_h, use_lists = S.lists;
     extern __shared__ __align__(16) unsigned char smem[];
     __shared__ int s_base[3], s_off[3];
     float2 *s_pos = reinterpret_cast<float2 *>(smem);
@@ -860,8 +871,9 @@ __global__ void __launch_bounds__(kThreads, kMinBlocks)
 // sweep: 4.81 -> 4.52 ms/step; 4.15M dam break: 3.92 -> 3.80).
 template <class G, class F, bool kList, int kThreads>
 __global__ void __launch_bounds__(kThreads, 2048 / kThreads)
-    k_shift_gradient_tiled(const __grid_constant__ G gs, int tile_h, int cap, int pass) {
+    k_shift_gradient_tiled(const __grid_constant__ G gs, int cap, int pass) {
     SPHNJ_SCENE(gs);
+    const int tile_h = S.tile_h;
     extern __shared__ __align__(16) unsigned char smem[];
     __shared__ int s_base[3], s_off[3];
     float2 *s_pos = reinterpret_cast<float2 *>(smem);
@@ -1042,37 +1054,44 @@ constexpr size_t kPairSmemPerEntry = 3 * sizeof(float2) + sizeof(int) + 1;
 
 }  // namespace
 
-cudaError_t configure_sweeps(const TileConfig &tc) {
-    using PDp = PairShape<GroupOne, false, FormPlain>;
-    using PDm = PairShape<GroupOne, false, FormMixed>;
-    using PLp = PairShape<GroupOne, true, FormPlain>;
-    using PLm = PairShape<GroupOne, true, FormMixed>;
-    using PMp = PairShape<GroupMany, true, FormPlain>;
-    using PMm = PairShape<GroupMany, true, FormMixed>;
-    // dynamic shared memory above 48 KB needs an opt-in (every launch stages
-    // at most kMaxPerCell per cell)
-    const int a = cudaFuncAttributeMaxDynamicSharedMemorySize;
-    const size_t smem = tile_cap(tc.tile_h, kMaxPerCell) * kPairSmemPerEntry;
-    const std::pair<const void *, size_t> kernels[] = {
-        {(const void *)k_fluid_pair_tiled<One, FormPlain, false, PDp::threads, PDp::min_blocks>, smem},
-        {(const void *)k_fluid_pair_tiled<One, FormPlain, true, PLp::threads, PLp::min_blocks>, smem},
-        {(const void *)k_fluid_pair_tiled<One, FormMixed, false, PDm::threads, PDm::min_blocks>, smem},
-        {(const void *)k_fluid_pair_tiled<One, FormMixed, true, PLm::threads, PLm::min_blocks>, smem},
-        {(const void *)k_fluid_pair_tiled<Many, FormPlain, true, PMp::threads, PMp::min_blocks>, smem},
-        {(const void *)k_fluid_pair_tiled<Many, FormMixed, true, PMm::threads, PMm::min_blocks>, smem}};
-    for (const auto &k : kernels) {
-        if (k.second <= 48 * 1024) continue;
-        const cudaError_t e = cudaFuncSetAttribute(k.first, (cudaFuncAttribute)a, (int)k.second);
-        if (e != cudaSuccess) return e;
-    }
-    return cudaSuccess;
+// Every pair-pass instantiation may stage up to kMaxPerCell particles per
+// cell of the tallest tile (64 cells): its dynamic shared memory above 48 KB
+// needs an opt-in, given once for the largest size.
+template <class D, class F, bool kList, int kT, int kMin> cudaError_t allow_pair_smem() {
+    const size_t smem = tile_cap(64, kMaxPerCell) * kPairSmemPerEntry;
+    return cudaFuncSetAttribute((const void *)k_fluid_pair_tiled<D, F, kList, kT, kMin>,
+                                cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+}
+template <class D, class G, class F, bool kList> cudaError_t allow_pair_smem_all() {
+    using Sh = PairShape<G, kList, F>;
+    cudaError_t e = allow_pair_smem<D, F, kList, Sh::threads, Sh::min_blocks>();
+    if (e == cudaSuccess) e = allow_pair_smem<D, F, kList, 128, PairBlock<F, kList, 128>::min_blocks>();
+    if (e == cudaSuccess) e = allow_pair_smem<D, F, kList, 256, PairBlock<F, kList, 256>::min_blocks>();
+    return e;
+}
+
+cudaError_t configure_sweeps(const TileConfig &) {
+    cudaError_t e = allow_pair_smem_all<One, GroupOne, FormPlain, false>();
+    if (e == cudaSuccess) e = allow_pair_smem_all<One, GroupOne, FormPlain, true>();
+    if (e == cudaSuccess) e = allow_pair_smem_all<One, GroupOne, FormMixed, false>();
+    if (e == cudaSuccess) e = allow_pair_smem_all<One, GroupOne, FormMixed, true>();
+    if (e == cudaSuccess) e = allow_pair_smem_all<Many, GroupMany, FormPlain, true>();
+    if (e == cudaSuccess) e = allow_pair_smem_all<Many, GroupMany, FormMixed, true>();
+    return e;
 }
 
 // Single scenes use the active-tile list when sweep_compacted() selects it;
 // batches always do (their scenes share one kernel).
-template <class G> bool use_tile_list(const G &g, int tile_h) {
+template <class G> bool use_tile_list(const G &g) {
     if constexpr (std::is_same<G, GroupMany>::value) return true;
-    else return sweep_compacted(g.s.p, tile_h);
+    else return sweep_compacted(g.s.p, g.s.tile_h);
+}
+// The tallest tile of the group's scenes (sizes a launch's staging).
+inline int max_tile_h(const GroupOne &g) { return g.s.tile_h; }
+inline int max_tile_h(const GroupMany &g) {
+    int h = 1;
+    for (int k = 0; k < g.n; ++k) h = std::max(h, g.h_scenes[k].tile_h);
+    return h;
 }
 
 // Per-particle fallback grid of one scene (grid-stride; it returns at once
@@ -1086,36 +1105,49 @@ inline unsigned fallback_blocks(int n) {
 
 namespace {
 
+// The tiled pair pass with block shape Sh: list launches get about one
+// block per tile the fluid can fill (twice that at 128 threads), a dense
+// scene one block per tile.  Each scene sweeps tiles of its own height.
+template <class F, class G, bool kList, class Sh>
+int pair_tiled(cudaStream_t st, G &g, int cap, size_t smem) {
+    using D = typename G::Dev;
+    const long long key = site_key(SITE_PAIR_TILED, Sh::threads);
+    if constexpr (kList)
+        return launch(
+            g, key,
+            [](const Scene &s) {
+                return std::min<unsigned>(tile_blocks(s.p, s.tile_h),
+                                          sweep_blocks(s.p, s.tile_h) * (kTileBlock / Sh::threads));
+            },
+            k_fluid_pair_tiled<D, F, true, Sh::threads, Sh::min_blocks>, Sh::threads, smem, st, cap);
+    else
+        return launch(
+            g, key, [](const Scene &s) { return tile_blocks(s.p, s.tile_h); },
+            k_fluid_pair_tiled<D, F, false, Sh::threads, Sh::min_blocks>, Sh::threads, smem, st, cap);
+}
+
+template <class F, class G, bool kList> int pair_tiled_shape(cudaStream_t st, G &g, const TileConfig &tc, int cap) {
+    const size_t smem = cap * kPairSmemPerEntry;
+    if (tc.pair_block == 128) return pair_tiled<F, G, kList, PairBlock<F, kList, 128>>(st, g, cap, smem);
+    if (tc.pair_block == 256) return pair_tiled<F, G, kList, PairBlock<F, kList, 256>>(st, g, cap, smem);
+    return pair_tiled<F, G, kList, PairShape<G, kList, F>>(st, g, cap, smem);
+}
+
 template <class F, class G> int fluid_pair(cudaStream_t st, G &g, const TileConfig &tc) {
     using D = typename G::Dev;
     if (!tc.tiled)
         return launch(
             g, site_key(SITE_PAIR_EACH), [](const Scene &s) { return grid_for(s.p.fluid_number_total, kPairBlock); },
             k_fluid_pair_each<D, F>, kPairBlock, 0, st, 0);
-    const bool list = use_tile_list(g, tc.tile_h);
-    const int cap = tile_cap(tc.tile_h, pair_per_cell(g, list));
-    const size_t smem = cap * kPairSmemPerEntry;
+    const bool list = use_tile_list(g);
+    const int cap = tile_cap(max_tile_h(g), pair_per_cell(g, list));
     // this step's active tiles (the cell lists are final), used by the pair
     // pass and every shifting pass of the step
-    int n = launch_tile_compact(st, g, tc.tile_h, std::is_same<G, GroupMany>::value);
-    // list launches: about one block per tile the fluid can fill, twice that
-    // at 128 threads; a dense scene: one block per tile
-    auto blocks = [&](const Scene &s) {
-        return std::min<unsigned>(tile_blocks(s.p, tc.tile_h),
-                                  sweep_blocks(s.p, tc.tile_h) * (kTileBlock / PairShape<G, true, F>::threads));
-    };
-    const int lists = tc.lists ? 1 : 0;
-    const long long key = site_key(SITE_PAIR_TILED, tc.tile_h);
+    int n = launch_tile_compact(st, g, std::is_same<G, GroupMany>::value);
     if (list) {
-        using Shape = PairShape<G, true, F>;
-        n += launch(g, key, blocks, k_fluid_pair_tiled<D, F, true, Shape::threads, Shape::min_blocks>, Shape::threads,
-                    smem, st, tc.tile_h, cap, lists);
+        n += pair_tiled_shape<F, G, true>(st, g, tc, cap);
     } else if constexpr (!std::is_same<G, GroupMany>::value) {  // batches always sweep their lists
-        using Shape = PairShape<G, false, F>;
-        n += launch(
-            g, key, [&](const Scene &s) { return tile_blocks(s.p, tc.tile_h); },
-            k_fluid_pair_tiled<D, F, false, Shape::threads, Shape::min_blocks>, Shape::threads, smem, st, tc.tile_h,
-            cap, lists);
+        n += pair_tiled_shape<F, G, false>(st, g, tc, cap);
     }
     n += launch(
         g, site_key(SITE_PAIR_FALLBACK), [](const Scene &s) { return fallback_blocks(s.p.fluid_number_total); },
@@ -1152,25 +1184,36 @@ template <class F, class G> int shift_pass(cudaStream_t st, G &g, const TileConf
             g, site_key(SITE_SHIFT_EACH, pass),
             [&](const Scene &s) { return active(s) ? grid_for(s.p.fluid_number_total, kPairBlock) : 0u; },
             k_shift_gradient_each<D, F>, kPairBlock, 0, st, 0, pass);
-    const int cap = tile_cap(tc.tile_h);
-    auto blocks = [&](const Scene &s) { return active(s) ? sweep_blocks(s.p, tc.tile_h) : 0u; };
-    const long long key = site_key(SITE_SHIFT_TILED, (tc.tile_h << 8) | pass);
+    const int cap = tile_cap(max_tile_h(g));
     const size_t smem = cap * sizeof(float2);
     // batched list launches: blocks of kListBlock threads, kTileBlock / kListBlock
     // times as many (a sparse scene swept alone, one short launch, keeps the
     // larger blocks: measured 116 against 132 ms/step on the sweep's scenes
     // stepped one by one).  A dense scene: one block of kDenseBlock threads
     // per tile (4.15M dam break 3.92 -> 3.80 ms/step against 256 threads;
-    // 64 threads: 4.39, 512: 4.73).
-    constexpr int kT = std::is_same<G, GroupMany>::value ? kListBlock : kTileBlock;
-    auto list_blocks = [&](const Scene &s) {
-        return active(s) ? std::min<unsigned>(tile_blocks(s.p, tc.tile_h), sweep_blocks(s.p, tc.tile_h) * (kTileBlock / kT))
-                         : 0u;
+    // 64 threads: 4.39, 512: 4.73).  tc.shift_block overrides either.
+    constexpr int kDefaultList = std::is_same<G, GroupMany>::value ? kListBlock : kTileBlock;
+    const bool list = use_tile_list(g);
+    const int kT = tc.shift_block ? tc.shift_block : list ? kDefaultList : kDenseBlock;
+    const long long key = site_key(SITE_SHIFT_TILED, (kT << 8) | pass);
+    auto go = [&](auto threads) {
+        constexpr int T = decltype(threads)::value;
+        if (list)
+            return launch(
+                g, key,
+                [&](const Scene &s) {
+                    return active(s) ? std::min<unsigned>(tile_blocks(s.p, s.tile_h),
+                                                          sweep_blocks(s.p, s.tile_h) * std::max(1, kTileBlock / T))
+                                     : 0u;
+                },
+                k_shift_gradient_tiled<D, F, true, T>, T, smem, st, cap, pass);
+        return launch(
+            g, key, [&](const Scene &s) { return active(s) ? sweep_blocks(s.p, s.tile_h) : 0u; },
+            k_shift_gradient_tiled<D, F, false, T>, T, smem, st, cap, pass);
     };
-    int n = use_tile_list(g, tc.tile_h)
-                ? launch(g, key, list_blocks, k_shift_gradient_tiled<D, F, true, kT>, kT, smem, st, tc.tile_h, cap, pass)
-                : launch(g, key, blocks, k_shift_gradient_tiled<D, F, false, kDenseBlock>, kDenseBlock, smem, st,
-                         tc.tile_h, cap, pass);
+    int n = kT == 64 ? go(std::integral_constant<int, 64>{})
+            : kT == 256 ? go(std::integral_constant<int, 256>{})
+                        : go(std::integral_constant<int, 128>{});
     n += launch(
         g, site_key(SITE_SHIFT_FALLBACK, pass),
         [&](const Scene &s) { return active(s) ? fallback_blocks(s.p.fluid_number_total) : 0u; },

@@ -46,9 +46,12 @@ const char *kUsage =
     "  --result-interval N   VTK output interval (default: the ini's result_interval)\n"
     "  --no-vtk              no VTK output\n"
     "  --global-every N      global data every N steps (default 1; 0 = none)\n"
-    "  --global LIST         comma-separated global files: total_force, von_mises_stress,\n"
-    "                        mean_pressure, frontier, total_energy, tip_disp\n"
-    "                        (default total_force,von_mises_stress,mean_pressure)\n"
+    "  --global LIST         comma-separated global writers of output.cu: total_force,\n"
+    "                        wedge_disp, von_mises_stress, mean_pressure (the four that\n"
+    "                        Output::outputGlobalData calls: 'default'), edge (frontier.dat\n"
+    "                        and height.dat), frontier, total_energy, end_position,\n"
+    "                        middle_position, tank_beam_end, crush_force, and tip_disp\n"
+    "                        (default: default)\n"
     "  --probe X,Y           a probe point (repeatable), written to global/probe-<id>.dat\n"
     "  --restart FILE        start from a checkpoint instead of the .dat files\n"
     "  --checkpoint-every N  write OUT/checkpoint-<step>.bin every N steps\n"
@@ -60,7 +63,7 @@ struct Args {
     int form = SPHNJ_FORM_PLAIN;
     long iend = -1, result_interval = -1, global_every = 1, checkpoint_every = 0, autotune = 0;
     bool vtk = true, quiet = false;
-    std::vector<std::string> global = {"total_force", "von_mises_stress", "mean_pressure"};
+    std::vector<std::string> global = {"total_force", "wedge_disp", "von_mises_stress", "mean_pressure"};
     std::vector<std::pair<float, float>> probes;
 };
 
@@ -102,8 +105,14 @@ Args parse(int argc, char **argv) {
             a.global.clear();
             std::stringstream ss(next("--global"));
             std::string item;
-            while (std::getline(ss, item, ','))
-                if (!item.empty()) a.global.push_back(item);
+            while (std::getline(ss, item, ',')) {
+                if (item == "default")  // Output::outputGlobalData, output.cu:562-582
+                    a.global.insert(a.global.end(), {"total_force", "wedge_disp", "von_mises_stress", "mean_pressure"});
+                else if (item == "edge")  // outputEdge writes both files, output.cu:339-369
+                    a.global.insert(a.global.end(), {"frontier", "height"});
+                else if (!item.empty())
+                    a.global.push_back(item);
+            }
         } else if (s == "--probe") {
             float x, y;
             if (std::sscanf(next("--probe"), "%f,%f", &x, &y) != 2) die("--probe wants X,Y", 2);
@@ -118,8 +127,9 @@ Args parse(int argc, char **argv) {
     }
     if (a.case_dir.empty()) die(std::string("no case directory\n") + kUsage, 2);
     if (a.out_dir.empty()) a.out_dir = (fs::path(a.case_dir) / "out").string();
-    static const char *known[] = {"total_force", "von_mises_stress", "mean_pressure", "frontier", "total_energy",
-                                  "tip_disp"};
+    static const char *known[] = {"total_force",     "wedge_disp",    "von_mises_stress", "mean_pressure",
+                                  "frontier",        "height",        "total_energy",     "end_position",
+                                  "middle_position", "tank_beam_end", "crush_force",      "tip_disp"};
     for (const auto &g : a.global) {
         bool ok = false;
         for (const char *k : known) ok = ok || g == k;
@@ -289,12 +299,106 @@ std::string fmt(std::initializer_list<double> v, bool as_float) {
     return s.str();
 }
 
-// Output::outputGlobalData and Probe::outputData for the current state.
-void write_global(sphnj_ctx *ctx, const Args &a, const sphnj_params &p, const fs::path &gdir) {
+// The writers of output.cu that follow one particle of a hard-coded case
+// geometry (the wedge, a beam's end or middle, the tank beam's end) or sum
+// over a band of particles read the state on the host, as the reference
+// does: the solid positions and coupling forces, or the fluid positions, are
+// copied for them.
+bool host_writer(const std::string &name) {
+    return name == "wedge_disp" || name == "middle_position" || name == "end_position" ||
+           name == "tank_beam_end" || name == "crush_force" || name == "height";
+}
+
+// Index of the solid particle whose reference position lies within half a
+// particle spacing of (x, y): the first one (the loops that `break`) or the
+// last one (outputWedgeDisp has no break); -1 if none.
+long solid_at(const HostState &h, size_t ns, double x, double y, float dx, bool last) {
+    long found = -1;
+    for (size_t i = 0; i < ns; ++i) {
+        const double ex = h.sref[2 * i] - x, ey = h.sref[2 * i + 1] - y;
+        if (std::sqrt(ex * ex + ey * ey) < 0.5 * dx) {
+            found = (long)i;
+            if (!last) break;
+        }
+    }
+    return found;
+}
+
+// A position that the reference leaves uninitialised when no particle
+// matches is written as "nan nan" here.
+std::string pair_at(long i, double x, double y) { return i < 0 ? std::string("nan nan") : fmt({x, y}, false); }
+
+void write_host_global(sphnj_ctx *ctx, const std::string &name, const sphnj_params &p, const fs::path &gdir,
+                       HostState &h, uint32_t &have) {
+    const bool fluid = name == "height";
+    const uint32_t mask = fluid ? (SPHNJ_F_FLUID_KINEMATICS | SPHNJ_F_FLUID_THERMO)
+                                : (SPHNJ_F_SOLID_KINEMATICS | SPHNJ_F_SOLID_DERIVED);
+    if ((have & mask) != mask && (fluid ? p.fluid_number_total : p.solid_number) > 0) {
+        if (sphnj_download(ctx, mask, &h.s)) die(sphnj_last_error(ctx), 3);
+        have |= mask;
+    }
+    const size_t ns = p.solid_number, nf = p.fluid_number_total;
+    const float dx = p.particle_diameter;
+    int step = 0;
+    sphnj_get_step(ctx, &step);
+    if (name == "wedge_disp") {  // outputWedgeDisp, output.cu:307-337
+        // SimTime's current_time - dt at this output (output before step + 1)
+        const float t = (float)(step + 1) * p.dt - p.dt;
+        const double middle = 1.5, half_L = 0.6, shift = 2.02;
+        const double left_mid_x = middle - 0.5 * half_L;
+        const double tan_10 = std::tan(10.0 * 3.141593f / 180.0);  // PI of global.h:4
+        const double left_mid_y = -tan_10 * (left_mid_x - middle) + shift;
+        const long k = solid_at(h, ns, left_mid_x - 0.5 * dx, left_mid_y + 0.5 * dx, dx, true);
+        const double down = -30.0 * t;
+        append(gdir, name, k < 0 ? std::string("nan nan")
+                                 : fmt({h.spos[2 * k] - h.sref[2 * k], h.spos[2 * k + 1] - h.sref[2 * k + 1] - down},
+                                       false));
+    } else if (name == "middle_position") {  // outputMiddlePosition, output.cu:371-397
+        const float thick = 0.05f;
+        const long k = solid_at(h, ns, 0.5 * ((double)p.domain_xmax[0] + p.domain_xmin[0]) - 0.5 * dx,
+                                -thick + 0.5 * dx, dx, false);
+        append(gdir, name, pair_at(k, k < 0 ? 0.0 : h.spos[2 * k] + 0.5 * dx,
+                                   k < 0 ? 0.0 : h.spos[2 * k + 1] + (thick - 0.5 * dx)));
+    } else if (name == "end_position") {  // outputEndPosition, output.cu:399-424
+        const long k = solid_at(h, ns, (double)p.domain_xmax[0] - 0.5 * dx,
+                                0.5 * ((double)p.domain_xmin[1] + p.domain_xmax[1]) - 0.5 * dx, dx, false);
+        append(gdir, name, pair_at(k, k < 0 ? 0.0 : h.spos[2 * k] + 0.5 * dx, k < 0 ? 0.0 : h.spos[2 * k + 1] + 0.5 * dx));
+    } else if (name == "tank_beam_end") {  // outputTankBeamEnd, output.cu:457-478
+        const double thick = 0.005, px = -0.5 * thick + 0.5 * dx, py = 0.5 * dx;
+        const long k = solid_at(h, ns, px, py, dx, false);
+        append(gdir, name, pair_at(k, k < 0 ? 0.0 : h.spos[2 * k] - px, k < 0 ? 0.0 : h.spos[2 * k + 1] - py));
+    } else if (name == "crush_force") {  // outputCrushForce, output.cu:480-502
+        const float rho = p.auxetic_density, dv = p.diameter_square;
+        float force = 0.0f;
+        for (size_t i = 0; i < ns; ++i)
+            if (h.sref[2 * i + 1] < dx && h.sref[2 * i + 1] > 0.0) force += h.scouple[2 * i + 1] * rho * dv;
+        append(gdir, name, fmt({force / 16.2e-3}, false));
+    } else if (name == "height") {  // outputEdge's height.dat, output.cu:354-368
+        float h0 = -0.5f * dx, h1 = -0.5f * dx;
+        const float x0 = 5.366f - 0.825f, x1 = 5.366f - 1.653f;
+        for (size_t i = 0; i < nf; ++i) {
+            if (h.fphase[i] != SPHNJ_LIQUID) continue;
+            const float x = h.fpos[2 * i], y = h.fpos[2 * i + 1];
+            if (y > h0 && x < x0 + 0.5f * dx && x > x0 - 0.5f * dx) h0 = y;
+            if (y > h1 && x < x1 + 0.5f * dx && x > x1 - 0.5f * dx) h1 = y;
+        }
+        append(gdir, name, fmt({h0 + dx * 0.5f, h1 + dx * 0.5f}, true));
+    }
+}
+
+// Output::outputGlobalData and Probe::outputData for the current state, in
+// the order the writers are named.
+void write_global(sphnj_ctx *ctx, const Args &a, const sphnj_params &p, const fs::path &gdir, HostState &h) {
     sphnj_diag g{};
     int rc = sphnj_diagnostics(ctx, &g);
     if (rc) die(std::string("diagnostics: ") + sphnj_last_error(ctx), 3);
+    uint32_t have = 0;  // fields copied to h for this output
     for (const auto &name : a.global) {
+        if (host_writer(name)) {
+            write_host_global(ctx, name, p, gdir, h, have);
+            continue;
+        }
+
         if (name == "total_force") append(gdir, name, fmt({g.total_force[0], g.total_force[1]}, true));
         else if (name == "von_mises_stress")
             append(gdir, name, fmt({g.von_mises[0], g.von_mises[1], std::max(g.von_mises[0], g.von_mises[1])}, false));
@@ -382,6 +486,7 @@ int main(int argc, char **argv) {
 
     const long ri = p.result_interval > 0 ? p.result_interval : 1;
     HostState bufs[2] = {HostState(p), HostState(p)};
+    HostState gbuf(p);  // host copy for the writers that read particles
     int cur = 0;
     Writer writer;
     const uint32_t vtk_mask = SPHNJ_F_FLUID_KINEMATICS | SPHNJ_F_FLUID_THERMO | SPHNJ_F_FLUID_FLAGS |
@@ -408,7 +513,7 @@ int main(int argc, char **argv) {
                 std::cout << "Outputing Data...\n--step=" << next - 1 << " file_step=" << next / ri << "--" << std::endl;
             output_vtk(next / ri);
         }
-        if (a.global_every > 0 && (next - 1) % a.global_every == 0) write_global(ctx, a, p, gdir);
+        if (a.global_every > 0 && (next - 1) % a.global_every == 0) write_global(ctx, a, p, gdir, gbuf);
         // run to the next event in one call
         long run = p.iend - i;
         auto until = [&](long every) {

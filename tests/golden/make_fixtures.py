@@ -41,6 +41,20 @@ FIXTURES = {
 }
 
 
+# output fixtures: the reference's own Output functions run by the harness's
+# `run` mode (DeviceCalculation::calculation with outputs); every file it
+# writes under ..\\..\\out is stored as text under its path below out/.
+# name -> (generator, kwargs, global writers)
+OUTPUT_FIXTURES = {
+    "out_water": ("dam_break_water", dict(dx=0.02, iend=100, extra_ini=dict(result_interval=50)),
+                  "default,edge,total_energy"),
+    # domain_xmax = beam length: outputEndPosition's point (xmax - d/2,
+    # (ymin + ymax)/2 - d/2) is then the beam's end particle
+    "out_beam": ("beam", dict(dx=0.002, cfl=0.25, iend=100, extra_ini=dict(result_interval=50, domain_xmax=0.2)),
+                 "default,total_energy,end_position,crush_force"),
+}
+
+
 def make_case(name: str):
     gen, kw, *_ = FIXTURES[name]
     return cases.by_name(gen, **kw)
@@ -90,9 +104,31 @@ def run_case(name: str, out_dir: Path, work: Path) -> Path:
     return out
 
 
+def run_outputs(name: str, out_dir: Path, work: Path) -> Path:
+    sys.path.insert(0, str(ROOT / "oracle" / "ref"))
+    import build_ref  # noqa: E402
+
+    gen, kw, globals_ = OUTPUT_FIXTURES[name]
+    case = cases.by_name(gen, **kw)
+    cdir = case.write(work / name)
+    run_dir = work / f"{name}_run"
+    r = build_ref.run(cdir, ["run", globals_], run_dir=run_dir)
+    if r.returncode:
+        raise RuntimeError(f"{name}: reference harness failed ({r.returncode})\n{r.stdout[-2000:]}\n{r.stderr[-2000:]}")
+    prefix = "..\\..\\out\\"
+    arrays = {"ini": np.array(case.ini_text()), "generator": np.array(json.dumps([gen, kw])),
+              "globals": np.array(globals_)}
+    for f in sorted(run_dir.iterdir()):
+        if f.is_file() and f.name.startswith(prefix):
+            arrays["out/" + f.name[len(prefix):].replace("\\", "/")] = np.array(f.read_text())
+    out = out_dir / f"{name}.npz"
+    np.savez_compressed(out, **arrays)
+    return out
+
+
 def main(argv):
     out_dir = Path(argv[1]) if len(argv) > 1 else Path(__file__).resolve().parent
-    names = argv[2:] or list(FIXTURES)
+    names = argv[2:] or list(FIXTURES) + list(OUTPUT_FIXTURES)
     out_dir.mkdir(parents=True, exist_ok=True)
     sys.path.insert(0, str(ROOT / "oracle" / "ref"))
     import build_ref  # noqa: E402
@@ -100,7 +136,7 @@ def main(argv):
     build_ref.build()
     with tempfile.TemporaryDirectory() as t:
         for n in names:
-            p = run_case(n, out_dir, Path(t))
+            p = (run_outputs if n in OUTPUT_FIXTURES else run_case)(n, out_dir, Path(t))
             print(n, p, p.stat().st_size, flush=True)
 
 

@@ -29,16 +29,18 @@ MIXED = {
 }
 
 
-def _states(loaded, steps, batched, tiled=True, graphs=True):
+def _states(loaded, steps, batched, tiled=True, graphs=True, chaining=True):
     sims = [S.Simulation(p) for p, _ in loaded]
     for sim, (_, arr) in zip(sims, loaded):
         sim.set_tiling(tiled)
         sim.set_graphs(graphs)
+        sim.set_launch_chaining(chaining)
         sim.upload(arr)
     if batched:
         with S.Batch(sims) as b:
             b.set_tiling(tiled)
             b.set_graphs(graphs)
+            b.set_launch_chaining(chaining)
             for chunk in steps:
                 b.step(chunk)
             b.synchronize()
@@ -79,6 +81,56 @@ def test_batch_equals_scenes_stepped_alone(graphs):
     assert 0 < launches < launches_alone / 3
 
 
+def test_batch_launch_chaining_changes_nothing():
+    """The batch's kernels chained by programmatic dependent launch give the
+    same states, bit for bit, as plain launches."""
+    names = list(MIXED)
+    loaded = [load(MIXED[n]()) for n in names]
+    steps = (1, 2, 7, 50, 3)
+    plain, _, _ = _states(loaded, steps, batched=True, chaining=False)
+    chained, _, _ = _states(loaded, steps, batched=True, chaining=True)
+    _assert_same(plain, chained, names)
+
+
+def test_scenes_with_their_own_tile_heights_equal_scenes_alone():
+    """A batch whose scenes sweep tiles of different heights (8, 12, 24 and
+    32 cells, lists off for one) and non-default block sizes gives every
+    scene the state it has stepped alone with the default shape."""
+    names = list(MIXED)
+    loaded = [load(MIXED[n]()) for n in names]
+    steps = (1, 2, 7, 50, 3)
+    alone, _, _ = _states(loaded, steps, batched=False)
+    sims = [S.Simulation(p) for p, _ in loaded]
+    for sim, (_, arr) in zip(sims, loaded):
+        sim.upload(arr)
+    shapes = [(8, True), (12, True), (24, False), (32, True), (16, True), (8, False), (24, True)]
+    with S.Batch(sims) as b:
+        for k, (h, lists) in enumerate(shapes[:len(sims)]):
+            b.set_scene_tiling(k, h, lists)
+        b.set_block_sizes(64, 256)
+        for chunk in steps:
+            b.step(chunk)
+        b.synchronize()
+        assert b.scene_tiling(2) == (24, False)
+    got = [sim.download(abi.F_ALL | abi.F_CELL_IDS) for sim in sims]
+    for sim in sims:
+        sim.close()
+    _assert_same(alone, got, names)
+
+
+@pytest.mark.parametrize("shift_threads,pair_threads", [(64, 128), (256, 256), (128, 0)])
+def test_block_sizes_change_nothing(shift_threads, pair_threads):
+    p, arr = load(MIXED["gas"]())
+    with S.Simulation(p) as a, S.Simulation(p) as b:
+        b.set_block_sizes(shift_threads, pair_threads)
+        for s in (a, b):
+            s.upload(arr)
+            s.step(60)
+        sa, sb = a.download(), b.download()
+    for k in sa:
+        assert np.array_equal(sa[k], sb[k], equal_nan=True), k
+
+
 def test_batch_untiled_equals_tiled():
     names = ["gas", "sweep_dam", "gate"]
     loaded = [load(MIXED[n]()) for n in names]
@@ -108,12 +160,17 @@ def test_batch_rejects_scenes_out_of_step():
     sims[1].synchronize()
     with S.Batch(sims) as b:
         b.step(2)
-        # one scene stepped on its own leaves the batch out of step
-        sims[0].step(1)
+        # a scene of a batch is stepped, restored and given a stream only
+        # through the batch: on its own it would leave the others behind
         with pytest.raises(S.SphnjError):
-            b.step(1)
+            sims[0].step(1)
+        with pytest.raises(S.SphnjError):
+            sims[0].restore(sims[0].checkpoint())
         with pytest.raises(S.SphnjError):
             sims[0].set_stream(None)
+        b.step(1)
+        b.synchronize()
+        assert sims[0].step_index == sims[1].step_index == 4
     for sim in sims:
         sim.close()
 

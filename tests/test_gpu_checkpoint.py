@@ -100,8 +100,10 @@ def test_autotune_leaves_the_run_unchanged(form):
         a.step(5)
         b.step(5)
         t = a.autotune(steps=3)
-        assert t["candidates"] == 9 and t["ms_per_step"] > 0
+        # tile heights and lists, then 3 shifting-pass and 2 pair-pass block sizes
+        assert t["candidates"] == (14 if t["tiled"] else 9) and t["ms_per_step"] > 0
         assert a.sweeps() == {"tiled": t["tiled"], "tile_h": t["tile_h"], "lists": t["lists"]}
+        assert a.block_sizes() == (t["shift_block"], t["pair_block"]) and t["size_classes"] == 1
         assert a.step_index == b.step_index == 5
         if form == abi.FORM_PLAIN:
             # the plain form's sums do not depend on the launch shape
@@ -113,6 +115,7 @@ def test_autotune_leaves_the_run_unchanged(form):
             # the run continues from exactly the tuned-from state
             b.set_tiling(t["tiled"], t["tile_h"])
             b.set_neighbour_lists(t["lists"])
+            b.set_block_sizes(t["shift_block"], t["pair_block"])
             a.step(10)
             b.step(10)
             same(b.download(), a.download())
@@ -132,8 +135,12 @@ def test_batch_autotune():
     with S.Batch(sims) as b:
         b.step(2)
         t = b.autotune(steps=3)
-        assert t["candidates"] == 9
-        assert b.sweeps()["tile_h"] == t["tile_h"]
+        # the two dam breaks form two size classes (the beams have no fluid)
+        assert t["size_classes"] == 2 and t["class_split"] == max(p.fluid_number_total for p, _ in loaded)
+        assert t["candidates"] == (9 + 3 + 2 + 2 * 4 if t["tiled"] else 9)
+        small, large = (0, 1) if loaded[0][0].fluid_number_total < loaded[1][0].fluid_number_total else (1, 0)
+        assert b.scene_tiling(small) == (t["class_tile_h"][0], t["class_lists"][0])
+        assert b.scene_tiling(large) == (t["class_tile_h"][1], t["class_lists"][1])
         b.step(10)
         b.synchronize()
     for sim, r in zip(sims, ref):

@@ -43,7 +43,10 @@ RUNS = {
 # relative to the column's scale over the run; the plain form computes in the
 # reference's precision, the mixed form rounds differently (FP32 solid loops,
 # cell + offset positions)
-TOL = {abi.FORM_PLAIN: {"fluid": 1e-3, "solid": 1e-4}, abi.FORM_MIXED: {"fluid": 2e-3, "solid": 2e-3}}
+# (measured: plain at most 2.5e-5 - the gate's strain energy - and 1.4e-5 for
+# the water's momentum over 2,000 steps; mixed at most 1.8e-4 - the gate's
+# solid kinetic energy - and 1.0e-4 for the water's momentum)
+TOL = {abi.FORM_PLAIN: {"fluid": 2e-4, "solid": 2e-4}, abi.FORM_MIXED: {"fluid": 1e-3, "solid": 1e-3}}
 
 
 def test_late_step_against_reference():
