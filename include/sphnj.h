@@ -47,8 +47,14 @@ extern "C" {
 #define SPHNJ_ERR_OUT_OF_GRID   7   /* a particle's cell id is outside the
                                        cell grid (the reference reads out of
                                        bounds there)                         */
-#define SPHNJ_ERR_NONFINITE     8   /* NaN/Inf found in the state           */
-#define SPHNJ_ERR_WATCHDOG      9   /* a bounded device wait ran out        */
+#define SPHNJ_ERR_NONFINITE     8   /* NaN/Inf in a particle's position,
+                                       velocity or density after an update
+                                       (reported by the next synchronising
+                                       call; the reference steps on)         */
+#define SPHNJ_ERR_WATCHDOG      9   /* reserved for a bounded device wait
+                                       that ran out: no kernel of this
+                                       version waits on another, so none
+                                       returns it                            */
 #define SPHNJ_ERR_UNSUPPORTED  10   /* feature not available in this form   */
 #define SPHNJ_ERR_NO_DEVICE    11   /* no CUDA device / extension missing   */
 

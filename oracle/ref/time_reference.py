@@ -26,6 +26,58 @@ import build_ref  # noqa: E402
 from sphnj_gb300 import cases  # noqa: E402
 
 
+class Clocks:
+    """nvidia-smi SM clock and throttle reasons sampled every 200 ms while
+    the harness runs (the samples under load: SM clock above 1 GHz or power
+    above 300 W)."""
+    Q = ("clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.hw_slowdown,"
+         "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+         "clocks_event_reasons.sw_power_cap")
+
+    def __enter__(self):
+        import subprocess
+        import threading
+
+        self.rows = []
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", "--id=0", f"--query-gpu={self.Q}",
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+        except OSError:
+            self.proc = None
+            return self
+
+        def read():
+            for line in self.proc.stdout:
+                self.rows.append([c.strip() for c in line.split(",")])
+
+        self.t = threading.Thread(target=read, daemon=True)
+        self.t.start()
+        return self
+
+    def __exit__(self, *exc):
+        if self.proc:
+            self.proc.terminate()
+            self.proc.wait(timeout=5)
+
+    def summary(self) -> dict:
+        import statistics
+
+        def num(x):
+            try:
+                return float(x)
+            except ValueError:
+                return None
+
+        rows = [r for r in self.rows if len(r) >= 7 and num(r[0]) is not None]
+        load = [r for r in rows if num(r[0]) > 1000 or (num(r[2]) or 0) > 300]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({names[k] for r in load for k in range(4) if r[3 + k].lower().startswith("active")})
+        return {"samples": len(rows), "samples_under_load": len(load),
+                "sm_mhz_median": statistics.median(num(r[0]) for r in load) if load else None,
+                "sm_max_mhz": max(num(r[1]) for r in rows) if rows else None, "reasons": reasons}
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("case")
@@ -41,14 +93,15 @@ def main():
     build_ref.build()
     with tempfile.TemporaryDirectory() as t:
         cdir = case.write(Path(t) / "case")
-        r = build_ref.run(cdir, ["time", str(a.warmup), str(a.steps)], run_dir=Path(t) / "run")
+        with Clocks() as clk:
+            r = build_ref.run(cdir, ["time", str(a.warmup), str(a.steps)], run_dir=Path(t) / "run")
     if r.returncode:
         print(json.dumps({"case": a.case, "error": r.stderr[-500:]}))
         return 1
     res = json.loads(r.stdout.strip().splitlines()[-1])
     n = res["n_fluid"] + res["n_solid"]
     res.update(case=a.case, args=kw, particle_steps_per_s=n * 1e3 / res["ms_per_step"],
-               impl="reference CUDA build (sm_103a, -use_fast_math, Eigen-subset shim)")
+               impl="reference CUDA build (sm_103a, -use_fast_math, Eigen-subset shim)", clocks=clk.summary())
     print(json.dumps(res))
     return 0
 

@@ -32,6 +32,34 @@ __device__ __forceinline__ float2 cells_to_len(const sphnj_params &p, int kx, in
     return make_float2(__fmul_rn((float)kx, p.interval[0]), __fmul_rn((float)ky, p.interval[1]));
 }
 
+// Packed FP32 pairs (PTX .f32x2 on sm_100 and later): one instruction does
+// the same two round-to-nearest operations as two scalar ones (same
+// results), on the x and y halves of a float2.  The mixed form's pair and
+// shifting loops use them for their vector arithmetic.
+__device__ __forceinline__ float2 sub2x(float2 a, float2 b) {
+    float2 r;
+    asm("{\n\t.reg .b64 a, b, d;\n\tmov.b64 a, {%2, %3};\n\tmov.b64 b, {%4, %5};\n\t"
+        "sub.rn.f32x2 d, a, b;\n\tmov.b64 {%0, %1}, d;\n\t}"
+        : "=f"(r.x), "=f"(r.y) : "f"(a.x), "f"(a.y), "f"(b.x), "f"(b.y));
+    return r;
+}
+__device__ __forceinline__ float2 mul2x(float2 a, float2 b) {
+    float2 r;
+    asm("{\n\t.reg .b64 a, b, d;\n\tmov.b64 a, {%2, %3};\n\tmov.b64 b, {%4, %5};\n\t"
+        "mul.rn.f32x2 d, a, b;\n\tmov.b64 {%0, %1}, d;\n\t}"
+        : "=f"(r.x), "=f"(r.y) : "f"(a.x), "f"(a.y), "f"(b.x), "f"(b.y));
+    return r;
+}
+// a * b + c per half, each one fused multiply-add
+__device__ __forceinline__ float2 fma2x(float2 a, float2 b, float2 c) {
+    float2 r;
+    asm("{\n\t.reg .b64 a, b, c, d;\n\tmov.b64 a, {%2, %3};\n\tmov.b64 b, {%4, %5};\n\t"
+        "mov.b64 c, {%6, %7};\n\tfma.rn.f32x2 d, a, b, c;\n\tmov.b64 {%0, %1}, d;\n\t}"
+        : "=f"(r.x), "=f"(r.y) : "f"(a.x), "f"(a.y), "f"(b.x), "f"(b.y), "f"(c.x), "f"(c.y));
+    return r;
+}
+__device__ __forceinline__ float2 splat2(float a) { return make_float2(a, a); }
+
 // 2^x by the SFU (PTX ex2.approx.ftz.f32, relative error ~2^-22)
 __device__ __forceinline__ float ex2_approx(float x) {
     float y;

@@ -207,6 +207,12 @@ template <class F> __device__ __forceinline__ void mad_to(float &a, float x, flo
     else a += x * y;
 }
 
+// x_j - x_i: two subtractions, packed in the mixed form (same results)
+template <class F> __device__ __forceinline__ float2 sep(float2 xj, float2 xi) {
+    if constexpr (F::kMixed) return sub2x(xj, xi);
+    else return sub2(xj, xi);
+}
+
 // Riemann pair term shared by fluid, solid and virtual neighbours
 // (fluid.cu:48-58, 115-124, 167-177).  The plain form divides as the
 // reference's fast-math build does, one approximate division per '/'.  The
@@ -225,17 +231,26 @@ __device__ __forceinline__ void riemann(float2 u_i, float2 u_j, float p_i, float
         ps = __fmul_rn(sum2(rho_i, p_j, rho_j, p_i), irs);
         const float z = sqn(dx);
         const float iz = rsqrt_approx(z);
-        n = z > 0.0f ? make_float2(__fmul_rn(dx.x, iz), __fmul_rn(dx.y, iz)) : dx;
-        const float du = dot2(sub2(u_i, u_j), n);
+        n = z > 0.0f ? mul2x(dx, splat2(iz)) : dx;
+        const float du = dot2(sub2x(u_i, u_j), n);
         if (du >= 0.0f)
             ps = __fadd_rn(ps, __fmul_rn(__fmul_rn(__fmul_rn(__fmul_rn(rho_i, rho_j), du), irs),
                                          fminf(__fmul_rn(3.0f, du), cs)));
-        vs = make_float2(__fmul_rn(sum2(rho_i, u_i.x, rho_j, u_j.x), irs),
-                         __fmul_rn(sum2(rho_i, u_i.y, rho_j, u_j.y), irs));
+        // (rho_i u_i + rho_j u_j) / (rho_i + rho_j), per component
+        // fma(rho_j, u_j, rho_i u_i) then times 1 / (rho_i + rho_j)
+        vs = mul2x(fma2x(splat2(rho_j), u_j, mul2x(splat2(rho_i), u_i)), splat2(irs));
         t = __fmul_rn(__fmul_rn(__fsub_rn(p_i, p_j), irs), rcp_approx(cs));
-        vs.x = __fmaf_rn(t, n.x, vs.x);
-        vs.y = __fmaf_rn(t, n.y, vs.y);
+        vs = fma2x(splat2(t), n, vs);
         am = __fmul_rn(__fmul_rn(-2.0f, ps), rcp_approx(rho_i));
+        // the sums, each product rounded and then one fused add, as mad_to:
+        // in pairs of components (packed FP32)
+        a.du_dt = fma2x(mul2x(splat2(am), dx), splat2(kc), a.du_dt);
+        a.velo_div = __fmaf_rn(__fmul_rn(__fmul_rn(2.0f, rho_i), dot2(sub2x(u_i, vs), dx)), kc, a.velo_div);
+        const float2 w = sub2x(u_j, u_i);
+        const float2 c0 = fma2x(mul2x(w, splat2(dx.x)), splat2(kc), make_float2(a.du_dx.x, a.du_dx.y));
+        const float2 c1 = fma2x(mul2x(w, splat2(dx.y)), splat2(kc), make_float2(a.du_dx.z, a.du_dx.w));
+        a.du_dx = make_float4(c0.x, c0.y, c1.x, c1.y);
+        return;
     } else {
         ps = fdiv(sum2(rho_i, p_j, rho_j, p_i), rs);
         n = nrm_fast(dx);
@@ -312,8 +327,12 @@ __device__ __forceinline__ void fluid_term(const sphnj_params &p, const Src &src
     const int ph_j = src.phase(k);
     if (!(s.ph == SPHNJ_LIQUID && ph_j == SPHNJ_GAS)) {
         mad_to<F>(a.color, dot2(dx, dx), kc);
-        mad_to<F>(a.grad.x, dx.x, kc);
-        mad_to<F>(a.grad.y, dx.y, kc);
+        if constexpr (F::kMixed) {
+            a.grad = fma2x(dx, splat2(kc), a.grad);
+        } else {
+            mad_to<F>(a.grad.x, dx.x, kc);
+            mad_to<F>(a.grad.y, dx.y, kc);
+        }
     }
     if (src.fbt(k) == SPHNJ_FREE_SURFACE && s.ph == SPHNJ_LIQUID && s.i != src.pid(k)) {
         if (sqn(dx) < 0.25f * R2) a.near = SPHNJ_HAS_NEAR_PARTICLE;
@@ -505,7 +524,7 @@ __device__ __forceinline__ void pair_particle_listed(const sphnj_params &p, cons
     for (int s = 0; s < 3; ++s) {
         const int2 rr = src.range(s, make_int2(S.base[s], S.len[s]));
         for (int t = rr.x; t < rr.x + rr.y; ++t)
-            if (sqn(sub2(src.x(src.key(t)), si.x)) < Rs2) {
+            if (sqn(sep<F>(src.x(src.key(t)), si.x)) < Rs2) {
                 if (n < kNbrCap) {
                     b0 = __funnelshift_r(b0, b1, 16);
                     b1 = __funnelshift_r(b1, b2, 16);
@@ -540,7 +559,7 @@ __device__ __forceinline__ void pair_particle_listed(const sphnj_params &p, cons
         for (int e = 0; e < 8; ++e) {
             if (c + e < n) {
                 const int k = src.key((int)(((w[e >> 1] >> (16 * (e & 1))) & 0xFFFFu) >> 3));
-                const float2 dx = sub2(src.x(k), si.x);
+                const float2 dx = sep<F>(src.x(k), si.x);
                 if (sqn(dx) < R2) fluid_term<F>(p, src, k, si, dx, a);
             }
         }
@@ -571,11 +590,15 @@ __device__ __forceinline__ float2 shift_particle_listed(const sphnj_params &p, c
 #pragma unroll
         for (int e = 0; e < 8; ++e) {
             if (e < m) {
-                const float2 dx = sub2(x_j[e], x_i);
+                const float2 dx = sep<F>(x_j[e], x_i);
                 if (sqn(dx) < R2) {
                     const float kc = F::gw_shift(p, sqn(dx));
-                    mad_to<F>(g.x, dx.x, kc);
-                    mad_to<F>(g.y, dx.y, kc);
+                    if constexpr (F::kMixed) {
+                        g = fma2x(dx, splat2(kc), g);
+                    } else {
+                        mad_to<F>(g.x, dx.x, kc);
+                        mad_to<F>(g.y, dx.y, kc);
+                    }
                 }
             }
         }

@@ -324,9 +324,9 @@ long solid_at(const HostState &h, size_t ns, double x, double y, float dx, bool 
     return found;
 }
 
-// A position that the reference leaves uninitialised when no particle
-// matches is written as "nan nan" here.
-std::string pair_at(long i, double x, double y) { return i < 0 ? std::string("nan nan") : fmt({x, y}, false); }
+// Where no particle sits at the writer's point the reference leaves its
+// position vector uninitialised; its build prints zeros there (the vector
+// as zero, then the writer's offsets added), and so does this driver.
 
 void write_host_global(sphnj_ctx *ctx, const std::string &name, const sphnj_params &p, const fs::path &gdir,
                        HostState &h, uint32_t &have) {
@@ -350,23 +350,24 @@ void write_host_global(sphnj_ctx *ctx, const std::string &name, const sphnj_para
         const double left_mid_y = -tan_10 * (left_mid_x - middle) + shift;
         const long k = solid_at(h, ns, left_mid_x - 0.5 * dx, left_mid_y + 0.5 * dx, dx, true);
         const double down = -30.0 * t;
-        append(gdir, name, k < 0 ? std::string("nan nan")
+        append(gdir, name, k < 0 ? fmt({0.0, 0.0}, false)
                                  : fmt({h.spos[2 * k] - h.sref[2 * k], h.spos[2 * k + 1] - h.sref[2 * k + 1] - down},
                                        false));
     } else if (name == "middle_position") {  // outputMiddlePosition, output.cu:371-397
         const float thick = 0.05f;
         const long k = solid_at(h, ns, 0.5 * ((double)p.domain_xmax[0] + p.domain_xmin[0]) - 0.5 * dx,
                                 -thick + 0.5 * dx, dx, false);
-        append(gdir, name, pair_at(k, k < 0 ? 0.0 : h.spos[2 * k] + 0.5 * dx,
-                                   k < 0 ? 0.0 : h.spos[2 * k + 1] + (thick - 0.5 * dx)));
+        append(gdir, name, fmt({(k < 0 ? 0.0 : h.spos[2 * k]) + 0.5 * dx,
+                                (k < 0 ? 0.0 : h.spos[2 * k + 1]) + (thick - 0.5 * dx)}, false));
     } else if (name == "end_position") {  // outputEndPosition, output.cu:399-424
         const long k = solid_at(h, ns, (double)p.domain_xmax[0] - 0.5 * dx,
                                 0.5 * ((double)p.domain_xmin[1] + p.domain_xmax[1]) - 0.5 * dx, dx, false);
-        append(gdir, name, pair_at(k, k < 0 ? 0.0 : h.spos[2 * k] + 0.5 * dx, k < 0 ? 0.0 : h.spos[2 * k + 1] + 0.5 * dx));
+        append(gdir, name, fmt({(k < 0 ? 0.0 : h.spos[2 * k]) + 0.5 * dx, (k < 0 ? 0.0 : h.spos[2 * k + 1]) + 0.5 * dx},
+                               false));
     } else if (name == "tank_beam_end") {  // outputTankBeamEnd, output.cu:457-478
         const double thick = 0.005, px = -0.5 * thick + 0.5 * dx, py = 0.5 * dx;
         const long k = solid_at(h, ns, px, py, dx, false);
-        append(gdir, name, pair_at(k, k < 0 ? 0.0 : h.spos[2 * k] - px, k < 0 ? 0.0 : h.spos[2 * k + 1] - py));
+        append(gdir, name, k < 0 ? fmt({0.0, 0.0}, false) : fmt({h.spos[2 * k] - px, h.spos[2 * k + 1] - py}, false));
     } else if (name == "crush_force") {  // outputCrushForce, output.cu:480-502
         const float rho = p.auxetic_density, dv = p.diameter_square;
         float force = 0.0f;

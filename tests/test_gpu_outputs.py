@@ -10,9 +10,9 @@ the VTK's "0.0" z column and "nan" byte-identical), and numbers within a
 tolerance relative to their column's largest magnitude in the file: the
 first output (the state read from the .dat files) within float formatting,
 later ones after free runs of 50 and 100 steps in the two implementations.
-The wedge's displacement is compared in layout only: the reference prints an
-uninitialised vector when no particle sits at the wedge's hard-coded point
-(output.cu:307-337), which sphnj_run writes as "nan nan".
+Where no particle sits at a writer's hard-coded point (the wedge of
+output.cu:307-337 in these cases) the reference prints an uninitialised
+vector, which its build writes as zeros; sphnj_run writes the same.
 """
 from __future__ import annotations
 
@@ -30,7 +30,7 @@ from helpers import golden
 pytestmark = pytest.mark.gpu
 
 TOL = 2e-3
-LAYOUT_ONLY = {"global/wedge_disp.dat"}
+LAYOUT_ONLY = set()
 
 
 def number(t):

@@ -298,9 +298,8 @@ def test_nonfinite_fluid_state_is_reported(form):
     """A NaN velocity injected on the host into an uploaded state: the
     reference steps on silently; here the fluid update flags it and the next
     synchronising call returns SPHNJ_ERR_NONFINITE (no device fault)."""
-    case = cases.dam_break_water(dx=0.05)
-    case.fluid_velocity[11] = [np.nan, 0.0]
-    p, arr = load(case)
+    p, arr = load(cases.dam_break_water(dx=0.05))
+    arr["fluid_velocity"][11] = [np.nan, 0.0]  # into the uploaded host state
     with S.Simulation(p, form) as g:
         g.upload(arr)
         g.step(1)
@@ -311,9 +310,9 @@ def test_nonfinite_fluid_state_is_reported(form):
 
 @pytest.mark.parametrize("form", [abi.FORM_PLAIN, abi.FORM_MIXED])
 def test_nonfinite_solid_state_is_reported(form):
-    case = cases.beam(dx=0.004)
-    case.solid_velocity[-1] = [0.0, np.inf]  # the tip (the clamp's particles move at the fixed speed)
-    p, arr = load(case)
+    p, arr = load(cases.beam(dx=0.004))
+    # the tip, in the uploaded host state (the clamp's particles move at the fixed speed)
+    arr["solid_velocity"][-1] = [0.0, np.inf]
     with S.Simulation(p, form) as g:
         g.upload(arr)
         g.step(1)
