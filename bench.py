@@ -476,10 +476,18 @@ def run_ours(args):
         barrier()
         torch.cuda.synchronize()
         t0 = time.perf_counter()
+        part = [0.0, 0.0, 0.0]  # upload (returns when copied), step (enqueue), download (waits for the step)
         for _ in range(ke):
+            ta = time.perf_counter()
             sim.upload_fields(mask, hin)
+            tb = time.perf_counter()
             sim.step(1)
+            tc = time.perf_counter()
             sim.download(mask, into=hout)
+            td = time.perf_counter()
+            part[0] += tb - ta
+            part[1] += tc - tb
+            part[2] += td - tc
             hin, hout = hout, hin
         torch.cuda.synchronize()
         dt = time.perf_counter() - t0
@@ -488,7 +496,9 @@ def run_ours(args):
             torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
             dt = float(t.item())
         e2e = {"value": units * world * ke / dt, "unit": UNIT, "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
-               "steps": ke, "api": "sphnj_upload_fields + sphnj_step(1) + sphnj_download per step"}
+               "steps": ke, "api": "sphnj_upload_fields + sphnj_step(1) + sphnj_download per step",
+               "ms_per_step_parts": {"upload": part[0] * 1e3 / ke, "step_enqueue": part[1] * 1e3 / ke,
+                                     "step_and_download": part[2] * 1e3 / ke}}
 
     normals = sim.download(abi.F_VIRT)["virt_normal"].copy()
     sim.close()
@@ -590,8 +600,24 @@ def run_ours(args):
     return 0
 
 
+def relaunch_distributed(args) -> int:
+    """bench.py --gpus N (N > 1) started without torchrun: runs itself as N
+    processes under torch.distributed.run (one per GPU, rendezvous on
+    127.0.0.1), as the multi-GPU launch does."""
+    import socket
+
+    with socket.socket() as s:
+        s.bind(("127.0.0.1", 0))
+        port = s.getsockname()[1]
+    cmd = [sys.executable, "-m", "torch.distributed.run", "--nnodes=1", f"--nproc-per-node={args.gpus}",
+           "--master-addr", "127.0.0.1", f"--master-port={port}", str(ROOT / "bench.py"), *sys.argv[1:]]
+    return subprocess.call(cmd)
+
+
 def main():
     args = parse()
+    if args.gpus > 1 and "WORLD_SIZE" not in os.environ:
+        return relaunch_distributed(args)
     if args.impl == "reference":
         return run_reference(args)
     return run_ours(args)
