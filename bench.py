@@ -240,7 +240,7 @@ def run_reference(args):
     return 0
 
 
-def run_sweep(args, stream):
+def run_sweep(args, stream, peak):
     """The 256-scene sweep (sphnj_gb300.cases.sweep_scene, seeds 0..255: 128
     water dam breaks of 2k-60k particles, 128 beams of 1k-20k): the plain
     form run scene by scene (each scene's steps as its own graph launches, the
@@ -250,7 +250,7 @@ def run_sweep(args, stream):
     import torch
 
     import sphnj_gb300 as S
-    from sphnj_gb300 import abi, cases
+    from sphnj_gb300 import abi, byte_model, cases
 
     from sphnj_gb300.sharding import balanced_partition
 
@@ -332,7 +332,15 @@ def run_sweep(args, stream):
         for sim in sims:
             sim.close()
         total = sum(v[0] for v in prof.values())
+        mixed = form == abi.FORM_MIXED
+        sweep_bytes = sum(byte_model.step_bytes(q.fluid_number_total, q.solid_number, q.virt_number,
+                                                q.shift_per_step, q.solid_sub_step, mixed) for q in params)
+        achieved = sweep_bytes / (ms / K / 1e3) / 1e9
         out[name] = dict(rate(ms), launches_per_step=launches / K, autotuned=tuned,
+                         roofline={"bound": "hbm", "what": "whole batched step: compulsory bytes of every scene's "
+                                                           "passes (byte model) / step time",
+                                   "bytes_per_step": sweep_bytes, "achieved": achieved, "peak": peak,
+                                   "unit": "GB/s", "frac": achieved / peak},
                          stage_share={k: round(v[0] / total, 4) for k, v in prof.items() if v[1]})
         out[name + "_over_plain"] = ms_plain / ms
     return {
@@ -455,6 +463,9 @@ def run_ours(args):
                 "traffic_source": "ncu dram bytes of one launch at 2.08M particles, scaled by particle count",
                 "peak_source": "MEASURED_PEAKS.json hbm_gbs (measured)" if peaks else "fallback 6.8 TB/s",
                 "bytes_per_launch": bpl, "avg_launch_ms": avg_ms,
+                "issue_slots_busy": (dict(byte_model.ISSUE_ACTIVE_MIXED,
+                                          source="ncu smsp__issue_active of one launch at 2.08M particles")
+                                     if mixed else None),
                 "stage_share": {k: round(v[0] / total_ms, 4) for k, v in prof.items() if v[1]}}
     step_bytes = byte_model.bytes_per_step(nf, ns, nv, p.shift_per_step, p.solid_sub_step)
 
@@ -541,7 +552,7 @@ def run_ours(args):
 
     sweep = None
     if not args.no_sweep:
-        sweep = run_sweep(args, stream)
+        sweep = run_sweep(args, stream, peak)
 
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu_baseline:

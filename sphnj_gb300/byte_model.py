@@ -76,6 +76,24 @@ def bytes_per_step(nf: int, ns: int, nv: int, shifts: int, substeps: int) -> flo
     return float(nf * (153 + 63 * shifts + 16 * (shifts & 1)) + nv * 46 + ns * (48 + 440 * substeps))
 
 
+def step_bytes(nf: int, ns: int, nv: int, shifts: int, substeps: int, mixed: bool = False) -> float:
+    """Compulsory bytes of one step of one scene in either form, from the
+    per-pass table of that form: every particle binned, the fluid's list
+    rebuild (the sort amortised), pair pass, update and shifting passes, the
+    virtual particles' data, and for solids the coupling pass (with fluid) and
+    k sub-steps of deformation, force and update."""
+    t = PER_PARTICLE_MIXED if mixed else PER_PARTICLE
+    b = (nf + ns + nv) * t["bin"]
+    if nf:
+        b += nf * (t["rebuild"] + t["sort"] / 50 + t["fluid_pair"] + t["fluid_update"] + shifts * t["shift_pass"]
+                   + (shifts & 1) * t["shift_copy_back"])
+    b += nv * t["virt_data"]
+    if ns:
+        b += ns * ((t["solid_couple"] if nf else 0) + substeps * (t["solid_deformation"] + t["solid_force"]
+                                                                   + t["solid_update"]))
+    return float(b)
+
+
 # DRAM traffic (dram__bytes_read.sum + dram__bytes_write.sum) per fluid
 # particle of one launch of the tiled neighbour sweeps, from one ncu capture of
 # the 2,083,750-particle gas-liquid dam break (plain form, tiles of 16 cells,
@@ -87,11 +105,14 @@ MEASURED_TRAFFIC_PER_PARTICLE = {
     "fluid_pair": 149.0,
     "shift_pass": 157.4,
 }
-# the same capture of the mixed form
+# the mixed form (the capture of the current build, packed FP32 pair arithmetic)
 MEASURED_TRAFFIC_PER_PARTICLE_MIXED = {
-    "fluid_pair": 149.4,
-    "shift_pass": 187.3,
+    "fluid_pair": 148.1,
+    "shift_pass": 186.2,
 }
+# issue slots busy (smsp__issue_active, % of peak) of the same captures: the
+# neighbour sweeps are bound by instruction issue and latency, not by DRAM
+ISSUE_ACTIVE_MIXED = {"fluid_pair": 0.660, "shift_pass": 0.541}
 
 
 def measured_traffic_per_launch(stage: str, nf: int, mixed: bool = False) -> float | None:

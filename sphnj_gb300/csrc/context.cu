@@ -163,6 +163,9 @@ size_t layout(sphnj_ctx *ctx, char *base) {
     d.f_phase = a.take<uint8_t>(nf); d.f_fbt = a.take<uint8_t>(nf); d.f_near = a.take<uint8_t>(nf);
     d.f_cell = a.take<int>(nf);
     d.f_x_alt = a.take<float2>(nf);
+    d.f_xl = a.take<float2>(nf);
+    d.f_xl_alt = a.take<float2>(nf);
+    d.f_celll = a.take<int>(nf);
     d.f_listed = a.take<int>(nf);
     ctx->f_listed_total = a.take<int>(1);
     d.f_listed_total = ctx->f_listed_total;

@@ -43,6 +43,16 @@ struct DevState {
     // positions (f_pos, or f_off in the mixed form) and writes the shifted
     // ones here; the launches of odd passes exchange the two pointers
     float2 *f_x_alt;
+    // The shifting passes in list order: before the first pass the positions
+    // (f_pos, or f_off) and cell ids of the listed fluid particles are
+    // gathered by their position h in the fluid CSR list into f_xl and
+    // f_celll; every pass reads and writes them there (f_xl, f_xl_alt,
+    // exchanged like f_pos / f_x_alt), so that staging a tile's neighbours
+    // reads contiguous ranges and a home particle's position and cell need
+    // no gather through the list; after the last pass they are scattered
+    // back.  Particles in no list stay in the particle arrays.
+    float2 *f_xl, *f_xl_alt;
+    int *f_celll;
     // solid
     double2 *s_pos, *s_ref, *s_vel, *s_dudt;
     dmat2 *s_F, *s_P, *s_L, *s_maxstrain;
@@ -262,7 +272,7 @@ struct Scene {
     // sweep shape of this scene: cells per tile of the tiled neighbour sweeps
     // and whether its pair pass stores neighbour lists (the scenes of a batch
     // may have different shapes, chosen by size)
-    int tile_h, lists, pad_[2];
+    int tile_h, lists, pad_[4];
 };
 
 // Where a block finds its scene.  Every kernel of the step is a template over

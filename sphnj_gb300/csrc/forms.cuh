@@ -99,6 +99,11 @@ struct FormPlain {
         return d.f_pos[i];
     }
     __device__ static __forceinline__ float2 f_nbr(const DevState &d, int j, float2) { return __ldg(&d.f_pos[j]); }
+    // the shifting passes' list-order positions, by CSR position h
+    __device__ static __forceinline__ float2 f_home_l(const sphnj_params &, const DevState &d, Frame, int h) {
+        return d.f_xl[h];
+    }
+    __device__ static __forceinline__ float2 f_nbr_l(const DevState &d, int t, float2) { return __ldg(&d.f_xl[t]); }
     __device__ static __forceinline__ float2 s_home(const sphnj_params &, const DevState &d, Frame, int i) {
         return to_f2(d.s_pos[i]);
     }
@@ -133,6 +138,12 @@ struct FormMixed {
     }
     __device__ static __forceinline__ float2 f_nbr(const DevState &d, int j, float2 sh) {
         return add2_rn(__ldg(&d.f_off[j]), sh);
+    }
+    __device__ static __forceinline__ float2 f_home_l(const sphnj_params &p, const DevState &d, Frame f, int h) {
+        return add2_rn(d.f_xl[h], corner(p, f));
+    }
+    __device__ static __forceinline__ float2 f_nbr_l(const DevState &d, int t, float2 sh) {
+        return add2_rn(__ldg(&d.f_xl[t]), sh);
     }
     __device__ static __forceinline__ float2 s_home(const sphnj_params &p, const DevState &d, Frame f, int i) {
         return add2_rn(d.s_off[i], corner(p, f));

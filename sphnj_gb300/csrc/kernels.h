@@ -42,7 +42,8 @@ enum Site : int {
     SITE_REBUILD_CELLS, SITE_REBUILD_TILES, SITE_REBUILD_ONE, SITE_CAPACITY, SITE_COUPLE, SITE_VIRT_NORMAL,
     SITE_VIRT_DATA, SITE_PAIR_TILED, SITE_PAIR_EACH, SITE_PAIR_FALLBACK, SITE_FLUID_UPDATE, SITE_SOLID_DEFORM,
     SITE_SOLID_FORCE, SITE_SOLID_UPDATE, SITE_SHIFT_TILED, SITE_SHIFT_EACH, SITE_SHIFT_FALLBACK,
-    SITE_SHIFT_COPY_BACK, SITE_TILE_COMPACT, SITE_TILE_SUMS, SITE_TILE_SCATTER, SITE_VIRT_BIN
+    SITE_SHIFT_COPY_BACK, SITE_TILE_COMPACT, SITE_TILE_SUMS, SITE_TILE_SCATTER, SITE_VIRT_BIN, SITE_SHIFT_GATHER,
+    SITE_SHIFT_SCATTER
 };
 inline long long site_key(int site, int arg = 0) { return ((long long)site << 32) | (unsigned)arg; }
 
@@ -53,6 +54,9 @@ inline void exchange_positions(Scene &s, int form) {
     float2 *t = x;
     x = s.d.f_x_alt;
     s.d.f_x_alt = t;
+    t = s.d.f_xl;  // the list-order pair of the shifting passes
+    s.d.f_xl = s.d.f_xl_alt;
+    s.d.f_xl_alt = t;
 }
 
 // exchange_positions() switches the group's records between the two buffer
@@ -225,9 +229,10 @@ cudaError_t configure_sweeps(const TileConfig &tc);
 template <class G> int launch_fluid_pair(cudaStream_t st, G &g, const TileConfig &tc);
 template <class G> int launch_fluid_update(cudaStream_t st, G &g);
 // Shifting pass `pass` of the step (gradient and position update in one
-// sweep; scenes with fewer shifting passes per step own no block of it), and,
-// after the last pass, the copy of the positions back to f_pos / f_off in the
-// scenes whose number of passes is odd.
+// sweep; scenes with fewer shifting passes per step own no block of it; pass
+// 0 first gathers the listed particles' positions into list order), and,
+// after the last pass, the positions back to f_pos / f_off: from f_x_alt in
+// the scenes whose number of passes is odd, then from list order.
 template <class G> int launch_shift_pass(cudaStream_t st, G &g, const TileConfig &tc, int pass);
 template <class G> int launch_shift_copy_back(cudaStream_t st, G &g);
 

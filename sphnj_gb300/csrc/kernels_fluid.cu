@@ -151,6 +151,16 @@ template <class F> struct SrcGlobal {
     __device__ __forceinline__ int pid(int k) const { return k; }
 };
 
+// The shifting passes' fluid neighbours read by CSR position from the
+// list-order positions (f_xl, in the frame of the cell they are listed in).
+template <class F> struct SrcListOrder {
+    const DevState *d;
+    __device__ __forceinline__ int2 range(int, int2 r) const { return r; }
+    __device__ __forceinline__ int key(int t) const { return t; }
+    __device__ __forceinline__ float2 x(int t, float2 sh = float2()) const { return F::f_nbr_l(*d, t, sh); }
+    __device__ __forceinline__ float2 x_byte(unsigned off) const { return x((int)(off >> 3)); }
+};
+
 struct SrcTile {
     const float2 *pos, *vel, *rp;  // rp = {rho, p}
     const uint8_t *flags;          // phase | boundary type << 1
@@ -411,13 +421,12 @@ __device__ __forceinline__ void pair_particle(const sphnj_params &p, const DevSt
 }
 
 // correctionCalculate for particle i (fluid.cu:316-367): its shifting gradient
+// at x_i (in frame fr) in cell c
 template <class F, class Src>
-__device__ __forceinline__ float2 shift_particle(const sphnj_params &p, const DevState &d, const Src &src, int i,
-                                                 Frame fr) {
+__device__ __forceinline__ float2 shift_particle(const sphnj_params &p, const DevState &d, const Src &src, float2 x_i,
+                                                 int c, Frame fr) {
     const int nx = p.cell_number[0], ny = p.cell_number[1];
     const float R2 = p.impact_distance_square, hinv2 = p.smoothing_length_inverse_square;
-    const float2 x_i = F::f_home(p, d, fr, i);
-    const int c = d.f_cell[i];
     float2 g = make_float2(0.f, 0.f);
     for (int n = 0; n < 9; ++n) {
         const int m = neighbour_cell(c, n, nx, ny);
@@ -567,15 +576,14 @@ __device__ __forceinline__ void pair_particle_listed(const sphnj_params &p, cons
     store_pair(d, i, a);
 }
 
-// Shifting gradient of particle i at CSR position h, through its neighbour
-// list when use_list (and it has one).
+// Shifting gradient of the particle at CSR position h, at x_i in cell c,
+// through its neighbour list when use_list (and it has one).
 template <class F, class Src>
 __device__ __forceinline__ float2 shift_particle_listed(const sphnj_params &p, const DevState &d, const Src &src,
-                                                        int i, int h, bool use_list, Frame fr) {
+                                                        int h, bool use_list, float2 x_i, int c, Frame fr) {
     const int n = use_list ? (int)d.f_nbr_cnt[h] : (int)kNbrNone;
-    if (n == kNbrNone) return shift_particle<F>(p, d, src, i, fr);
+    if (n == kNbrNone) return shift_particle<F>(p, d, src, x_i, c, fr);
     const float R2 = p.impact_distance_square;
-    const float2 x_i = F::f_home(p, d, fr, i);
     const size_t nf = (size_t)p.fluid_number_total;
     const uint4 *col = d.f_nbr + h;  // chunk c at col[c nf]
     float2 g = make_float2(0.f, 0.f);
@@ -696,15 +704,17 @@ template <class F> __device__ __forceinline__ float2 project(float2 g, float2 di
 
 // shiftDisplacementCalculate + correctionUpdate (fluid.cu:369-427) for
 // particle i with shifting gradient g, done by the thread that computed g.
-// The pass reads the positions from f_pos (f_off in the mixed form) and
-// writes the shifted one to f_x_alt, so that every other particle's gradient
-// in this pass still sees the positions before the update; the velocity,
-// boundary type, compensations and the gradient itself are only ever read
-// by particle i's own thread during the shifting passes and are updated in
-// place.  Returns the squared displacement (float bits).
+// The pass reads the position from xin[k] and writes the shifted one to
+// xout[k] - the list-order pair f_xl / f_xl_alt at the particle's CSR
+// position for a listed particle, f_pos (f_off in the mixed form) / f_x_alt
+// at its index otherwise - so that every other particle's gradient in this
+// pass still sees the positions before the update; the velocity, boundary
+// type, compensations and the gradient itself are only ever read by particle
+// i's own thread during the shifting passes and are updated in place.
+// Returns the squared displacement (float bits).
 template <class F>
 __device__ __forceinline__ unsigned int shift_update_particle(const sphnj_params &p, const DevState &d, int i,
-                                                              float2 g) {
+                                                              float2 g, const float2 *xin, float2 *xout, int k) {
     d.f_grad[i] = g;
     // getMaxSpeed's clamp, fluid.cu:438-439
     const float vmax = __fsqrt_rn(__uint_as_float(*d.max_speed2_bits));
@@ -738,21 +748,21 @@ __device__ __forceinline__ unsigned int shift_update_particle(const sphnj_params
     const float2 sh = make_float2(max_speed * dd.x, max_speed * dd.y);
     const float4 m = d.f_dudx[i];
     if constexpr (F::kMixed) {
-        float2 x = d.f_off[i], xc = d.f_offc[i], v = d.f_vel[i], vc = d.f_velc[i];
+        float2 x = xin[k], xc = d.f_offc[i], v = d.f_vel[i], vc = d.f_velc[i];
         const float2 x0 = x;
         kahan_add2(x, xc, sh);
         kahan_add2(v, vc, make_float2(sum2(m.x, sh.x, m.z, sh.y), sum2(m.y, sh.x, m.w, sh.y)));
-        d.f_x_alt[i] = x;
+        xout[k] = x;
         d.f_offc[i] = xc;
         d.f_vel[i] = v;
         d.f_velc[i] = vc;
         return disp2(x0, x);
     } else {
-        const float2 x0 = d.f_pos[i];
+        const float2 x0 = xin[k];
         float2 x = x0;
         x.x += sh.x;
         x.y += sh.y;
-        d.f_x_alt[i] = x;
+        xout[k] = x;
         float2 v = d.f_vel[i];
         v.x += m.x * sh.x + m.z * sh.y;
         v.y += m.y * sh.x + m.w * sh.y;
@@ -823,10 +833,30 @@ __device__ __forceinline__ float2 tile_pos(const sphnj_params &p, const DevState
     }
 }
 
+// The same for the entry at CSR position t, from the shifting passes'
+// list-order positions and cells (contiguous reads over a strip).
+template <class F>
+__device__ __forceinline__ float2 tile_pos_l(const sphnj_params &p, const DevState &d, const TileGeom &g, int s,
+                                             int t) {
+    if constexpr (F::kMixed) {
+        const int col = g.col + s - 1;
+        const int row = __ldg(&d.f_celll[t]) - col * p.cell_number[1];
+        return add2_rn(__ldg(&d.f_xl[t]), cells_to_len(p, s - 1, row - g.row0));
+    } else {
+        return __ldg(&d.f_xl[t]);
+    }
+}
+
 // Frame of home particle i in tile g (mixed form: the tile's origin cell).
 template <class F>
 __device__ __forceinline__ Frame tile_frame(const sphnj_params &p, const DevState &d, const TileGeom &g, int i) {
     if constexpr (F::kMixed) return Frame{0, d.f_cell[i] - g.col * p.cell_number[1] - g.row0};
+    else return Frame{0, 0};
+}
+// ... of the home particle with cell c (its list-order cell)
+template <class F>
+__device__ __forceinline__ Frame tile_frame_c(const sphnj_params &p, const TileGeom &g, int c) {
+    if constexpr (F::kMixed) return Frame{0, c - g.col * p.cell_number[1] - g.row0};
     else return Frame{0, 0};
 }
 
@@ -919,7 +949,7 @@ __global__ void __launch_bounds__(kThreads, 2048 / kThreads)
         if (staged) {
             for (int k = threadIdx.x; k < g.total; k += blockDim.x) {
                 const int s = tile_strip(s_off, k);
-                s_pos[k] = tile_pos<F>(p, d, g, s, __ldg(&d.lst_f[s_base[s] + k - s_off[s]]));
+                s_pos[k] = tile_pos_l<F>(p, d, g, s, s_base[s] + k - s_off[s]);
             }
         }
         __syncthreads();
@@ -927,16 +957,20 @@ __global__ void __launch_bounds__(kThreads, 2048 / kThreads)
             const SrcTile src{s_pos, nullptr, nullptr, nullptr, nullptr, s_base, s_off};
             for (int h = g.home_b + threadIdx.x; h < g.home_e; h += blockDim.x) {
                 const int i = d.lst_f[h];
-                const float2 gr = shift_particle_listed<F>(p, d, src, i, h, use_list, tile_frame<F>(p, d, g, i));
-                moved2 = max(moved2, shift_update_particle<F>(p, d, i, gr));
+                const int c = d.f_celll[h];
+                const Frame fr = tile_frame_c<F>(p, g, c);
+                const float2 gr =
+                    shift_particle_listed<F>(p, d, src, h, use_list, F::f_home_l(p, d, fr, h), c, fr);
+                moved2 = max(moved2, shift_update_particle<F>(p, d, i, gr, d.f_xl, d.f_xl_alt, h));
             }
         } else {
             // a tile the pair pass could not stage has no lists either
-            const SrcGlobal<F> src{&d};
+            const SrcListOrder<F> src{&d};
             for (int h = g.home_b + threadIdx.x; h < g.home_e; h += blockDim.x) {
                 const int i = d.lst_f[h];
-                const float2 gr = shift_particle_listed<F>(p, d, src, i, h, false, Frame{0, 0});
-                moved2 = max(moved2, shift_update_particle<F>(p, d, i, gr));
+                const float2 gr = shift_particle_listed<F>(p, d, src, h, false, F::f_home_l(p, d, Frame{0, 0}, h),
+                                                           d.f_celll[h], Frame{0, 0});
+                moved2 = max(moved2, shift_update_particle<F>(p, d, i, gr, d.f_xl, d.f_xl_alt, h));
             }
         }
     };
@@ -965,19 +999,58 @@ __global__ void __launch_bounds__(kPairBlock) k_fluid_pair_each(const __grid_con
         if (!only_unlisted || d.f_listed[i] != stamp) pair_particle<F>(p, d, src, i, Frame{0, 0});
 }
 
+// The shifting pass one thread per particle: the listed particles by their
+// CSR position, from the list-order positions (only_unlisted 0: the untiled
+// sweep), or the particles in no list, by index, from the particle arrays
+// (only_unlisted 1).  Fluid neighbours are read in list order either way.
 template <class G, class F>
 __global__ void __launch_bounds__(kPairBlock) k_shift_gradient_each(const __grid_constant__ G g, int only_unlisted,
                                                                    int pass) {
     SPHNJ_SCENE(g);
     const int nf = p.fluid_number_total;
-    if (only_unlisted && *d.f_listed_total == nf) return;
-    const int stamp = *d.stamp;
-    const SrcGlobal<F> src{&d};
+    const int listed = *d.f_listed_total;
+    if (only_unlisted && listed == nf) return;
+    const SrcListOrder<F> src{&d};
     unsigned int moved2 = 0u;
-    for (int i = blk * blockDim.x + threadIdx.x; i < nf; i += nblk * blockDim.x)
-        if (!only_unlisted || d.f_listed[i] != stamp)
-            moved2 = max(moved2, shift_update_particle<F>(p, d, i, shift_particle<F>(p, d, src, i, Frame{0, 0})));
+    if (only_unlisted) {
+        const int stamp = *d.stamp;
+        float2 *const x = F::kMixed ? d.f_off : d.f_pos;
+        for (int i = blk * blockDim.x + threadIdx.x; i < nf; i += nblk * blockDim.x)
+            if (d.f_listed[i] != stamp) {
+                const float2 gr = shift_particle<F>(p, d, src, F::f_home(p, d, Frame{0, 0}, i), d.f_cell[i],
+                                                    Frame{0, 0});
+                moved2 = max(moved2, shift_update_particle<F>(p, d, i, gr, x, d.f_x_alt, i));
+            }
+    } else {
+        for (int h = blk * blockDim.x + threadIdx.x; h < listed; h += nblk * blockDim.x) {
+            const float2 gr = shift_particle<F>(p, d, src, F::f_home_l(p, d, Frame{0, 0}, h), d.f_celll[h],
+                                                Frame{0, 0});
+            moved2 = max(moved2, shift_update_particle<F>(p, d, d.lst_f[h], gr, d.f_xl, d.f_xl_alt, h));
+        }
+    }
     if (pass < kMaskShifts) warp_max_to(moved2, &d.disp2_bits[1 + pass]);
+}
+
+// Before the first shifting pass: the listed particles' positions (f_pos,
+// f_off in the mixed form) and cells into list order.
+template <class G, class F> __global__ void __launch_bounds__(kBlock) k_shift_gather(const __grid_constant__ G g) {
+    SPHNJ_SCENE(g);
+    const int h = blk * blockDim.x + threadIdx.x;
+    if (p.shift_per_step <= 0 || h >= *d.f_listed_total) return;
+    const int i = __ldg(&d.lst_f[h]);
+    d.f_xl[h] = (F::kMixed ? d.f_off : d.f_pos)[i];
+    d.f_celll[h] = __ldg(&d.f_cell[i]);
+}
+
+// After the last one (and the copy back of the unlisted particles after an
+// odd number of passes): the listed particles' positions back to the
+// particle arrays, from the list-order buffer the last pass wrote.
+template <class G, class F> __global__ void __launch_bounds__(kBlock) k_shift_scatter(const __grid_constant__ G g) {
+    SPHNJ_SCENE(g);
+    const int h = blk * blockDim.x + threadIdx.x;
+    if (p.shift_per_step <= 0 || h >= *d.f_listed_total) return;
+    const float2 *x = (p.shift_per_step & 1) ? d.f_xl_alt : d.f_xl;
+    (F::kMixed ? d.f_off : d.f_pos)[__ldg(&d.lst_f[h])] = x[h];
 }
 
 // densityToPressure, fluid.cu:15-23
@@ -1200,13 +1273,24 @@ template <class G> struct PositionsExchanged {
 
 template <class F, class G> int shift_pass(cudaStream_t st, G &g, const TileConfig &tc, int pass) {
     using D = typename G::Dev;
-    const PositionsExchanged<G> buffers(g, (pass & 1) != 0);
     auto active = [pass](const Scene &s) { return s.p.fluid_number_total > 0 && pass < s.p.shift_per_step; };
+    int gathered = 0;
+    if (pass == 0)  // the listed particles' positions and cells into list order
+        gathered = launch(
+            g, site_key(SITE_SHIFT_GATHER),
+            [&](const Scene &s) { return active(s) ? grid_for(s.p.fluid_number_total, kBlock) : 0u; },
+            k_shift_gather<D, F>, kBlock, 0, st);
+    const PositionsExchanged<G> buffers(g, (pass & 1) != 0);
     if (!tc.tiled)
-        return launch(
-            g, site_key(SITE_SHIFT_EACH, pass),
-            [&](const Scene &s) { return active(s) ? grid_for(s.p.fluid_number_total, kPairBlock) : 0u; },
-            k_shift_gradient_each<D, F>, kPairBlock, 0, st, 0, pass);
+        return gathered +
+               launch(
+                   g, site_key(SITE_SHIFT_EACH, pass),
+                   [&](const Scene &s) { return active(s) ? grid_for(s.p.fluid_number_total, kPairBlock) : 0u; },
+                   k_shift_gradient_each<D, F>, kPairBlock, 0, st, 0, pass) +
+               launch(
+                   g, site_key(SITE_SHIFT_FALLBACK, pass),
+                   [&](const Scene &s) { return active(s) ? fallback_blocks(s.p.fluid_number_total) : 0u; },
+                   k_shift_gradient_each<D, F>, kPairBlock, 0, st, 1, pass);
     const int cap = tile_cap(max_tile_h(g));
     const size_t smem = cap * sizeof(float2);
     // batched list launches: blocks of kListBlock threads, kTileBlock / kListBlock
@@ -1241,14 +1325,25 @@ template <class F, class G> int shift_pass(cudaStream_t st, G &g, const TileConf
         g, site_key(SITE_SHIFT_FALLBACK, pass),
         [&](const Scene &s) { return active(s) ? fallback_blocks(s.p.fluid_number_total) : 0u; },
         k_shift_gradient_each<D, F>, kPairBlock, 0, st, 1, pass);
-    return n;
+    return gathered + n;
 }
 
+// After the last pass: the unlisted particles' positions back from f_x_alt
+// after an odd number of passes (every particle is copied; the listed ones
+// are overwritten next), then the listed ones from list order.
 template <class F, class G> int shift_copy_back(cudaStream_t st, G &g) {
-    return launch(
+    int n = launch(
         g, site_key(SITE_SHIFT_COPY_BACK),
         [](const Scene &s) { return (s.p.shift_per_step & 1) ? grid_for(s.p.fluid_number_total, kBlock) : 0u; },
         k_shift_copy_back<typename G::Dev, F>, kBlock, 0, st);
+    n += launch(
+        g, site_key(SITE_SHIFT_SCATTER),
+        [](const Scene &s) {
+            return s.p.fluid_number_total > 0 && s.p.shift_per_step > 0 ? grid_for(s.p.fluid_number_total, kBlock)
+                                                                        : 0u;
+        },
+        k_shift_scatter<typename G::Dev, F>, kBlock, 0, st);
+    return n;
 }
 
 }  // namespace
