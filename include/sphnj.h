@@ -302,6 +302,21 @@ int  sphnj_synchronize(sphnj_ctx *ctx);
 /* Copies the selected fields to the caller's buffers (synchronous). */
 int  sphnj_download(sphnj_ctx *ctx, uint32_t field_mask, sphnj_host_state *s);
 
+/* Pinned host memory mapped into every device's address space, for the
+ * arrays of a sphnj_host_state.  Fluid positions, velocities, densities and
+ * pressures that lie in such memory (each array wholly inside one
+ * allocation) are moved by sphnj_upload_fields and sphnj_download in one
+ * kernel that reads or writes them in place over the host link, converting
+ * the mixed form's cell + offset positions on the way, instead of one
+ * copy-engine transfer per field plus a conversion pass.  Results are the
+ * same either way; other memory takes the copy path.  Replaces the
+ * reference's thrust host vectors (particle.cuh:65-81) as the host side of
+ * its per-step copies.  Memory is zeroed.  sphnj_host_free takes only
+ * pointers sphnj_host_alloc returned (SPHNJ_ERR_ARG otherwise); no transfer
+ * may still use it. */
+int  sphnj_host_alloc(uint64_t bytes, void **out);
+int  sphnj_host_free(void *ptr);
+
 /* Current step counter i (SimTime::i, sim_time.cpp:27-40). */
 int  sphnj_get_step(const sphnj_ctx *ctx, int *step);
 

@@ -233,6 +233,13 @@ class Simulation:
     def synchronize(self):
         self._check(self._lib.sphnj_synchronize(self._h), "synchronize")
 
+    def host_state(self, fields=None) -> dict:
+        """Zeroed host arrays for this scene's state (all fields, or those
+        named) in pinned, device-mapped memory (sphnj_host_alloc): uploads
+        and downloads of the fluid positions, velocities, densities and
+        pressures held there run as one kernel over the host link."""
+        return alloc_state(self.params, fields, lib=self._lib)
+
     def download(self, mask: int = abi.F_ALL, into: dict | None = None) -> dict:
         arrays = into if into is not None else alloc_state(self.params)
         s = state_struct(arrays)

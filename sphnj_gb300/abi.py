@@ -192,17 +192,54 @@ def state_struct(arrays: dict) -> HostState:
     return s
 
 
-def alloc_state(p: Params, fields=None) -> dict:
+class HostBlock:
+    """One sphnj_host_alloc allocation (pinned, device-mapped host memory),
+    freed when the last array viewing it is gone."""
+
+    def __init__(self, lib, nbytes: int):
+        self._lib = lib
+        self.ptr = C.c_void_p()
+        rc = lib.sphnj_host_alloc(max(int(nbytes), 1), C.byref(self.ptr))
+        if rc:
+            raise RuntimeError(f"sphnj_host_alloc({nbytes}) failed: {ERROR_NAMES.get(rc, rc)}")
+        self.nbytes = max(int(nbytes), 1)
+
+    def array(self, offset: int, shape, dtype):
+        import numpy as np
+
+        n = int(np.prod(shape)) * np.dtype(dtype).itemsize
+        assert 0 <= offset and offset + n <= self.nbytes
+        buf = (C.c_char * max(n, 1)).from_address(self.ptr.value + offset)
+        buf.owner = self  # the ctypes buffer keeps the block alive
+        return np.frombuffer(buf, dtype=dtype, count=int(np.prod(shape))).reshape(shape)
+
+    def __del__(self):
+        if getattr(self, "ptr", None) and self.ptr.value:
+            self._lib.sphnj_host_free(self.ptr)
+            self.ptr = C.c_void_p()
+
+
+def alloc_state(p: Params, fields=None, lib=None) -> dict:
+    """Zeroed host arrays of a state (all fields, or those named).  With the
+    library given they share one sphnj_host_alloc block (pinned and
+    device-mapped, each array 256-byte aligned), which the transfers move
+    without copy-engine copies; otherwise they are ordinary numpy arrays."""
     import numpy as np
 
-    out = {}
+    spec = []
     for name, _, dtype, width, kind in STATE_FIELDS:
         if fields is not None and name not in fields:
             continue
         n = count_of(p, kind)
-        shape = (n,) if width == 1 else (n, width)
-        out[name] = np.zeros(shape, dtype=dtype)
-    return out
+        spec.append((name, (n,) if width == 1 else (n, width), dtype))
+    if lib is None:
+        return {name: np.zeros(shape, dtype=dtype) for name, shape, dtype in spec}
+    offs, total = [], 0
+    for _, shape, dtype in spec:
+        offs.append(total)
+        total += (int(np.prod(shape)) * np.dtype(dtype).itemsize + 255) // 256 * 256
+    block = HostBlock(lib, total)
+    return {name: block.array(o, shape, dtype) for (name, shape, dtype), o in zip(spec, offs)}
 
 
 def set_cells_args(cells):
@@ -263,6 +300,10 @@ def declare(lib: C.CDLL, prefix: str) -> None:
             g(n).restype = C.c_int
         g("batch_last_error").argtypes = [vp]
         g("batch_last_error").restype = C.c_char_p
+        g("host_alloc").argtypes = [C.c_uint64, C.POINTER(vp)]
+        g("host_alloc").restype = C.c_int
+        g("host_free").argtypes = [vp]
+        g("host_free").restype = C.c_int
         g("checkpoint_size").argtypes = [vp, C.POINTER(C.c_uint64)]
         g("checkpoint_save").argtypes = [vp, vp, C.c_uint64]
         g("checkpoint_load").argtypes = [vp, vp, C.c_uint64]

@@ -315,6 +315,29 @@ int enum_d2h(sphnj_ctx *ctx, int32_t *dst, const uint8_t *src, int n) {
         if (r_) return r_;          \
     } while (0)
 
+// The fluid kinematics (mask bit) and densities / pressures (thermo bit) of s
+// that lie in sphnj_host_alloc memory, aligned for the kernel's float2 /
+// float accesses.
+bool kernel_access(const void *ptr, size_t bytes, size_t align) {
+    return ptr && reinterpret_cast<uintptr_t>(ptr) % align == 0 && host_mapped(ptr, bytes);
+}
+FluidHost fluid_host(uint32_t mask, const sphnj_host_state *s, int nf) {
+    FluidHost h{};
+    if (nf <= 0) return h;
+    const size_t n = (size_t)nf;
+    if (mask & SPHNJ_F_FLUID_KINEMATICS) {
+        if (kernel_access(s->fluid_position, n * sizeof(float2), alignof(float2)))
+            h.pos = reinterpret_cast<float2 *>(s->fluid_position);
+        if (kernel_access(s->fluid_velocity, n * sizeof(float2), alignof(float2)))
+            h.vel = reinterpret_cast<float2 *>(s->fluid_velocity);
+    }
+    if (mask & SPHNJ_F_FLUID_THERMO) {
+        if (kernel_access(s->fluid_density, n * sizeof(float), alignof(float))) h.rho = s->fluid_density;
+        if (kernel_access(s->fluid_pressure, n * sizeof(float), alignof(float))) h.p = s->fluid_pressure;
+    }
+    return h;
+}
+
 }  // namespace
 
 extern "C" {
@@ -627,24 +650,27 @@ int sphnj_upload_fields(sphnj_ctx *ctx, uint32_t mask, const sphnj_host_state *s
     // kinds whose positions are given are re-split (a round trip through an
     // absolute FP32 position would lose the offset's precision).
     const bool mixed = ctx->form == SPHNJ_FORM_MIXED;
+    // fluid fields in device-mapped host memory: one kernel, no copies
+    const FluidHost fh = fluid_host(mask, s, nf);
     int resplit = 0;
     if (mixed) {
-        if ((mask & SPHNJ_F_FLUID_KINEMATICS) && s->fluid_position) resplit |= 1;
+        if ((mask & SPHNJ_F_FLUID_KINEMATICS) && s->fluid_position && !fh.pos) resplit |= 1;
         if ((mask & SPHNJ_F_SOLID_KINEMATICS) &&
             (s->solid_position || s->solid_reference_position || s->solid_velocity))
             resplit |= 2;
         // (a re-split fluid reads only the positions it is given)
         launch_mixed_join(ctx->st, GroupOne{scene_of(ctx, ctx->parity), ctx->form}, resplit & 2);
-        if ((mask & SPHNJ_F_FLUID_KINEMATICS) && s->fluid_velocity && !s->fluid_position)
+        if ((mask & SPHNJ_F_FLUID_KINEMATICS) && s->fluid_velocity && !s->fluid_position && !fh.vel)
             CK(cudaMemsetAsync(d.f_velc, 0, sizeof(float2) * (size_t)nf, ctx->st));
     }
+    launch_fluid_from_host(ctx->st, GroupOne{scene_of(ctx, ctx->parity), ctx->form}, fh);
     if (mask & SPHNJ_F_FLUID_KINEMATICS) {
-        if (s->fluid_position) RET(h2d(ctx, d.f_pos, s->fluid_position, nf));
-        if (s->fluid_velocity) RET(h2d(ctx, d.f_vel, s->fluid_velocity, nf));
+        if (s->fluid_position && !fh.pos) RET(h2d(ctx, d.f_pos, s->fluid_position, nf));
+        if (s->fluid_velocity && !fh.vel) RET(h2d(ctx, d.f_vel, s->fluid_velocity, nf));
     }
     if (mask & SPHNJ_F_FLUID_THERMO) {
-        if (s->fluid_density) RET(h2d(ctx, d.f_rho, s->fluid_density, nf));
-        if (s->fluid_pressure) RET(h2d(ctx, d.f_p, s->fluid_pressure, nf));
+        if (s->fluid_density && !fh.rho) RET(h2d(ctx, d.f_rho, s->fluid_density, nf));
+        if (s->fluid_pressure && !fh.p) RET(h2d(ctx, d.f_p, s->fluid_pressure, nf));
         if (s->fluid_phase) RET(enum_h2d(ctx, d.f_phase, s->fluid_phase, nf));
     }
     if (mask & SPHNJ_F_FLUID_FLAGS) {
@@ -816,18 +842,21 @@ int sphnj_download(sphnj_ctx *ctx, uint32_t mask, sphnj_host_state *s) {
     const sphnj_params &p = ctx->p;
     const int nf = p.fluid_number_total, ns = p.solid_number, nv = p.virt_number;
     const DevState &d = ctx->d;
+    // fluid fields in device-mapped host memory: one kernel, no copies
+    const FluidHost fh = fluid_host(mask, s, nf);
     // mixed form: absolute positions and FP64 solid kinematics from the state
     if (ctx->form == SPHNJ_FORM_MIXED)
         launch_mixed_join(ctx->st, GroupOne{scene_of(ctx, ctx->parity), ctx->form},
-                          ((mask & SPHNJ_F_FLUID_KINEMATICS) ? 1 : 0) |
+                          ((mask & SPHNJ_F_FLUID_KINEMATICS) && !fh.pos ? 1 : 0) |
                               ((mask & (SPHNJ_F_SOLID_KINEMATICS | SPHNJ_F_SOLID_DERIVED)) ? 2 : 0));
+    launch_fluid_to_host(ctx->st, GroupOne{scene_of(ctx, ctx->parity), ctx->form}, fh);
     if (mask & SPHNJ_F_FLUID_KINEMATICS) {
-        RET(d2h(ctx, s->fluid_position, d.f_pos, nf));
-        RET(d2h(ctx, s->fluid_velocity, d.f_vel, nf));
+        if (!fh.pos) RET(d2h(ctx, s->fluid_position, d.f_pos, nf));
+        if (!fh.vel) RET(d2h(ctx, s->fluid_velocity, d.f_vel, nf));
     }
     if (mask & SPHNJ_F_FLUID_THERMO) {
-        RET(d2h(ctx, s->fluid_density, d.f_rho, nf));
-        RET(d2h(ctx, s->fluid_pressure, d.f_p, nf));
+        if (!fh.rho) RET(d2h(ctx, s->fluid_density, d.f_rho, nf));
+        if (!fh.p) RET(d2h(ctx, s->fluid_pressure, d.f_p, nf));
         RET(enum_d2h(ctx, s->fluid_phase, d.f_phase, nf));
     }
     if (mask & SPHNJ_F_FLUID_FLAGS) {

@@ -254,6 +254,20 @@ template <class G> int launch_solid_update(cudaStream_t st, G &g, int sub);
 void launch_mixed_split(cudaStream_t st, const GroupOne &g, int kinds);
 void launch_mixed_join(cudaStream_t st, const GroupOne &g, int kinds);  // bit 0 fluid, bit 1 solid
 
+// Fluid fields in device-mapped host memory (null: not moved), moved in
+// place by one kernel: from_host writes the device state (the mixed form
+// splits the positions as launch_mixed_split does), to_host reads it (the
+// mixed form joins them as launch_mixed_join does, refreshing f_pos too).
+struct FluidHost {
+    float2 *pos, *vel;
+    float *rho, *p;
+    bool any() const { return pos || vel || rho || p; }
+};
+void launch_fluid_from_host(cudaStream_t st, const GroupOne &g, const FluidHost &h);
+void launch_fluid_to_host(cudaStream_t st, const GroupOne &g, const FluidHost &h);
+// whether [ptr, ptr + bytes) lies inside one sphnj_host_alloc allocation
+bool host_mapped(const void *ptr, size_t bytes);
+
 // global diagnostics (kernels_diag.cu): kDiagBlocks x kDiagSlots doubles of
 // per-block partials, then the result in *out (device memory)
 constexpr int kDiagBlocks = 304;

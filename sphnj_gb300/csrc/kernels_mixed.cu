@@ -127,7 +127,94 @@ __global__ void k_join(const __grid_constant__ One g, int kinds) {
     }
 }
 
+// Fluid fields between the device state and device-mapped host arrays, one
+// thread per particle: every host load is issued before any store, so a
+// warp keeps its reads of the host link in flight together.  Positions are
+// split (in) or joined (out) with k_split / k_join's fluid arithmetic, and
+// f_pos is written as those kernels leave it.
+template <bool kMixed>
+__global__ void __launch_bounds__(kBlock) k_fluid_from_host(const __grid_constant__ One g, FluidHost h, double iwx,
+                                                            double iwy) {
+    const Scene &S = g.s;
+    const sphnj_params &p = S.p;
+    const DevState &d = S.d;
+    const long t = (long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= p.fluid_number_total) return;
+    const int i = (int)t;
+    float2 x = make_float2(0.f, 0.f), v = make_float2(0.f, 0.f);
+    float rho = 0.f, pr = 0.f;
+    if (h.pos) x = h.pos[i];
+    if (h.vel) v = h.vel[i];
+    if (h.rho) rho = h.rho[i];
+    if (h.p) pr = h.p[i];
+    if (h.pos) {
+        d.f_pos[i] = x;
+        if constexpr (kMixed) {
+            const Grid2 gr = grid_of(p, iwx, iwy);
+            float2 off;
+            const int2 c = split_pos(gr, x.x, x.y, off, d.err, 0, i);
+            d.f_cell[i] = c.x * gr.ny + c.y;
+            d.f_off[i] = off;
+            d.f_offc[i] = make_float2(0.f, 0.f);
+        }
+    }
+    if (h.vel) d.f_vel[i] = v;
+    // new positions or velocities start without compensation
+    if (kMixed && (h.pos || h.vel)) d.f_velc[i] = make_float2(0.f, 0.f);
+    if (h.rho) d.f_rho[i] = rho;
+    if (h.p) d.f_p[i] = pr;
+}
+
+template <bool kMixed>
+__global__ void __launch_bounds__(kBlock) k_fluid_to_host(const __grid_constant__ One g, FluidHost h) {
+    const Scene &S = g.s;
+    const sphnj_params &p = S.p;
+    const DevState &d = S.d;
+    const long t = (long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= p.fluid_number_total) return;
+    const int i = (int)t;
+    if (h.pos) {
+        float2 x;
+        if constexpr (kMixed) {
+            const Grid2 gr = grid_of(p);
+            const int c = d.f_cell[i];
+            const int cx = c / gr.ny, cy = c - cx * gr.ny;
+            const float2 off = d.f_off[i], oc = d.f_offc[i];
+            x = make_float2((float)(gr.x0 + cx * gr.wx + ((double)off.x - (double)oc.x)),
+                            (float)(gr.y0 + cy * gr.wy + ((double)off.y - (double)oc.y)));
+            d.f_pos[i] = x;
+        } else {
+            x = d.f_pos[i];
+        }
+        h.pos[i] = x;
+    }
+    if (h.vel) h.vel[i] = d.f_vel[i];
+    if (h.rho) h.rho[i] = d.f_rho[i];
+    if (h.p) h.p[i] = d.f_p[i];
+}
+
 }  // namespace
+
+void launch_fluid_from_host(cudaStream_t st, const GroupOne &g, const FluidHost &h) {
+    const sphnj_params &p = g.s.p;
+    if (p.fluid_number_total <= 0 || !h.any()) return;
+    const unsigned blocks = grid_for(p.fluid_number_total, kBlock);
+    if (g.form == SPHNJ_FORM_MIXED)
+        k_fluid_from_host<true><<<blocks, kBlock, 0, st>>>(One{g.s}, h, 1.0 / (double)p.interval[0],
+                                                           1.0 / (double)p.interval[1]);
+    else
+        k_fluid_from_host<false><<<blocks, kBlock, 0, st>>>(One{g.s}, h, 0.0, 0.0);
+}
+
+void launch_fluid_to_host(cudaStream_t st, const GroupOne &g, const FluidHost &h) {
+    const sphnj_params &p = g.s.p;
+    if (p.fluid_number_total <= 0 || !h.any()) return;
+    const unsigned blocks = grid_for(p.fluid_number_total, kBlock);
+    if (g.form == SPHNJ_FORM_MIXED)
+        k_fluid_to_host<true><<<blocks, kBlock, 0, st>>>(One{g.s}, h);
+    else
+        k_fluid_to_host<false><<<blocks, kBlock, 0, st>>>(One{g.s}, h);
+}
 
 void launch_mixed_split(cudaStream_t st, const GroupOne &g, int kinds) {
     const sphnj_params &p = g.s.p;

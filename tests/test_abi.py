@@ -50,3 +50,14 @@ def test_no_cpu_fallback_in_the_product():
     pkg = Path(S.__file__).resolve().parent
     for f in pkg.rglob("*.py"):
         assert "oracle" not in re.findall(r"^\s*(?:from|import)\s+(\w+)", f.read_text(), flags=re.M), f
+
+
+def test_host_free_refuses_memory_it_did_not_allocate():
+    """sphnj_host_free checks its registry before any CUDA call, so this runs
+    without a GPU."""
+    import numpy as np
+
+    lib = S.lib()
+    x = np.zeros(16, np.float32)
+    assert lib.sphnj_host_free(C.c_void_p(x.ctypes.data)) == abi.ERR_ARG
+    assert lib.sphnj_host_free(None) == 0
