@@ -348,8 +348,11 @@ int  sphnj_debug_max_speed(sphnj_ctx *ctx, float *max_speed);
 /* Launch configuration of the fluid neighbour sweeps (pair pass and shifting
  * gradient): tiled != 0 stages the neighbours of a column segment of tile_h
  * cells (1..64) in shared memory per block; 0 runs one thread per particle.
- * Both sum the same terms in the same order, so results are identical; only
- * the speed differs.  Default: tiled, tile_h = 16. */
+ * Both sum the same terms in the same order: plain-form results are
+ * identical, only the speed differs.  The mixed form takes neighbour
+ * offsets in the frame of the tile's first cell (tiled) or of the particle's
+ * own cell (one thread per particle), so tiling and tile height change its
+ * results in rounding only.  Default: tiled, tile_h = 16. */
 int  sphnj_set_tiling(sphnj_ctx *ctx, int tiled, int tile_h);
 
 /* on != 0 (default): each kind of step (sort or rebuild step, list buffer,
@@ -390,7 +393,9 @@ int  sphnj_get_block_sizes(const sphnj_ctx *ctx, int *shift_threads, int *pair_t
  * is tuned with the other's fixed.  Each candidate runs `steps` steps from a
  * device copy of the current state (once to capture its graphs, once timed
  * with CUDA events); the state is put back after each trial, so tuning does
- * not advance or change the run.  The fastest candidate is installed and
+ * not advance or change the run (in the mixed form the installed tile height
+ * then sets the rounding of later steps, as for sphnj_set_tiling).  The
+ * fastest candidate is installed and
  * reported: tile_h / lists are those of class 0 (the only class of a single
  * scene); class_split is the fluid particle count at which class 1 starts
  * (0 with one class). */
