@@ -721,8 +721,12 @@ template <class F> __device__ __forceinline__ float2 project(float2 g, float2 di
 // Returns the squared displacement (float bits).
 template <class F>
 __device__ __forceinline__ unsigned int shift_update_particle(const sphnj_params &p, const DevState &d, int i,
-                                                              float2 g, const float2 *xin, float2 *xout, int k) {
-    d.f_grad[i] = g;
+                                                              float2 g, const float2 *xin, float2 *xout, int k,
+                                                              bool last) {
+    // the gradient and boundary type are state only after the step's last
+    // pass (no pass reads them): earlier passes skip the two stores
+    // (4.15M dam break: shifting stage 1.985 -> 1.953 ms/step)
+    if (last) d.f_grad[i] = g;
     // getMaxSpeed's clamp, fluid.cu:438-439
     const float vmax = __fsqrt_rn(__uint_as_float(*d.max_speed2_bits));
     const float max_speed = fminf(vmax, __fmul_rn(0.1f, fminf(p.sound_speed[0], p.sound_speed[1])));
@@ -751,7 +755,7 @@ __device__ __forceinline__ unsigned int shift_update_particle(const sphnj_params
         bt = SPHNJ_INNER;
         dd = disp;
     }
-    d.f_fbt[i] = bt;
+    if (last) d.f_fbt[i] = bt;
     const float2 sh = make_float2(max_speed * dd.x, max_speed * dd.y);
     const float4 m = d.f_dudx[i];
     if constexpr (F::kMixed) {
@@ -934,6 +938,7 @@ __global__ void __launch_bounds__(kThreads, 2048 / kThreads)
     k_shift_gradient_tiled(const __grid_constant__ G gs, int cap, int pass) {
     SPHNJ_SCENE(gs);
     const int tile_h = S.tile_h;
+    const bool last = pass + 1 >= p.shift_per_step;
     extern __shared__ __align__(16) unsigned char smem[];
     __shared__ int s_base[3], s_off[3];
     float2 *s_pos = reinterpret_cast<float2 *>(smem);
@@ -968,7 +973,7 @@ __global__ void __launch_bounds__(kThreads, 2048 / kThreads)
                 const Frame fr = tile_frame_c<F>(p, g, c);
                 const float2 gr =
                     shift_particle_listed<F>(p, d, src, h, use_list, F::f_home_l(p, d, fr, h), c, fr);
-                moved2 = max(moved2, shift_update_particle<F>(p, d, i, gr, d.f_xl, d.f_xl_alt, h));
+                moved2 = max(moved2, shift_update_particle<F>(p, d, i, gr, d.f_xl, d.f_xl_alt, h, last));
             }
         } else {
             // a tile the pair pass could not stage has no lists either
@@ -977,7 +982,7 @@ __global__ void __launch_bounds__(kThreads, 2048 / kThreads)
                 const int i = d.lst_f[h];
                 const float2 gr = shift_particle_listed<F>(p, d, src, h, false, F::f_home_l(p, d, Frame{0, 0}, h),
                                                            d.f_celll[h], Frame{0, 0});
-                moved2 = max(moved2, shift_update_particle<F>(p, d, i, gr, d.f_xl, d.f_xl_alt, h));
+                moved2 = max(moved2, shift_update_particle<F>(p, d, i, gr, d.f_xl, d.f_xl_alt, h, last));
             }
         }
     };
@@ -1017,6 +1022,7 @@ __global__ void __launch_bounds__(kPairBlock) k_shift_gradient_each(const __grid
     const int nf = p.fluid_number_total;
     const int listed = *d.f_listed_total;
     if (only_unlisted && listed == nf) return;
+    const bool last = pass + 1 >= p.shift_per_step;
     const SrcListOrder<F> src{&d};
     unsigned int moved2 = 0u;
     if (only_unlisted) {
@@ -1026,13 +1032,13 @@ __global__ void __launch_bounds__(kPairBlock) k_shift_gradient_each(const __grid
             if (d.f_listed[i] != stamp) {
                 const float2 gr = shift_particle<F>(p, d, src, F::f_home(p, d, Frame{0, 0}, i), d.f_cell[i],
                                                     Frame{0, 0});
-                moved2 = max(moved2, shift_update_particle<F>(p, d, i, gr, x, d.f_x_alt, i));
+                moved2 = max(moved2, shift_update_particle<F>(p, d, i, gr, x, d.f_x_alt, i, last));
             }
     } else {
         for (int h = blk * blockDim.x + threadIdx.x; h < listed; h += nblk * blockDim.x) {
             const float2 gr = shift_particle<F>(p, d, src, F::f_home_l(p, d, Frame{0, 0}, h), d.f_celll[h],
                                                 Frame{0, 0});
-            moved2 = max(moved2, shift_update_particle<F>(p, d, d.lst_f[h], gr, d.f_xl, d.f_xl_alt, h));
+            moved2 = max(moved2, shift_update_particle<F>(p, d, d.lst_f[h], gr, d.f_xl, d.f_xl_alt, h, last));
         }
     }
     if (pass < kMaskShifts) warp_max_to(moved2, &d.disp2_bits[1 + pass]);
