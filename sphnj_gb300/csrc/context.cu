@@ -190,6 +190,7 @@ size_t layout(sphnj_ctx *ctx, char *base) {
     const bool mixed = ctx->form == SPHNJ_FORM_MIXED;
     if (mixed) {
         d.f_off = a.take<float2>(nf); d.f_offc = a.take<float2>(nf); d.f_velc = a.take<float2>(nf);
+        d.f_x0l = a.take<float2>(nf); d.f_xc0l = a.take<float2>(nf);
         d.s_rc = a.take<int2>(ns);
         d.s_roff = a.take<float2>(ns); d.s_u = a.take<float2>(ns); d.s_uc = a.take<float2>(ns);
         d.s_v = a.take<float2>(ns); d.s_vc = a.take<float2>(ns); d.s_off = a.take<float2>(ns);

@@ -99,6 +99,10 @@ struct DevState {
     // particle is listed in) plus an FP32 offset from that cell's lower-left
     // corner; fluid positions and velocities carry Kahan compensations.
     float2 *f_off, *f_offc, *f_velc;
+    // the listed fluid particles' offsets and their compensations before the
+    // step's first shifting pass, in list order (the velocity correction of
+    // all passes is applied once, from the total displacement, after the last)
+    float2 *f_x0l, *f_xc0l;
     // Solids: reference position = reference cell (x, y) + FP32 offset;
     // current position = reference position + FP32 displacement u (Kahan);
     // s_off is the current offset from the corner of s_cell (set by binning).

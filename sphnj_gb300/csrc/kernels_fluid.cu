@@ -722,7 +722,7 @@ template <class F> __device__ __forceinline__ float2 project(float2 g, float2 di
 template <class F>
 __device__ __forceinline__ unsigned int shift_update_particle(const sphnj_params &p, const DevState &d, int i,
                                                               float2 g, const float2 *xin, float2 *xout, int k,
-                                                              bool last) {
+                                                              bool last, bool listed) {
     // the gradient and boundary type are state only after the step's last
     // pass (no pass reads them): earlier passes skip the two stores
     // (4.15M dam break: shifting stage 1.985 -> 1.953 ms/step)
@@ -757,18 +757,34 @@ __device__ __forceinline__ unsigned int shift_update_particle(const sphnj_params
     }
     if (last) d.f_fbt[i] = bt;
     const float2 sh = make_float2(max_speed * dd.x, max_speed * dd.y);
-    const float4 m = d.f_dudx[i];
     if constexpr (F::kMixed) {
-        float2 x = xin[k], xc = d.f_offc[i], v = d.f_vel[i], vc = d.f_velc[i];
+        float2 x = xin[k], xc = d.f_offc[i];
         const float2 x0 = x;
         kahan_add2(x, xc, sh);
-        kahan_add2(v, vc, make_float2(sum2(m.x, sh.x, m.z, sh.y), sum2(m.y, sh.x, m.w, sh.y)));
         xout[k] = x;
         d.f_offc[i] = xc;
-        d.f_vel[i] = v;
-        d.f_velc[i] = vc;
+        // the velocity correction is linear in the shift with the pair
+        // pass's du_dx, which no pass changes: a listed particle takes the
+        // sum of its passes' corrections once, in the last pass, from its
+        // total displacement (offset and compensation differences against
+        // the values gathered before the first pass; the cell is the same in
+        // every pass); an unlisted particle takes one per pass
+        if (!listed || last) {
+            float2 dx = sh;
+            if (listed) {
+                const float2 s0 = d.f_x0l[k], c0 = d.f_xc0l[k];
+                dx = make_float2(__fsub_rn(__fsub_rn(x.x, s0.x), __fsub_rn(xc.x, c0.x)),
+                                 __fsub_rn(__fsub_rn(x.y, s0.y), __fsub_rn(xc.y, c0.y)));
+            }
+            const float4 m = d.f_dudx[i];
+            float2 v = d.f_vel[i], vc = d.f_velc[i];
+            kahan_add2(v, vc, make_float2(sum2(m.x, dx.x, m.z, dx.y), sum2(m.y, dx.x, m.w, dx.y)));
+            d.f_vel[i] = v;
+            d.f_velc[i] = vc;
+        }
         return disp2(x0, x);
     } else {
+        const float4 m = d.f_dudx[i];
         const float2 x0 = xin[k];
         float2 x = x0;
         x.x += sh.x;
@@ -973,7 +989,7 @@ __global__ void __launch_bounds__(kThreads, 2048 / kThreads)
                 const Frame fr = tile_frame_c<F>(p, g, c);
                 const float2 gr =
                     shift_particle_listed<F>(p, d, src, h, use_list, F::f_home_l(p, d, fr, h), c, fr);
-                moved2 = max(moved2, shift_update_particle<F>(p, d, i, gr, d.f_xl, d.f_xl_alt, h, last));
+                moved2 = max(moved2, shift_update_particle<F>(p, d, i, gr, d.f_xl, d.f_xl_alt, h, last, true));
             }
         } else {
             // a tile the pair pass could not stage has no lists either
@@ -982,7 +998,7 @@ __global__ void __launch_bounds__(kThreads, 2048 / kThreads)
                 const int i = d.lst_f[h];
                 const float2 gr = shift_particle_listed<F>(p, d, src, h, false, F::f_home_l(p, d, Frame{0, 0}, h),
                                                            d.f_celll[h], Frame{0, 0});
-                moved2 = max(moved2, shift_update_particle<F>(p, d, i, gr, d.f_xl, d.f_xl_alt, h, last));
+                moved2 = max(moved2, shift_update_particle<F>(p, d, i, gr, d.f_xl, d.f_xl_alt, h, last, true));
             }
         }
     };
@@ -1032,13 +1048,13 @@ __global__ void __launch_bounds__(kPairBlock) k_shift_gradient_each(const __grid
             if (d.f_listed[i] != stamp) {
                 const float2 gr = shift_particle<F>(p, d, src, F::f_home(p, d, Frame{0, 0}, i), d.f_cell[i],
                                                     Frame{0, 0});
-                moved2 = max(moved2, shift_update_particle<F>(p, d, i, gr, x, d.f_x_alt, i, last));
+                moved2 = max(moved2, shift_update_particle<F>(p, d, i, gr, x, d.f_x_alt, i, last, false));
             }
     } else {
         for (int h = blk * blockDim.x + threadIdx.x; h < listed; h += nblk * blockDim.x) {
             const float2 gr = shift_particle<F>(p, d, src, F::f_home_l(p, d, Frame{0, 0}, h), d.f_celll[h],
                                                 Frame{0, 0});
-            moved2 = max(moved2, shift_update_particle<F>(p, d, d.lst_f[h], gr, d.f_xl, d.f_xl_alt, h, last));
+            moved2 = max(moved2, shift_update_particle<F>(p, d, d.lst_f[h], gr, d.f_xl, d.f_xl_alt, h, last, true));
         }
     }
     if (pass < kMaskShifts) warp_max_to(moved2, &d.disp2_bits[1 + pass]);
@@ -1051,8 +1067,13 @@ template <class G, class F> __global__ void __launch_bounds__(kBlock) k_shift_ga
     const int h = blk * blockDim.x + threadIdx.x;
     if (p.shift_per_step <= 0 || h >= *d.f_listed_total) return;
     const int i = __ldg(&d.lst_f[h]);
-    d.f_xl[h] = (F::kMixed ? d.f_off : d.f_pos)[i];
+    const float2 x = (F::kMixed ? d.f_off : d.f_pos)[i];
+    d.f_xl[h] = x;
     d.f_celll[h] = __ldg(&d.f_cell[i]);
+    if constexpr (F::kMixed) {
+        d.f_x0l[h] = x;
+        d.f_xc0l[h] = d.f_offc[i];
+    }
 }
 
 // After the last one (and the copy back of the unlisted particles after an
