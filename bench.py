@@ -448,7 +448,7 @@ def run_ours(args):
     d_ms, d_calls, d_kern = prof[dom]
     avg_ms = d_ms / max(d_calls, 1)
     mixed = form == abi.FORM_MIXED
-    bpl = byte_model.bytes_per_launch(dom, nf, ns, nv, mixed)
+    bpl = byte_model.bytes_per_launch(dom, nf, ns, nv, mixed, shifts=p.shift_per_step)
     peaks = {}
     try:
         peaks = json.loads((ROOT / "MEASURED_PEAKS.json").read_text())
@@ -467,7 +467,7 @@ def run_ours(args):
                                           source="ncu smsp__issue_active of one launch at 2.08M particles")
                                      if mixed else None),
                 "stage_share": {k: round(v[0] / total_ms, 4) for k, v in prof.items() if v[1]}}
-    step_bytes = byte_model.bytes_per_step(nf, ns, nv, p.shift_per_step, p.solid_sub_step)
+    step_bytes = byte_model.step_bytes(nf, ns, nv, p.shift_per_step, p.solid_sub_step, mixed)
 
     # ---- end to end through the C ABI with pinned host buffers ---------------
     e2e = None

@@ -13,16 +13,19 @@ neighbour re-reads are not counted.  Sizes are those of the plain form
                                     gradient 8, du_dx 16 = 41
   fluid_update              57      read pos 8, vel 8, du_dt 8, rho 4, drho 4, phase 1 = 33;
                                     write pos 8, vel 8, rho 4, p 4 = 24
-  shift_pass                63      gradient and update in one sweep: read pos 8, color 4,
-                                    near 1, phase 1, du_dx 16, vel 8 = 38; write gradient 8,
-                                    pos 8 (the other buffer), vel 8, boundary 1 = 25
+  shift_pass                54      one shifting pass, gradient and update in one sweep:
+                                    read pos 8, color 4, near 1, phase 1, du_dx 16, vel 8 = 38;
+                                    write pos 8 (the other buffer), vel 8 = 16
+  shift_last                9       the step's last pass also writes the gradient 8 and the
+                                    boundary type 1 (earlier passes' values are never read)
   shift_copy_back           16      read pos 8, write pos 8 (odd S only)
   virt_data (per virtual)   34      read pos 8, normal 8, phase 1, boundary 1, cell 4;
                                     write vel 8, p 4, rho 4, phase 1 (~34 with the cell id)
   solid per fluid step      48      bin 20 + coupling 28
   solid per sub-step        440     deformation ~178 + force ~181 + update ~81
 
-B_step = N_f (153 + 63 S + 16 (S odd)) + N_v 46 + N_s (48 + 440 k)   (S shifts, k sub-steps)
+B_step = N_f (153 + 54 S + 9 [S > 0] + 16 [S odd]) + N_v 46 + N_s (48 + 440 k)
+(S shifting passes, k solid sub-steps)
 """
 from __future__ import annotations
 
@@ -32,7 +35,8 @@ PER_PARTICLE = {
     "sort": 2 * 50,  # per sort call (the amortised 2 B/step of the model, over 50 steps)
     "fluid_pair": 67,
     "fluid_update": 57,
-    "shift_pass": 63,
+    "shift_pass": 54,
+    "shift_last": 9,
     "shift_copy_back": 16,
     "virt_data": 34,
     "solid_couple": 28,
@@ -44,7 +48,7 @@ PER_PARTICLE = {
 # which particle count a stage's bytes scale with
 STAGE_KIND = {
     "bin": "all", "rebuild": "fluid", "sort": "fluid", "fluid_pair": "fluid", "fluid_update": "fluid",
-    "shift_pass": "fluid", "shift_copy_back": "fluid", "virt_data": "virt", "solid_couple": "solid",
+    "shift_pass": "fluid", "shift_last": "fluid", "shift_copy_back": "fluid", "virt_data": "virt", "solid_couple": "solid",
     "solid_deformation": "solid", "solid_force": "solid", "solid_update": "solid", "capacity": "none",
 }
 
@@ -53,27 +57,35 @@ STAGE_KIND = {
 # (the rest are as above):
 #   bin             20   read cell 4 + offset 8, write cell 4 + offset 8 when a particle
 #                        changes cell (counted always: 12 + 8)
-#   fluid_pair      71   the pair pass's 67 + the cell id of each staged neighbour 4
+#   fluid_pair      71   the pair pass's 67 + 4: the home position is a cell id 4 and an
+#                        offset 8
 #   fluid_update    89   57 + offset and velocity compensations read and written 32
-#   shift_pass      99   63 + the cell id of each staged neighbour 4 + the two
-#                        compensations read and written 32
+#   shift_pass      42   read cell 4 + offset 8, color 4, near 1, phase 1, offset
+#                        compensation 8 = 26; write offset 8, compensation 8 = 16.  A
+#                        listed particle's velocity correction is linear in the shift with
+#                        a du_dx no pass changes, so it is applied once, in the last pass
+#   shift_last      73   gradient 8 and boundary type 1 written; du_dx 16, velocity and its
+#                        compensation 16, offset and compensation before the first pass 16
+#                        read; velocity and compensation written 16
 #   solid passes         FP32 state: deformation 8 + 8 + 8 + 8 read (reference cell, offset,
 #                        displacement of i; neighbours counted once) + writes F, P, L 96 and
 #                        P L, F L 32 = 160; force 8 + 8 + 8 + 16 + 16 + 4 + 1 read, 16 write = 77;
 #                        update 8 + 8 + 8 + 8 + 8 + 1 + 8 read (+ reference cell / offset 16 for the
 #                        current offset), 8 x 5 write = 105
-PER_PARTICLE_MIXED = dict(PER_PARTICLE, bin=20, fluid_pair=71, fluid_update=89, shift_pass=99,
+PER_PARTICLE_MIXED = dict(PER_PARTICLE, bin=20, fluid_pair=71, fluid_update=89, shift_pass=42, shift_last=73,
                           solid_deformation=160, solid_force=77, solid_update=105)
 
 
-def bytes_per_launch(stage: str, nf: int, ns: int, nv: int, mixed: bool = False) -> float:
+def bytes_per_launch(stage: str, nf: int, ns: int, nv: int, mixed: bool = False, shifts: int = 0) -> float:
+    """Compulsory bytes of one launch of a stage; for the shifting passes the
+    average launch of a step of `shifts` passes (the last one writes more)."""
+    t = PER_PARTICLE_MIXED if mixed else PER_PARTICLE
     kind = STAGE_KIND.get(stage, "none")
     n = {"all": nf + ns + nv, "fluid": nf, "solid": ns, "virt": nv, "none": 0}[kind]
-    return float((PER_PARTICLE_MIXED if mixed else PER_PARTICLE).get(stage, 0) * n)
-
-
-def bytes_per_step(nf: int, ns: int, nv: int, shifts: int, substeps: int) -> float:
-    return float(nf * (153 + 63 * shifts + 16 * (shifts & 1)) + nv * 46 + ns * (48 + 440 * substeps))
+    b = float(t.get(stage, 0))
+    if stage == "shift_pass" and shifts > 0:
+        b += t["shift_last"] / shifts
+    return b * n
 
 
 def step_bytes(nf: int, ns: int, nv: int, shifts: int, substeps: int, mixed: bool = False) -> float:
@@ -86,12 +98,17 @@ def step_bytes(nf: int, ns: int, nv: int, shifts: int, substeps: int, mixed: boo
     b = (nf + ns + nv) * t["bin"]
     if nf:
         b += nf * (t["rebuild"] + t["sort"] / 50 + t["fluid_pair"] + t["fluid_update"] + shifts * t["shift_pass"]
-                   + (shifts & 1) * t["shift_copy_back"])
+                   + (shifts > 0) * t["shift_last"] + (shifts & 1) * t["shift_copy_back"])
     b += nv * t["virt_data"]
     if ns:
         b += ns * ((t["solid_couple"] if nf else 0) + substeps * (t["solid_deformation"] + t["solid_force"]
                                                                    + t["solid_update"]))
     return float(b)
+
+
+def bytes_per_step(nf: int, ns: int, nv: int, shifts: int, substeps: int) -> float:
+    """The plain form's step_bytes (the closed formula of the table above)."""
+    return step_bytes(nf, ns, nv, shifts, substeps, mixed=False)
 
 
 # DRAM traffic (dram__bytes_read.sum + dram__bytes_write.sum) per fluid
