@@ -166,6 +166,7 @@ size_t layout(sphnj_ctx *ctx, char *base) {
     d.f_xl = a.take<float2>(nf);
     d.f_xl_alt = a.take<float2>(nf);
     d.f_celll = a.take<int>(nf);
+    d.f_btl = a.take<uint8_t>(nf);
     d.f_listed = a.take<int>(nf);
     ctx->f_listed_total = a.take<int>(1);
     d.f_listed_total = ctx->f_listed_total;
@@ -190,7 +191,7 @@ size_t layout(sphnj_ctx *ctx, char *base) {
     const bool mixed = ctx->form == SPHNJ_FORM_MIXED;
     if (mixed) {
         d.f_off = a.take<float2>(nf); d.f_offc = a.take<float2>(nf); d.f_velc = a.take<float2>(nf);
-        d.f_x0l = a.take<float2>(nf); d.f_xc0l = a.take<float2>(nf);
+        d.f_x0l = a.take<float2>(nf); d.f_xc0l = a.take<float2>(nf); d.f_offcl = a.take<float2>(nf);
         d.s_rc = a.take<int2>(ns);
         d.s_roff = a.take<float2>(ns); d.s_u = a.take<float2>(ns); d.s_uc = a.take<float2>(ns);
         d.s_v = a.take<float2>(ns); d.s_vc = a.take<float2>(ns); d.s_off = a.take<float2>(ns);

@@ -53,6 +53,7 @@ struct DevState {
     // back.  Particles in no list stay in the particle arrays.
     float2 *f_xl, *f_xl_alt;
     int *f_celll;
+    uint8_t *f_btl;  // boundary types the shifting update assigns, gathered with them
     // solid
     double2 *s_pos, *s_ref, *s_vel, *s_dudt;
     dmat2 *s_F, *s_P, *s_L, *s_maxstrain;
@@ -103,6 +104,9 @@ struct DevState {
     // step's first shifting pass, in list order (the velocity correction of
     // all passes is applied once, from the total displacement, after the last)
     float2 *f_x0l, *f_xc0l;
+    // the listed particles' offset compensations during the shifting passes,
+    // in list order (back to f_offc after the last pass)
+    float2 *f_offcl;
     // Solids: reference position = reference cell (x, y) + FP32 offset;
     // current position = reference position + FP32 displacement u (Kahan);
     // s_off is the current offset from the corner of s_cell (set by binning).

@@ -709,60 +709,61 @@ template <class F> __device__ __forceinline__ float2 project(float2 g, float2 di
     }
 }
 
-// shiftDisplacementCalculate + correctionUpdate (fluid.cu:369-427) for
-// particle i with shifting gradient g, done by the thread that computed g.
-// The pass reads the position from xin[k] and writes the shifted one to
-// xout[k] - the list-order pair f_xl / f_xl_alt at the particle's CSR
-// position for a listed particle, f_pos (f_off in the mixed form) / f_x_alt
-// at its index otherwise - so that every other particle's gradient in this
-// pass still sees the positions before the update; the velocity, boundary
-// type, compensations and the gradient itself are only ever read by particle
-// i's own thread during the shifting passes and are updated in place.
-// Returns the squared displacement (float bits).
+// Boundary type of a fluid particle as the shifting update assigns it
+// (shiftDisplacementCalculate, fluid.cu:380-412): a function of its phase,
+// colour and near flag, which only the pair pass sets, so it is the same in
+// every pass of a step (the listed particles' types are computed once, in
+// list order, before the first pass).
+__device__ __forceinline__ uint8_t shift_class(int ph, float color, int near) {
+    if (ph == SPHNJ_GAS) return SPHNJ_INNER;
+    if (color < 1.5f) return near == SPHNJ_NO_PARTICLE ? SPHNJ_SPLASH : SPHNJ_FREE_SURFACE;
+    if (color < 2.0f && near == SPHNJ_HAS_NEAR_PARTICLE) return SPHNJ_VICINITY;
+    return SPHNJ_INNER;
+}
+
+// shiftDisplacementCalculate + correctionUpdate (fluid.cu:369-427) for one
+// particle with shifting gradient g, done by the thread that computed g.
+// A listed particle is addressed by its CSR position k (i < 0: its index is
+// read from the list only where a particle-order field is touched); an
+// unlisted one by its index, k = i.  The pass reads the position from xin[k]
+// and writes the shifted one to xout[k] - the list-order pair f_xl / f_xl_alt
+// for a listed particle, f_pos (f_off in the mixed form) / f_x_alt otherwise -
+// so that every other particle's gradient in this pass still sees the
+// positions before the update; the boundary type, the velocity, the
+// compensations and the gradient are only ever read by the particle's own
+// thread during the shifting passes and are updated in place.  Returns the
+// squared displacement (float bits).
 template <class F>
-__device__ __forceinline__ unsigned int shift_update_particle(const sphnj_params &p, const DevState &d, int i,
-                                                              float2 g, const float2 *xin, float2 *xout, int k,
-                                                              bool last, bool listed) {
-    // the gradient and boundary type are state only after the step's last
-    // pass (no pass reads them): earlier passes skip the two stores
-    // (4.15M dam break: shifting stage 1.985 -> 1.953 ms/step)
-    if (last) d.f_grad[i] = g;
+__device__ __forceinline__ unsigned int shift_update_particle(const sphnj_params &p, const DevState &d, int i, int k,
+                                                              float2 g, const float2 *xin, float2 *xout, bool last,
+                                                              bool listed) {
+    auto index = [&] { return i >= 0 ? i : __ldg(&d.lst_f[k]); };
     // getMaxSpeed's clamp, fluid.cu:438-439
     const float vmax = __fsqrt_rn(__uint_as_float(*d.max_speed2_bits));
     const float max_speed = fminf(vmax, __fmul_rn(0.1f, fminf(p.sound_speed[0], p.sound_speed[1])));
     const float s = -p.particle_shift_coef * p.smoothing_length * p.dt;
     const float2 disp = make_float2(s * g.x, s * g.y);
-    const int ph = d.f_phase[i];
-    const float color = d.f_color[i];
-    const int near = d.f_near[i];
+    const uint8_t bt = listed ? d.f_btl[k] : shift_class(d.f_phase[i], d.f_color[i], d.f_near[i]);
     float2 dd;
-    uint8_t bt;
-    if (ph == SPHNJ_GAS) {
-        bt = SPHNJ_INNER;
-        dd = disp;
-    } else if (color < 1.5f) {
-        if (near == SPHNJ_NO_PARTICLE) {
-            bt = SPHNJ_SPLASH;
-            dd = make_float2(0.f, 0.f);
-        } else {
-            bt = SPHNJ_FREE_SURFACE;
-            dd = project<F>(g, disp);
-        }
-    } else if (color < 2.0f && near == SPHNJ_HAS_NEAR_PARTICLE) {
-        bt = SPHNJ_VICINITY;
-        dd = project<F>(g, disp);
-    } else {
-        bt = SPHNJ_INNER;
-        dd = disp;
+    if (bt == SPHNJ_SPLASH) dd = make_float2(0.f, 0.f);
+    else if (bt == SPHNJ_FREE_SURFACE || bt == SPHNJ_VICINITY) dd = project<F>(g, disp);
+    else dd = disp;
+    // the gradient and boundary type are state only after the step's last
+    // pass (no pass reads them): earlier passes skip the two stores
+    // (4.15M dam break: shifting stage 1.985 -> 1.953 ms/step)
+    if (last) {
+        const int ii = index();
+        d.f_grad[ii] = g;
+        d.f_fbt[ii] = bt;
     }
-    if (last) d.f_fbt[i] = bt;
     const float2 sh = make_float2(max_speed * dd.x, max_speed * dd.y);
     if constexpr (F::kMixed) {
-        float2 x = xin[k], xc = d.f_offc[i];
+        float2 *const cp = listed ? d.f_offcl + k : d.f_offc + i;
+        float2 x = xin[k], xc = *cp;
         const float2 x0 = x;
         kahan_add2(x, xc, sh);
         xout[k] = x;
-        d.f_offc[i] = xc;
+        *cp = xc;
         // the velocity correction is linear in the shift with the pair
         // pass's du_dx, which no pass changes: a listed particle takes the
         // sum of its passes' corrections once, in the last pass, from its
@@ -776,24 +777,26 @@ __device__ __forceinline__ unsigned int shift_update_particle(const sphnj_params
                 dx = make_float2(__fsub_rn(__fsub_rn(x.x, s0.x), __fsub_rn(xc.x, c0.x)),
                                  __fsub_rn(__fsub_rn(x.y, s0.y), __fsub_rn(xc.y, c0.y)));
             }
-            const float4 m = d.f_dudx[i];
-            float2 v = d.f_vel[i], vc = d.f_velc[i];
+            const int ii = index();
+            const float4 m = d.f_dudx[ii];
+            float2 v = d.f_vel[ii], vc = d.f_velc[ii];
             kahan_add2(v, vc, make_float2(sum2(m.x, dx.x, m.z, dx.y), sum2(m.y, dx.x, m.w, dx.y)));
-            d.f_vel[i] = v;
-            d.f_velc[i] = vc;
+            d.f_vel[ii] = v;
+            d.f_velc[ii] = vc;
         }
         return disp2(x0, x);
     } else {
-        const float4 m = d.f_dudx[i];
+        const int ii = index();
+        const float4 m = d.f_dudx[ii];
         const float2 x0 = xin[k];
         float2 x = x0;
         x.x += sh.x;
         x.y += sh.y;
         xout[k] = x;
-        float2 v = d.f_vel[i];
+        float2 v = d.f_vel[ii];
         v.x += m.x * sh.x + m.z * sh.y;
         v.y += m.y * sh.x + m.w * sh.y;
-        d.f_vel[i] = v;
+        d.f_vel[ii] = v;
         return disp2(x0, x);
     }
 }
@@ -984,21 +987,19 @@ __global__ void __launch_bounds__(kThreads, 2048 / kThreads)
         if (staged) {
             const SrcTile src{s_pos, nullptr, nullptr, nullptr, nullptr, s_base, s_off};
             for (int h = g.home_b + threadIdx.x; h < g.home_e; h += blockDim.x) {
-                const int i = d.lst_f[h];
                 const int c = d.f_celll[h];
                 const Frame fr = tile_frame_c<F>(p, g, c);
                 const float2 gr =
                     shift_particle_listed<F>(p, d, src, h, use_list, F::f_home_l(p, d, fr, h), c, fr);
-                moved2 = max(moved2, shift_update_particle<F>(p, d, i, gr, d.f_xl, d.f_xl_alt, h, last, true));
+                moved2 = max(moved2, shift_update_particle<F>(p, d, -1, h, gr, d.f_xl, d.f_xl_alt, last, true));
             }
         } else {
             // a tile the pair pass could not stage has no lists either
             const SrcListOrder<F> src{&d};
             for (int h = g.home_b + threadIdx.x; h < g.home_e; h += blockDim.x) {
-                const int i = d.lst_f[h];
                 const float2 gr = shift_particle_listed<F>(p, d, src, h, false, F::f_home_l(p, d, Frame{0, 0}, h),
                                                            d.f_celll[h], Frame{0, 0});
-                moved2 = max(moved2, shift_update_particle<F>(p, d, i, gr, d.f_xl, d.f_xl_alt, h, last, true));
+                moved2 = max(moved2, shift_update_particle<F>(p, d, -1, h, gr, d.f_xl, d.f_xl_alt, last, true));
             }
         }
     };
@@ -1048,20 +1049,22 @@ __global__ void __launch_bounds__(kPairBlock) k_shift_gradient_each(const __grid
             if (d.f_listed[i] != stamp) {
                 const float2 gr = shift_particle<F>(p, d, src, F::f_home(p, d, Frame{0, 0}, i), d.f_cell[i],
                                                     Frame{0, 0});
-                moved2 = max(moved2, shift_update_particle<F>(p, d, i, gr, x, d.f_x_alt, i, last, false));
+                moved2 = max(moved2, shift_update_particle<F>(p, d, i, i, gr, x, d.f_x_alt, last, false));
             }
     } else {
         for (int h = blk * blockDim.x + threadIdx.x; h < listed; h += nblk * blockDim.x) {
             const float2 gr = shift_particle<F>(p, d, src, F::f_home_l(p, d, Frame{0, 0}, h), d.f_celll[h],
                                                 Frame{0, 0});
-            moved2 = max(moved2, shift_update_particle<F>(p, d, d.lst_f[h], gr, d.f_xl, d.f_xl_alt, h, last, true));
+            moved2 = max(moved2, shift_update_particle<F>(p, d, -1, h, gr, d.f_xl, d.f_xl_alt, last, true));
         }
     }
     if (pass < kMaskShifts) warp_max_to(moved2, &d.disp2_bits[1 + pass]);
 }
 
 // Before the first shifting pass: the listed particles' positions (f_pos,
-// f_off in the mixed form) and cells into list order.
+// f_off in the mixed form), cells and boundary types into list order (in the
+// mixed form also the offset compensations, and both offset and compensation
+// once more as the start of the total displacement).
 template <class G, class F> __global__ void __launch_bounds__(kBlock) k_shift_gather(const __grid_constant__ G g) {
     SPHNJ_SCENE(g);
     const int h = blk * blockDim.x + threadIdx.x;
@@ -1070,21 +1073,26 @@ template <class G, class F> __global__ void __launch_bounds__(kBlock) k_shift_ga
     const float2 x = (F::kMixed ? d.f_off : d.f_pos)[i];
     d.f_xl[h] = x;
     d.f_celll[h] = __ldg(&d.f_cell[i]);
+    d.f_btl[h] = shift_class(d.f_phase[i], d.f_color[i], d.f_near[i]);
     if constexpr (F::kMixed) {
+        const float2 xc = d.f_offc[i];
+        d.f_offcl[h] = xc;
         d.f_x0l[h] = x;
-        d.f_xc0l[h] = d.f_offc[i];
+        d.f_xc0l[h] = xc;
     }
 }
 
 // After the last one (and the copy back of the unlisted particles after an
-// odd number of passes): the listed particles' positions back to the
-// particle arrays, from the list-order buffer the last pass wrote.
+// odd number of passes): the listed particles' positions (and offset
+// compensations) back to the particle arrays, from the list-order buffers.
 template <class G, class F> __global__ void __launch_bounds__(kBlock) k_shift_scatter(const __grid_constant__ G g) {
     SPHNJ_SCENE(g);
     const int h = blk * blockDim.x + threadIdx.x;
     if (p.shift_per_step <= 0 || h >= *d.f_listed_total) return;
     const float2 *x = (p.shift_per_step & 1) ? d.f_xl_alt : d.f_xl;
-    (F::kMixed ? d.f_off : d.f_pos)[__ldg(&d.lst_f[h])] = x[h];
+    const int i = __ldg(&d.lst_f[h]);
+    (F::kMixed ? d.f_off : d.f_pos)[i] = x[h];
+    if constexpr (F::kMixed) d.f_offc[i] = d.f_offcl[h];
 }
 
 // densityToPressure, fluid.cu:15-23
