@@ -317,6 +317,20 @@ int  sphnj_download(sphnj_ctx *ctx, uint32_t field_mask, sphnj_host_state *s);
 int  sphnj_host_alloc(uint64_t bytes, void **out);
 int  sphnj_host_free(void *ptr);
 
+/* sphnj_upload_fields(in_mask, in), sphnj_step(n) and sphnj_download(out_mask,
+ * out) as one call, with the same results, returning when `out` is written
+ * (in or out may be NULL: no upload or no download).  The host transfers
+ * overlap the steps where the data allow: the fluid velocities, densities
+ * and pressures go up on a second stream while the first step bins its
+ * particles and builds its cell lists (its first stage that reads them
+ * waits), and the last step's densities and pressures come down while its
+ * shifting passes run (nothing after the fluid update changes them).  The
+ * reference copies state to the host inside its loop every step for
+ * getMaxSpeed and the global outputs (fluid.cu:429-440, output.cu:562-582),
+ * with no overlap. */
+int  sphnj_step_exchange(sphnj_ctx *ctx, int n, uint32_t in_mask, const sphnj_host_state *in,
+                         uint32_t out_mask, sphnj_host_state *out);
+
 /* Current step counter i (SimTime::i, sim_time.cpp:27-40). */
 int  sphnj_get_step(const sphnj_ctx *ctx, int *step);
 

@@ -54,6 +54,9 @@ def lib() -> C.CDLL:
         L.sphnj_abi_sizeof.argtypes = [C.c_int]
         L.sphnj_upload_fields.argtypes = [C.c_void_p, C.c_uint32, C.POINTER(abi.HostState)]
         L.sphnj_upload_fields.restype = C.c_int
+        L.sphnj_step_exchange.argtypes = [C.c_void_p, C.c_int, C.c_uint32, C.POINTER(abi.HostState), C.c_uint32,
+                                          C.POINTER(abi.HostState)]
+        L.sphnj_step_exchange.restype = C.c_int
         L.sphnj_profile_stage_count.argtypes = []
         L.sphnj_profile_stage_count.restype = C.c_int
         L.sphnj_profile_stage_name.argtypes = [C.c_int]
@@ -212,6 +215,18 @@ class Simulation:
 
     def step(self, n: int = 1):
         self._check(self._lib.sphnj_step(self._h, int(n)), "step")
+
+    def step_exchange(self, n: int, in_mask: int, arrays_in: dict | None, out_mask: int,
+                      into: dict | None) -> dict | None:
+        """upload_fields(in_mask, arrays_in) + step(n) + download(out_mask,
+        into) as one call (sphnj_step_exchange), with the host transfers
+        overlapped with the steps; returns `into`."""
+        sin = state_struct(arrays_in) if arrays_in is not None else None
+        sout = state_struct(into) if into is not None else None
+        self._check(self._lib.sphnj_step_exchange(self._h, int(n), int(in_mask),
+                                                  C.byref(sin) if sin is not None else None, int(out_mask),
+                                                  C.byref(sout) if sout is not None else None), "step_exchange")
+        return into
 
     def profile_enable(self, on: bool = True):
         self._check(self._lib.sphnj_profile_enable(self._h, 1 if on else 0), "profile_enable")

@@ -401,6 +401,12 @@ void sphnj_destroy(sphnj_ctx *ctx) {
     for (auto &g : ctx->graphs) cudaGraphExecDestroy(g.second.exec);
     if (ctx->arena) cudaFree(ctx->arena);
     if (ctx->h_err) cudaFreeHost(ctx->h_err);
+    if (ctx->io_st) {
+        cudaStreamSynchronize(ctx->io_st);
+        cudaStreamDestroy(ctx->io_st);
+    }
+    for (cudaEvent_t e : {ctx->ev_start, ctx->ev_in, ctx->ev_rho_p, ctx->ev_out})
+        if (e) cudaEventDestroy(e);
     if (ctx->own) cudaStreamDestroy(ctx->own);
     delete ctx;
 }
@@ -496,8 +502,13 @@ int sphnj_upload(sphnj_ctx *ctx, const sphnj_host_state *s) {
 
 namespace sphnj {
 
-template <class G> int issue_step(G &g, const StepKind &k, cudaStream_t st, const TileConfig &tc, Profiler *prof) {
+template <class G>
+int issue_step(G &g, const StepKind &k, cudaStream_t st, const TileConfig &tc, Profiler *prof, const StepIO *io) {
     int launched = 0;
+    // (captured as external event nodes, so one graph serves every call)
+    auto wait_inputs = [&] {
+        if (io && io->in && (k.io & 1)) cudaStreamWaitEvent(st, io->in, cudaEventWaitExternal);
+    };
     auto stage = [&](int s, auto &&fn) {
         Profiler::Rec r{s, 0, nullptr, nullptr};
         if (prof) {
@@ -518,6 +529,7 @@ template <class G> int issue_step(G &g, const StepKind &k, cudaStream_t st, cons
     const bool any_fluid = g.any(fluid), any_solid = g.any(solid);
     stage(ST_BIN, [&] { return launch_bin(st, g, k.bin_virt); });
     if (k.is_sort) {
+        wait_inputs();  // the sort moves every fluid field
         if (any_fluid) stage(ST_SORT, [&] { return launch_sort_kind(st, g, KF, k.parity); });
         if (any_solid) stage(ST_SORT, [&] { return launch_sort_kind(st, g, KS, k.parity); });
         if (k.sort_virt) stage(ST_SORT, [&] { return launch_sort_kind(st, g, KV, k.parity); });
@@ -526,6 +538,7 @@ template <class G> int issue_step(G &g, const StepKind &k, cudaStream_t st, cons
         if (any_solid) stage(ST_REBUILD, [&] { return launch_rebuild_kind(st, g, KS, k.parity); });
     }
     stage(ST_CAPACITY, [&] { return launch_capacity_check(st, g); });
+    if (!k.is_sort) wait_inputs();  // binning and the list rebuild read positions only
     if (g.any([](const sphnj_params &p) { return p.fluid_number_total > 0 && p.solid_number > 0; }))
         stage(ST_SOLID_COUPLE, [&] { return launch_solid_couple(st, g); });
     if (g.any(virt)) stage(ST_VIRT_DATA, [&] { return launch_virt_data(st, g); });
@@ -533,6 +546,7 @@ template <class G> int issue_step(G &g, const StepKind &k, cudaStream_t st, cons
         stage(ST_FLUID_PAIR, [&] { return launch_fluid_pair(st, g, tc); });
         stage(ST_FLUID_UPDATE, [&] { return launch_fluid_update(st, g); });
     }
+    if (io && io->rho_p && (k.io & 2)) cudaEventRecordWithFlags(io->rho_p, st, cudaEventRecordExternal);
     int subs = 0, shifts = 0;
     g.any([&](const sphnj_params &p) {
         if (p.solid_number > 0) subs = std::max(subs, p.solid_sub_step);
@@ -549,8 +563,10 @@ template <class G> int issue_step(G &g, const StepKind &k, cudaStream_t st, cons
     return launched;
 }
 
-template int issue_step<GroupOne>(GroupOne &, const StepKind &, cudaStream_t, const TileConfig &, Profiler *);
-template int issue_step<GroupMany>(GroupMany &, const StepKind &, cudaStream_t, const TileConfig &, Profiler *);
+template int issue_step<GroupOne>(GroupOne &, const StepKind &, cudaStream_t, const TileConfig &, Profiler *,
+                                  const StepIO *);
+template int issue_step<GroupMany>(GroupMany &, const StepKind &, cudaStream_t, const TileConfig &, Profiler *,
+                                   const StepIO *);
 
 StepKind next_kind(const sphnj_ctx *ctx) {
     const sphnj_params &p = ctx->p;
@@ -586,14 +602,17 @@ void drop_graphs(sphnj_ctx *ctx) {
 
 }  // namespace
 
-extern "C" int sphnj_step(sphnj_ctx *ctx, int n) {
-    if (!ctx || n < 0) return SPHNJ_ERR_ARG;
-    if (!ctx->uploaded) return fail(ctx, SPHNJ_ERR_ARG, "sphnj_step before sphnj_upload");
-    if (ctx->batch) return fail(ctx, SPHNJ_ERR_ARG, "the scene is in a batch: step the batch");
-    cudaSetDevice(ctx->device);
+namespace {
+
+// Issues n steps of ctx on its stream (a captured graph per kind of step,
+// unless graphs are off or the stages are being timed); io_first / io_last
+// are the StepKind::io bits of the first and the last step.
+int run_steps(sphnj_ctx *ctx, int n, int io_first = 0, int io_last = 0) {
     cudaStream_t st = ctx->st;
+    const StepIO io{ctx->ev_in, ctx->ev_rho_p};
     for (int it = 0; it < n; ++it) {
-        const StepKind k = next_kind(ctx);
+        StepKind k = next_kind(ctx);
+        k.io = (it == 0 ? io_first : 0) | (it == n - 1 ? io_last : 0);
         GroupOne g{scene_of(ctx, k.parity), ctx->form};
         g.pdl = ctx->pdl;
         if (ctx->use_graphs && !ctx->prof.on) {
@@ -601,7 +620,7 @@ extern "C" int sphnj_step(sphnj_ctx *ctx, int n) {
             if (it_g == ctx->graphs.end()) {
                 cudaGraph_t graph = nullptr;
                 CK(cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal));
-                const int launched = issue_step(g, k, st, ctx->tiles, nullptr);
+                const int launched = issue_step(g, k, st, ctx->tiles, nullptr, &io);
                 cudaError_t e = cudaStreamEndCapture(st, &graph);
                 cudaGraphExec_t exec = nullptr;
                 if (e == cudaSuccess) e = cudaGraphInstantiate(&exec, graph, 0);
@@ -612,12 +631,22 @@ extern "C" int sphnj_step(sphnj_ctx *ctx, int n) {
             CK(cudaGraphLaunch(it_g->second.exec, st));
             ctx->launches += (uint64_t)it_g->second.kernels;
         } else {
-            ctx->launches += (uint64_t)issue_step(g, k, st, ctx->tiles, ctx->prof.on ? &ctx->prof : nullptr);
+            ctx->launches += (uint64_t)issue_step(g, k, st, ctx->tiles, ctx->prof.on ? &ctx->prof : nullptr, &io);
         }
         CK(cudaGetLastError());
         commit_step(ctx, k);
     }
     return SPHNJ_OK;
+}
+
+}  // namespace
+
+extern "C" int sphnj_step(sphnj_ctx *ctx, int n) {
+    if (!ctx || n < 0) return SPHNJ_ERR_ARG;
+    if (!ctx->uploaded) return fail(ctx, SPHNJ_ERR_ARG, "sphnj_step before sphnj_upload");
+    if (ctx->batch) return fail(ctx, SPHNJ_ERR_ARG, "the scene is in a batch: step the batch");
+    cudaSetDevice(ctx->device);
+    return run_steps(ctx, n);
 }
 
 extern "C" {
@@ -640,10 +669,16 @@ int sphnj_set_graphs(sphnj_ctx *ctx, int on) {
     return SPHNJ_OK;
 }
 
-int sphnj_upload_fields(sphnj_ctx *ctx, uint32_t mask, const sphnj_host_state *s) {
-    if (!ctx || !s) return SPHNJ_ERR_ARG;
-    if (!ctx->uploaded) return fail(ctx, SPHNJ_ERR_ARG, "sphnj_upload_fields before sphnj_upload");
-    cudaSetDevice(ctx->device);
+}  // extern "C"
+
+namespace {
+
+// Fields of sphnj_step_exchange's transfers that move on its second stream.
+enum Deferred : uint32_t { DEF_VEL = 1u, DEF_RHO = 2u, DEF_P = 4u };
+
+// sphnj_upload_fields without the final synchronisation; the fluid fields
+// in `defer` are left out (the caller moves them).
+int upload_fields_enqueue(sphnj_ctx *ctx, uint32_t mask, const sphnj_host_state *s, uint32_t defer) {
     const sphnj_params &p = ctx->p;
     const int nf = p.fluid_number_total, ns = p.solid_number, nv = p.virt_number;
     DevState &d = ctx->d;
@@ -653,7 +688,10 @@ int sphnj_upload_fields(sphnj_ctx *ctx, uint32_t mask, const sphnj_host_state *s
     // absolute FP32 position would lose the offset's precision).
     const bool mixed = ctx->form == SPHNJ_FORM_MIXED;
     // fluid fields in device-mapped host memory: one kernel, no copies
-    const FluidHost fh = fluid_host(mask, s, nf);
+    FluidHost fh = fluid_host(mask, s, nf);
+    if (defer & DEF_VEL) fh.vel = nullptr;
+    if (defer & DEF_RHO) fh.rho = nullptr;
+    if (defer & DEF_P) fh.p = nullptr;
     int resplit = 0;
     if (mixed) {
         if ((mask & SPHNJ_F_FLUID_KINEMATICS) && s->fluid_position && !fh.pos) resplit |= 1;
@@ -668,11 +706,11 @@ int sphnj_upload_fields(sphnj_ctx *ctx, uint32_t mask, const sphnj_host_state *s
     launch_fluid_from_host(ctx->st, GroupOne{scene_of(ctx, ctx->parity), ctx->form}, fh);
     if (mask & SPHNJ_F_FLUID_KINEMATICS) {
         if (s->fluid_position && !fh.pos) RET(h2d(ctx, d.f_pos, s->fluid_position, nf));
-        if (s->fluid_velocity && !fh.vel) RET(h2d(ctx, d.f_vel, s->fluid_velocity, nf));
+        if (s->fluid_velocity && !fh.vel && !(defer & DEF_VEL)) RET(h2d(ctx, d.f_vel, s->fluid_velocity, nf));
     }
     if (mask & SPHNJ_F_FLUID_THERMO) {
-        if (s->fluid_density && !fh.rho) RET(h2d(ctx, d.f_rho, s->fluid_density, nf));
-        if (s->fluid_pressure && !fh.p) RET(h2d(ctx, d.f_p, s->fluid_pressure, nf));
+        if (s->fluid_density && !fh.rho && !(defer & DEF_RHO)) RET(h2d(ctx, d.f_rho, s->fluid_density, nf));
+        if (s->fluid_pressure && !fh.p && !(defer & DEF_P)) RET(h2d(ctx, d.f_p, s->fluid_pressure, nf));
         if (s->fluid_phase) RET(enum_h2d(ctx, d.f_phase, s->fluid_phase, nf));
     }
     if (mask & SPHNJ_F_FLUID_FLAGS) {
@@ -715,6 +753,18 @@ int sphnj_upload_fields(sphnj_ctx *ctx, uint32_t mask, const sphnj_host_state *s
     }
     if (resplit) launch_mixed_split(ctx->st, GroupOne{scene_of(ctx, ctx->parity), ctx->form}, resplit);
     CK(cudaGetLastError());
+    return SPHNJ_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+int sphnj_upload_fields(sphnj_ctx *ctx, uint32_t mask, const sphnj_host_state *s) {
+    if (!ctx || !s) return SPHNJ_ERR_ARG;
+    if (!ctx->uploaded) return fail(ctx, SPHNJ_ERR_ARG, "sphnj_upload_fields before sphnj_upload");
+    cudaSetDevice(ctx->device);
+    RET(upload_fields_enqueue(ctx, mask, s, 0u));
     CK(cudaStreamSynchronize(ctx->st));
     return SPHNJ_OK;
 }
@@ -838,14 +888,20 @@ int sphnj_synchronize(sphnj_ctx *ctx) {
     return check_device_error(ctx);
 }
 
-int sphnj_download(sphnj_ctx *ctx, uint32_t mask, sphnj_host_state *s) {
-    if (!ctx || !s) return SPHNJ_ERR_ARG;
-    cudaSetDevice(ctx->device);
+}  // extern "C"
+
+namespace {
+
+// sphnj_download without the final device-error check; the fluid densities
+// and pressures in `defer` are left out (the caller moves them).
+int download_enqueue(sphnj_ctx *ctx, uint32_t mask, sphnj_host_state *s, uint32_t defer) {
     const sphnj_params &p = ctx->p;
     const int nf = p.fluid_number_total, ns = p.solid_number, nv = p.virt_number;
     const DevState &d = ctx->d;
     // fluid fields in device-mapped host memory: one kernel, no copies
-    const FluidHost fh = fluid_host(mask, s, nf);
+    FluidHost fh = fluid_host(mask, s, nf);
+    if (defer & DEF_RHO) fh.rho = nullptr;
+    if (defer & DEF_P) fh.p = nullptr;
     // mixed form: absolute positions and FP64 solid kinematics from the state
     if (ctx->form == SPHNJ_FORM_MIXED)
         launch_mixed_join(ctx->st, GroupOne{scene_of(ctx, ctx->parity), ctx->form},
@@ -857,8 +913,8 @@ int sphnj_download(sphnj_ctx *ctx, uint32_t mask, sphnj_host_state *s) {
         if (!fh.vel) RET(d2h(ctx, s->fluid_velocity, d.f_vel, nf));
     }
     if (mask & SPHNJ_F_FLUID_THERMO) {
-        if (!fh.rho) RET(d2h(ctx, s->fluid_density, d.f_rho, nf));
-        if (!fh.p) RET(d2h(ctx, s->fluid_pressure, d.f_p, nf));
+        if (!fh.rho && !(defer & DEF_RHO)) RET(d2h(ctx, s->fluid_density, d.f_rho, nf));
+        if (!fh.p && !(defer & DEF_P)) RET(d2h(ctx, s->fluid_pressure, d.f_p, nf));
         RET(enum_d2h(ctx, s->fluid_phase, d.f_phase, nf));
     }
     if (mask & SPHNJ_F_FLUID_FLAGS) {
@@ -905,6 +961,72 @@ int sphnj_download(sphnj_ctx *ctx, uint32_t mask, sphnj_host_state *s) {
         RET(d2h(ctx, s->solid_cell_id, d.s_cell, ns));
         RET(d2h(ctx, s->virt_cell_id, d.v_cell, nv));
     }
+    return SPHNJ_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+int sphnj_download(sphnj_ctx *ctx, uint32_t mask, sphnj_host_state *s) {
+    if (!ctx || !s) return SPHNJ_ERR_ARG;
+    cudaSetDevice(ctx->device);
+    RET(download_enqueue(ctx, mask, s, 0u));
+    return check_device_error(ctx);
+}
+
+int sphnj_step_exchange(sphnj_ctx *ctx, int n, uint32_t in_mask, const sphnj_host_state *in, uint32_t out_mask,
+                        sphnj_host_state *out) {
+    if (!ctx || n < 1) return SPHNJ_ERR_ARG;
+    if (!ctx->uploaded) return fail(ctx, SPHNJ_ERR_ARG, "sphnj_step_exchange before sphnj_upload");
+    if (ctx->batch) return fail(ctx, SPHNJ_ERR_ARG, "the scene is in a batch: step the batch");
+    cudaSetDevice(ctx->device);
+    const int nf = ctx->p.fluid_number_total;
+    const DevState &d = ctx->d;
+    if (!ctx->io_st) {
+        if (cudaStreamCreateWithFlags(&ctx->io_st, cudaStreamNonBlocking) != cudaSuccess ||
+            cudaEventCreateWithFlags(&ctx->ev_start, cudaEventDisableTiming) != cudaSuccess ||
+            cudaEventCreateWithFlags(&ctx->ev_in, cudaEventDisableTiming) != cudaSuccess ||
+            cudaEventCreateWithFlags(&ctx->ev_rho_p, cudaEventDisableTiming) != cudaSuccess ||
+            cudaEventCreateWithFlags(&ctx->ev_out, cudaEventDisableTiming) != cudaSuccess)
+            return cuda_fail(ctx, cudaGetLastError(), "step_exchange streams");
+    }
+    cudaStream_t st = ctx->st, io = ctx->io_st;
+    // Fluid velocities, densities and pressures go up on the second stream,
+    // after everything queued so far, while the first step bins and builds
+    // its lists; its first stage that reads them waits (StepKind::io bit 0).
+    uint32_t in_late = 0;
+    if (in && nf > 0) {
+        if ((in_mask & SPHNJ_F_FLUID_KINEMATICS) && in->fluid_velocity) in_late |= DEF_VEL;
+        if ((in_mask & SPHNJ_F_FLUID_THERMO) && in->fluid_density) in_late |= DEF_RHO;
+        if ((in_mask & SPHNJ_F_FLUID_THERMO) && in->fluid_pressure) in_late |= DEF_P;
+    }
+    // The last step's densities and pressures come down on the second stream
+    // during its shifting passes (after the fluid update, StepKind::io bit 1).
+    uint32_t out_late = 0;
+    if (out && nf > 0 && (out_mask & SPHNJ_F_FLUID_THERMO)) {
+        if (out->fluid_density) out_late |= DEF_RHO;
+        if (out->fluid_pressure) out_late |= DEF_P;
+    }
+    const size_t n2 = sizeof(float2) * (size_t)nf, n1 = sizeof(float) * (size_t)nf;
+    if (in_late) {
+        CK(cudaEventRecord(ctx->ev_start, st));
+        CK(cudaStreamWaitEvent(io, ctx->ev_start, 0));
+        if (in_late & DEF_VEL) CK(cudaMemcpyAsync(d.f_vel, in->fluid_velocity, n2, cudaMemcpyHostToDevice, io));
+        if (in_late & DEF_RHO) CK(cudaMemcpyAsync(d.f_rho, in->fluid_density, n1, cudaMemcpyHostToDevice, io));
+        if (in_late & DEF_P) CK(cudaMemcpyAsync(d.f_p, in->fluid_pressure, n1, cudaMemcpyHostToDevice, io));
+        CK(cudaEventRecord(ctx->ev_in, io));
+    }
+    if (in) RET(upload_fields_enqueue(ctx, in_mask, in, in_late));
+    RET(run_steps(ctx, n, in_late ? 1 : 0, out_late ? 2 : 0));
+    if (out_late) {
+        CK(cudaStreamWaitEvent(io, ctx->ev_rho_p, 0));
+        if (out_late & DEF_RHO) CK(cudaMemcpyAsync(out->fluid_density, d.f_rho, n1, cudaMemcpyDeviceToHost, io));
+        if (out_late & DEF_P) CK(cudaMemcpyAsync(out->fluid_pressure, d.f_p, n1, cudaMemcpyDeviceToHost, io));
+        CK(cudaEventRecord(ctx->ev_out, io));
+    }
+    if (out) RET(download_enqueue(ctx, out_mask, out, out_late));
+    if (out_late) CK(cudaStreamWaitEvent(st, ctx->ev_out, 0));
     return check_device_error(ctx);
 }
 

@@ -44,13 +44,26 @@ struct StepGraph {
 struct StepKind {
     bool is_sort, bin_virt, sort_virt;
     int parity;  // list buffer that this step writes and reads
-    int key() const { return (is_sort ? 1 : 0) | (bin_virt ? 2 : 0) | (sort_virt ? 4 : 0) | (parity << 3); }
+    // host transfers overlapping the step (sphnj_step_exchange): bit 0, wait
+    // for StepIO::in before the first stage that reads fluid velocities,
+    // densities or pressures; bit 1, record StepIO::rho_p after the fluid
+    // update, which writes the step's last densities and pressures
+    int io = 0;
+    int key() const {
+        return (is_sort ? 1 : 0) | (bin_virt ? 2 : 0) | (sort_virt ? 4 : 0) | (parity << 3) | (io << 4);
+    }
+};
+struct StepIO {
+    cudaEvent_t in = nullptr, rho_p = nullptr;
 };
 
 // Issues the launches of one step of every scene of g on stream st; returns
 // the number of kernels launched.  Reads no host state that changes from
-// step to step except through `k`, so the sequence can be captured.
-template <class G> int issue_step(G &g, const StepKind &k, cudaStream_t st, const TileConfig &tc, Profiler *prof);
+// step to step except through `k`, so the sequence can be captured (with
+// the events of `io` as external event nodes).
+template <class G>
+int issue_step(G &g, const StepKind &k, cudaStream_t st, const TileConfig &tc, Profiler *prof,
+               const StepIO *io = nullptr);
 
 }  // namespace sphnj
 
@@ -61,6 +74,10 @@ struct sphnj_ctx {
     int form = SPHNJ_FORM_PLAIN;
     int device = 0;
     cudaStream_t own = nullptr, st = nullptr;
+    // sphnj_step_exchange: the stream of its overlapped transfers and their
+    // events (created on first use)
+    cudaStream_t io_st = nullptr;
+    cudaEvent_t ev_start = nullptr, ev_in = nullptr, ev_rho_p = nullptr, ev_out = nullptr;
     char *arena = nullptr;
     size_t arena_bytes = 0;
     sphnj::DevState d{};

@@ -107,3 +107,64 @@ def test_misaligned_arrays_take_the_copy_path():
         # one split and one join: within an FP32 rounding of the input
         np.testing.assert_allclose(back["fluid_position"], pos, rtol=0, atol=2e-6)
 
+
+
+@pytest.mark.parametrize("form", [abi.FORM_PLAIN, abi.FORM_MIXED])
+@pytest.mark.parametrize("mapped", [False, True])
+def test_step_exchange_equals_separate_calls(form, mapped):
+    """sphnj_step_exchange (upload, n steps, download in one call, its
+    transfers overlapped with the steps) gives exactly what the three calls
+    give, through a sort step, round-tripping the state through the host."""
+    p, arr = case()
+    runs = []
+    for exchange in (False, True):
+        with S.Simulation(p, form) as sim:
+            sim.upload(arr)
+            sim.step(3)
+            hin = sim.host_state(IO) if mapped else S.alloc_state(p, IO)
+            hout = sim.host_state(IO) if mapped else S.alloc_state(p, IO)
+            sim.download(MASK, into=hin)
+            seq = []
+            for it in range(4):  # steps 4..63: the sort step 51 inside
+                hin["fluid_velocity"] *= np.float32(0.999)
+                hin["fluid_pressure"] += np.float32(0.5)
+                if exchange:
+                    sim.step_exchange(15, MASK, hin, MASK, hout)
+                else:
+                    sim.upload_fields(MASK, hin)
+                    sim.step(15)
+                    sim.download(MASK, into=hout)
+                seq.append({k: v.copy() for k, v in hout.items()})
+                hin, hout = hout, hin
+            runs.append((seq, sim.download(), sim.step_index))
+    (sa, fa, ia), (sb, fb, ib) = runs
+    assert ia == ib == 63
+    for a, b in zip(sa, sb):
+        same(a, b)
+    same(fa, fb)
+
+
+@pytest.mark.parametrize("form", [abi.FORM_PLAIN, abi.FORM_MIXED])
+def test_step_exchange_one_way(form):
+    """Upload only, download only, and a velocity-only upload (the mixed
+    form's compensation reset) through sphnj_step_exchange."""
+    p, arr = case()
+    runs = []
+    for exchange in (False, True):
+        with S.Simulation(p, form) as sim:
+            sim.upload(arr)
+            sim.step(2)
+            v = sim.download(abi.F_FLUID_KINEMATICS, into=S.alloc_state(p, ("fluid_velocity",)))
+            v["fluid_velocity"] *= np.float32(1.01)
+            got = S.alloc_state(p, ("fluid_density", "fluid_pressure"))
+            if exchange:
+                sim.step_exchange(4, abi.F_FLUID_KINEMATICS, v, 0, None)
+                sim.step_exchange(3, 0, None, abi.F_FLUID_THERMO, got)
+            else:
+                sim.upload_fields(abi.F_FLUID_KINEMATICS, v)
+                sim.step(4)
+                sim.step(3)
+                sim.download(abi.F_FLUID_THERMO, into=got)
+            runs.append((got, sim.download()))
+    same(runs[0][0], runs[1][0])
+    same(runs[0][1], runs[1][1])
