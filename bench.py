@@ -463,9 +463,13 @@ def run_ours(args):
                 "traffic_source": "ncu dram bytes of one launch at 2.08M particles, scaled by particle count",
                 "peak_source": "MEASURED_PEAKS.json hbm_gbs (measured)" if peaks else "fallback 6.8 TB/s",
                 "bytes_per_launch": bpl, "avg_launch_ms": avg_ms,
-                "issue_slots_busy": (dict(byte_model.ISSUE_ACTIVE_MIXED,
-                                          source="ncu smsp__issue_active of one launch at 2.08M particles")
-                                     if mixed else None),
+                # the DRAM bytes ncu measured for such a launch over the same
+                # CUDA-event time: the rate the kernel actually draws
+                "dram_gbs": (byte_model.measured_traffic_per_launch(dom, nf, mixed) / (avg_ms / 1e3) / 1e9
+                             if byte_model.measured_traffic_per_launch(dom, nf, mixed) and args.tile_h == 16
+                             and not args.untiled else None),
+                "issue_slots_busy": dict(byte_model.ISSUE_ACTIVE_MIXED if mixed else byte_model.ISSUE_ACTIVE,
+                                         source="ncu smsp__issue_active of one launch at 2.08M particles"),
                 "stage_share": {k: round(v[0] / total_ms, 4) for k, v in prof.items() if v[1]}}
     step_bytes = byte_model.step_bytes(nf, ns, nv, p.shift_per_step, p.solid_sub_step, mixed)
 

@@ -113,23 +113,24 @@ def bytes_per_step(nf: int, ns: int, nv: int, shifts: int, substeps: int) -> flo
 
 # DRAM traffic (dram__bytes_read.sum + dram__bytes_write.sum) per fluid
 # particle of one launch of the tiled neighbour sweeps, from one ncu capture of
-# the 2,083,750-particle gas-liquid dam break (plain form, tiles of 16 cells,
-# stored neighbour lists, fused shifting pass, 128-thread blocks); it grows in proportion to the
-# particle count (same tile shape, same list length per particle).  Well above
-# the compulsory bytes above: the pair pass writes the per-step neighbour lists
-# and every shifting pass reads them back.
+# the 2,083,750-particle gas-liquid dam break per form (tiles of 16 cells,
+# stored neighbour lists, 128-thread blocks; the shifting launch is a pass
+# before the step's last); it grows in proportion to the particle count (same
+# tile shape, same list length per particle).  Well above the compulsory
+# bytes above: the pair pass writes the per-step neighbour lists and every
+# shifting pass reads them back (about 96 B per particle).
 MEASURED_TRAFFIC_PER_PARTICLE = {
-    "fluid_pair": 149.0,
-    "shift_pass": 157.4,
+    "fluid_pair": 148.9,
+    "shift_pass": 154.1,
 }
-# the mixed form (the capture of the current build, packed FP32 pair arithmetic)
 MEASURED_TRAFFIC_PER_PARTICLE_MIXED = {
     "fluid_pair": 148.1,
-    "shift_pass": 186.2,
+    "shift_pass": 130.6,
 }
 # issue slots busy (smsp__issue_active, % of peak) of the same captures: the
 # neighbour sweeps are bound by instruction issue and latency, not by DRAM
-ISSUE_ACTIVE_MIXED = {"fluid_pair": 0.660, "shift_pass": 0.541}
+ISSUE_ACTIVE = {"fluid_pair": 0.749, "shift_pass": 0.762}
+ISSUE_ACTIVE_MIXED = {"fluid_pair": 0.660, "shift_pass": 0.665}
 
 
 def measured_traffic_per_launch(stage: str, nf: int, mixed: bool = False) -> float | None:
