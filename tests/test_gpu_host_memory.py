@@ -168,3 +168,27 @@ def test_step_exchange_one_way(form):
             runs.append((got, sim.download()))
     same(runs[0][0], runs[1][0])
     same(runs[0][1], runs[1][1])
+
+
+@pytest.mark.parametrize("form", [abi.FORM_PLAIN, abi.FORM_MIXED])
+def test_step_exchange_without_graphs_and_while_profiling(form):
+    """The exchange's event waits and records also order direct launches
+    (graphs off) and the timed stages of profiling."""
+    p, arr = case()
+    runs = []
+    for mode in ("graphs", "direct", "profiled"):
+        with S.Simulation(p, form) as sim:
+            if mode == "direct":
+                sim.set_graphs(False)
+            if mode == "profiled":
+                sim.profile_enable(True)
+            sim.upload(arr)
+            sim.step(2)
+            h = sim.host_state(IO)
+            sim.download(MASK, into=h)
+            for _ in range(3):
+                h["fluid_pressure"] *= np.float32(1.001)
+                sim.step_exchange(20, MASK, h, MASK, h)
+            runs.append(sim.download())
+    same(runs[0], runs[1])
+    same(runs[0], runs[2])
