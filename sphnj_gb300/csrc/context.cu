@@ -505,9 +505,14 @@ namespace sphnj {
 template <class G>
 int issue_step(G &g, const StepKind &k, cudaStream_t st, const TileConfig &tc, Profiler *prof, const StepIO *io) {
     int launched = 0;
-    // (captured as external event nodes, so one graph serves every call)
+    // Under stream capture the event operations become external event nodes,
+    // so that one graph serves every call; direct launches use them as they are.
+    cudaStreamCaptureStatus cap = cudaStreamCaptureStatusNone;
+    if (io && k.io) cudaStreamIsCapturing(st, &cap);
+    const bool capturing = cap == cudaStreamCaptureStatusActive;
     auto wait_inputs = [&] {
-        if (io && io->in && (k.io & 1)) cudaStreamWaitEvent(st, io->in, cudaEventWaitExternal);
+        if (io && io->in && (k.io & 1))
+            cudaStreamWaitEvent(st, io->in, capturing ? cudaEventWaitExternal : cudaEventWaitDefault);
     };
     auto stage = [&](int s, auto &&fn) {
         Profiler::Rec r{s, 0, nullptr, nullptr};
@@ -546,7 +551,8 @@ int issue_step(G &g, const StepKind &k, cudaStream_t st, const TileConfig &tc, P
         stage(ST_FLUID_PAIR, [&] { return launch_fluid_pair(st, g, tc); });
         stage(ST_FLUID_UPDATE, [&] { return launch_fluid_update(st, g); });
     }
-    if (io && io->rho_p && (k.io & 2)) cudaEventRecordWithFlags(io->rho_p, st, cudaEventRecordExternal);
+    if (io && io->rho_p && (k.io & 2))
+        cudaEventRecordWithFlags(io->rho_p, st, capturing ? cudaEventRecordExternal : cudaEventRecordDefault);
     int subs = 0, shifts = 0;
     g.any([&](const sphnj_params &p) {
         if (p.solid_number > 0) subs = std::max(subs, p.solid_sub_step);

@@ -242,7 +242,8 @@ __device__ __forceinline__ void riemann(float2 u_i, float2 u_j, float p_i, float
         const float z = sqn(dx);
         const float iz = rsqrt_approx(z);
         n = z > 0.0f ? mul2x(dx, splat2(iz)) : dx;
-        const float du = dot2(sub2x(u_i, u_j), n);
+        const float2 uij = sub2x(u_i, u_j);
+        const float du = dot2(uij, n);
         if (du >= 0.0f)
             ps = __fadd_rn(ps, __fmul_rn(__fmul_rn(__fmul_rn(__fmul_rn(rho_i, rho_j), du), irs),
                                          fminf(__fmul_rn(3.0f, du), cs)));
@@ -251,14 +252,15 @@ __device__ __forceinline__ void riemann(float2 u_i, float2 u_j, float p_i, float
         vs = mul2x(fma2x(splat2(rho_j), u_j, mul2x(splat2(rho_i), u_i)), splat2(irs));
         t = __fmul_rn(__fmul_rn(__fsub_rn(p_i, p_j), irs), rcp_approx(cs));
         vs = fma2x(splat2(t), n, vs);
-        am = __fmul_rn(__fmul_rn(-2.0f, ps), rcp_approx(rho_i));
+        am = __fmul_rn(ps, __fmul_rn(-2.0f, rcp_approx(rho_i)));  // = (-2 ps) / rho_i, one rounding
         // the sums, each product rounded and then one fused add, as mad_to:
         // in pairs of components (packed FP32)
         a.du_dt = fma2x(mul2x(splat2(am), dx), splat2(kc), a.du_dt);
         a.velo_div = __fmaf_rn(__fmul_rn(__fmul_rn(2.0f, rho_i), dot2(sub2x(u_i, vs), dx)), kc, a.velo_div);
-        const float2 w = sub2x(u_j, u_i);
-        const float2 c0 = fma2x(mul2x(w, splat2(dx.x)), splat2(kc), make_float2(a.du_dx.x, a.du_dx.y));
-        const float2 c1 = fma2x(mul2x(w, splat2(dx.y)), splat2(kc), make_float2(a.du_dx.z, a.du_dx.w));
+        // (u_j - u_i) dx kc as (u_i - u_j) dx (-kc): the same value (a zero
+        // difference may give the other zero sign)
+        const float2 c0 = fma2x(mul2x(uij, splat2(dx.x)), splat2(-kc), make_float2(a.du_dx.x, a.du_dx.y));
+        const float2 c1 = fma2x(mul2x(uij, splat2(dx.y)), splat2(-kc), make_float2(a.du_dx.z, a.du_dx.w));
         a.du_dx = make_float4(c0.x, c0.y, c1.x, c1.y);
         return;
     } else {
