@@ -192,3 +192,17 @@ def test_step_exchange_without_graphs_and_while_profiling(form):
             runs.append(sim.download())
     same(runs[0], runs[1])
     same(runs[0], runs[2])
+
+
+def test_step_exchange_refuses_a_batched_scene():
+    loaded = [load(cases.sweep_scene(s)) for s in (3, 9)]
+    sims = [S.Simulation(p, abi.FORM_MIXED) for p, _ in loaded]
+    try:
+        for sim, (_, arr) in zip(sims, loaded):
+            sim.upload(arr)
+        with S.Batch(sims):
+            with pytest.raises(S.SphnjError):
+                sims[0].step_exchange(1, 0, None, 0, None)
+    finally:
+        for sim in sims:
+            sim.close()
