@@ -39,8 +39,8 @@ struct TileConfig {
 // Launch sites: a batch keeps one block table per (site, argument).
 enum Site : int {
     SITE_BIN, SITE_SORT_CLEAR, SITE_SORT_N, SITE_SORT_TILES, SITE_SORT_ONE, SITE_SORT_CELLS32,
-    SITE_REBUILD_CELLS, SITE_REBUILD_TILES, SITE_REBUILD_ONE, SITE_CAPACITY, SITE_COUPLE, SITE_VIRT_NORMAL,
-    SITE_VIRT_DATA, SITE_PAIR_TILED, SITE_PAIR_EACH, SITE_PAIR_FALLBACK, SITE_FLUID_UPDATE, SITE_SOLID_DEFORM,
+    SITE_REBUILD_CELLS, SITE_REBUILD_TILES, SITE_REBUILD_ONE, SITE_REBUILD_ZERO, SITE_CAPACITY, SITE_COUPLE,
+    SITE_VIRT_NORMAL, SITE_VIRT_DATA, SITE_PAIR_TILED, SITE_PAIR_EACH, SITE_PAIR_FALLBACK, SITE_FLUID_UPDATE, SITE_SOLID_DEFORM,
     SITE_SOLID_FORCE, SITE_SOLID_UPDATE, SITE_SHIFT_TILED, SITE_SHIFT_EACH, SITE_SHIFT_FALLBACK,
     SITE_SHIFT_COPY_BACK, SITE_TILE_COMPACT, SITE_TILE_SUMS, SITE_TILE_SCATTER, SITE_VIRT_BIN, SITE_SHIFT_GATHER,
     SITE_SHIFT_SCATTER

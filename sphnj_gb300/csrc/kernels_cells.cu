@@ -22,9 +22,9 @@
 //   - sort = histogram + two-level scan + atomic bucket fill + a warp rank
 //     sort inside each cell (indices are unique, so rank = number of smaller
 //     indices); stable by construction, no radix passes, no library calls.
-//   - rebuild = each old cell m scatters its 9 outgoing counts to
-//     cnt9[c][slot] (every (c,slot) pair has exactly one writer, so no
-//     atomics and no zeroing), a tiled scan gives the new cell starts, and
+//   - rebuild = each old cell m scatters its non-zero outgoing counts to
+//     cnt9[c][slot], zeroed first (every (c,slot) pair has at most one
+//     writer, so no atomics), a tiled scan gives the new cell starts, and
 //     m writes its particles to their destinations in previous-list order.
 //   - every kernel runs over one scene or a batch of scenes (SPHNJ_SCENE):
 //     each scene's scan, sort and rebuild use that scene's own scratch, so
@@ -556,6 +556,18 @@ __device__ __forceinline__ int slot_from(int mi, int mj, int c, int ny) {
     return 3 * (di + 1) + (dj + 1);
 }
 
+// The per-(cell, slot) counts start at zero, so that k_rebuild_count writes
+// only the non-zero ones: most cells of a sparse scene are empty, and a
+// particle that stays in its cell leaves its cell's eight other slots at
+// zero.  A count kernel that wrote all nine (each to another cell's row)
+// spent most of its time on those scattered stores of zeros.
+template <class G> __global__ void __launch_bounds__(kBlock) k_zero_cnt9(const __grid_constant__ G g) {
+    SPHNJ_SCENE(g);
+    const long n = 9L * p.cell_number_total;
+    int *cnt9 = S.sc.cnt9;
+    for (long t = (long)blk * blockDim.x + threadIdx.x; t < n; t += (long)nblk * blockDim.x) cnt9[t] = 0;
+}
+
 template <class G> __global__ void k_rebuild_count(const __grid_constant__ G g, int k, int parity) {
     SPHNJ_SCENE(g);
     const int C = p.cell_number_total, nx = p.cell_number[0], ny = p.cell_number[1];
@@ -577,7 +589,7 @@ template <class G> __global__ void k_rebuild_count(const __grid_constant__ G g, 
 #pragma unroll
     for (int s = 0; s < 9; ++s) {
         int ci = mi - (s / 3 - 1), cj = mj - (s % 3 - 1);
-        if (ci >= 0 && ci < nx && cj >= 0 && cj < ny) cnt9[(long)(ci * ny + cj) * 9 + s] = run[s];
+        if (run[s] && ci >= 0 && ci < nx && cj >= 0 && cj < ny) cnt9[(long)(ci * ny + cj) * 9 + s] = run[s];
     }
 }
 
@@ -592,6 +604,8 @@ template <class G> __global__ void k_rebuild_write(const __grid_constant__ G g, 
     int *listed = k == KF ? d.f_listed : nullptr;
     const int mi = m / ny, mj = m - mi * ny;
     cur.rng[m].x = cell_start(sc.local, sc.sums, m);
+    const int2 r = prev.rng[m];
+    if (r.y == 0) return;  // no particle of cell m to place
     int base[9];
 #pragma unroll
     for (int s = 0; s < 9; ++s) {
@@ -606,7 +620,6 @@ template <class G> __global__ void k_rebuild_write(const __grid_constant__ G g, 
         base[s] = b;
     }
     const int stamp = listed ? *d.stamp : 0;
-    const int2 r = prev.rng[m];
     for (int q = r.x; q < r.x + r.y; ++q) {
         int pidx = __ldg(&prev.lst[q]);
         int s = slot_from(mi, mj, __ldg(&cell[pidx]), ny);
@@ -711,8 +724,11 @@ template <class G> int launch_rebuild_kind(cudaStream_t st, G &g, Kind k, int pa
     auto cells = [&](const Scene &s) { return has(s) ? grid_for(s.p.cell_number_total, kBlock) : 0u; };
     auto tiles = [&](const Scene &s) { return has(s) ? grid_for(s.p.cell_number_total, SCAN_TILE) : 0u; };
     auto one = [&](const Scene &s) { return has(s) ? 1u : 0u; };
+    // zeroing: eight counts a thread (the scene's 9 per cell)
+    auto zero = [&](const Scene &s) { return has(s) ? grid_for(9L * s.p.cell_number_total, 8 * kBlock) : 0u; };
     const int ki = (int)k;
     int n = 0;
+    n += launch(g, site_key(SITE_REBUILD_ZERO, ki), zero, k_zero_cnt9<D>, kBlock, 0, st);
     n += launch(g, site_key(SITE_REBUILD_CELLS, ki), cells, k_rebuild_count<D>, kBlock, 0, st, ki, parity);
     n += launch(g, site_key(SITE_REBUILD_TILES, ki), tiles, k_scan_tile<D, true>, kBlock, 0, st, ki, parity);
     n += launch(g, site_key(SITE_REBUILD_ONE, ki), one, k_scan_sums<D>, 1024, 0, st, k == KF ? 1 : 0, 0);
