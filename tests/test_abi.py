@@ -61,3 +61,23 @@ def test_host_free_refuses_memory_it_did_not_allocate():
     x = np.zeros(16, np.float32)
     assert lib.sphnj_host_free(C.c_void_p(x.ctypes.data)) == abi.ERR_ARG
     assert lib.sphnj_host_free(None) == 0
+
+
+def test_host_alloc_without_a_gpu_fails_cleanly():
+    """With no device, pinned allocation reports an error instead of
+    returning memory, and the numpy state falls back to ordinary arrays."""
+    import numpy as np
+    import torch
+
+    if torch.cuda.is_available():
+        import pytest
+
+        pytest.skip("a GPU is present")
+    lib = S.lib()
+    ptr = C.c_void_p()
+    assert lib.sphnj_host_alloc(1024, C.byref(ptr)) != 0
+    assert not ptr.value
+    p = abi.Params()
+    p.fluid_number_total = 4
+    st = abi.alloc_state(p, ("fluid_position",))
+    assert isinstance(st["fluid_position"], np.ndarray) and st["fluid_position"].shape == (4, 2)
