@@ -283,6 +283,8 @@ struct Scene {
     int tile_h, lists, pad_[4];
 };
 
+__device__ __forceinline__ void pdl_enter();
+
 // Where a block finds its scene.  Every kernel of the step is a template over
 // one of the two, and starts with SPHNJ_SCENE(g), which defines
 //   blk, nblk  the block's index among its scene's blocks, and their number
@@ -296,6 +298,16 @@ struct One {
         blk = blockIdx.x;
         nblk = gridDim.x;
         return &s;
+    }
+    // a block of a sweep over the scene's active-tile list: waits for the
+    // launch's predecessor (pdl_enter), then reads the list's length; null
+    // when the block has no tile of it
+    __device__ __forceinline__ const Scene *locate_listed(int &blk, int &nblk, int &n_active) const {
+        blk = blockIdx.x;
+        nblk = gridDim.x;
+        pdl_enter();
+        n_active = *s.d.tile_count;
+        return blk < n_active ? &s : nullptr;
     }
 };
 
@@ -323,6 +335,25 @@ struct Many {
         __syncthreads();
         return &s_scene;
     }
+    // As One::locate_listed.  A batched list launch has more blocks than its
+    // scenes have active tiles; a block without a tile reads only its
+    // scene's list length (two dependent loads) and returns before copying
+    // the record.
+    __device__ __forceinline__ const Scene *locate_listed(int &blk, int &nblk, int &n_active) const {
+        const int4 t = __ldg(&blocks[blockIdx.x]);
+        blk = t.y;
+        nblk = t.z;
+        pdl_enter();
+        const int *count = scenes[t.x].d.tile_count;
+        n_active = *count;
+        if (blk >= n_active) return nullptr;
+        __shared__ __align__(16) Scene s_scene;
+        const int4 *src = reinterpret_cast<const int4 *>(scenes + t.x);
+        int4 *dst = reinterpret_cast<int4 *>(&s_scene);
+        for (int w = threadIdx.x; w < (int)(sizeof(Scene) / 16); w += blockDim.x) dst[w] = __ldg(&src[w]);
+        __syncthreads();
+        return &s_scene;
+    }
 };
 
 // Programmatic dependent launch: every kernel of a step is launched with
@@ -337,6 +368,30 @@ __device__ __forceinline__ void pdl_enter() {
     asm volatile("griddepcontrol.wait;" ::: "memory");
     asm volatile("griddepcontrol.launch_dependents;" ::: "memory");
 }
+
+// The neighbour sweeps: with kList (blocks loop over the scene's active-tile
+// list) the block reads the list's length first and, when it has no tile of
+// it, returns before loading anything else (locate_listed).
+template <bool kList, class G>
+__device__ __forceinline__ const Scene *locate_sweep(const G &g, int &blk, int &nblk, int &n_active) {
+    if constexpr (kList) {
+        return g.locate_listed(blk, nblk, n_active);
+    } else {
+        const Scene *s = g.locate(blk, nblk);
+        pdl_enter();
+        return s;
+    }
+}
+#define SPHNJ_SCENE_SWEEP(g, kList, n_active)                                          \
+    int blk, nblk;                                                                    \
+    const ::sphnj::Scene *S_ptr_ = ::sphnj::locate_sweep<kList>(g, blk, nblk, n_active); \
+    if (!S_ptr_) return;                                                              \
+    const ::sphnj::Scene &S = *S_ptr_;                                                \
+    const sphnj_params &p = S.p;                                                      \
+    const ::sphnj::DevState &d = S.d;                                                 \
+    (void)nblk;                                                                       \
+    (void)p;                                                                          \
+    (void)d
 
 #define SPHNJ_SCENE(g)                                   \
     int blk, nblk;                                       \

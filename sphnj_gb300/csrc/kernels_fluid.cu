@@ -898,7 +898,8 @@ __device__ __forceinline__ Frame tile_frame_c(const sphnj_params &p, const TileG
 template <class G, class F, bool kList, int kThreads, int kMinBlocks>
 __global__ void __launch_bounds__(kThreads, kMinBlocks)
     k_fluid_pair_tiled(const __grid_constant__ G gs, int cap) {
-    SPHNJ_SCENE(gs);
+    int n_active = 0;
+    SPHNJ_SCENE_SWEEP(gs, kList, n_active);
     const int tile_h = S.tile_h, use_lists = S.lists;
     extern __shared__ __align__(16) unsigned char smem[];
     __shared__ int s_base[3], s_off[3];
@@ -936,7 +937,6 @@ __global__ void __launch_bounds__(kThreads, kMinBlocks)
         }
     };
     if constexpr (kList) {
-        const int n_active = *d.tile_count;
         for (int a = blk; a < n_active; a += nblk) {
             sweep(__ldg(&d.tile_list[a]));
             __syncthreads();  // the next tile overwrites the staged entries
@@ -957,7 +957,8 @@ __global__ void __launch_bounds__(kThreads, kMinBlocks)
 template <class G, class F, bool kList, int kThreads>
 __global__ void __launch_bounds__(kThreads, 2048 / kThreads)
     k_shift_gradient_tiled(const __grid_constant__ G gs, int cap, int pass) {
-    SPHNJ_SCENE(gs);
+    int n_active = 0;
+    SPHNJ_SCENE_SWEEP(gs, kList, n_active);
     const int tile_h = S.tile_h;
     const bool last = pass + 1 >= p.shift_per_step;
     extern __shared__ __align__(16) unsigned char smem[];
@@ -1006,7 +1007,6 @@ __global__ void __launch_bounds__(kThreads, 2048 / kThreads)
         }
     };
     if constexpr (kList) {
-        const int n_active = *d.tile_count;
         for (int a = blk; a < n_active; a += nblk) {
             sweep(__ldg(&d.tile_list[a]));
             __syncthreads();  // the next tile overwrites the staged entries
