@@ -31,6 +31,7 @@ from __future__ import annotations
 
 PER_PARTICLE = {
     "bin": 12,
+    "bin_solid": 20,  # FP64 position 16 + cell id 4
     "rebuild": 15,
     "sort": 2 * 50,  # per sort call (the amortised 2 B/step of the model, over 50 steps)
     "fluid_pair": 67,
@@ -47,7 +48,7 @@ PER_PARTICLE = {
 
 # which particle count a stage's bytes scale with
 STAGE_KIND = {
-    "bin": "all", "rebuild": "fluid", "sort": "fluid", "fluid_pair": "fluid", "fluid_update": "fluid",
+    "bin": "all", "bin_solid": "solid", "rebuild": "fluid", "sort": "fluid", "fluid_pair": "fluid", "fluid_update": "fluid",
     "shift_pass": "fluid", "shift_last": "fluid", "shift_copy_back": "fluid", "virt_data": "virt", "solid_couple": "solid",
     "solid_deformation": "solid", "solid_force": "solid", "solid_update": "solid", "capacity": "none",
 }
@@ -72,7 +73,7 @@ STAGE_KIND = {
 #                        P L, F L 32 = 160; force 8 + 8 + 8 + 16 + 16 + 4 + 1 read, 16 write = 77;
 #                        update 8 + 8 + 8 + 8 + 8 + 1 + 8 read (+ reference cell / offset 16 for the
 #                        current offset), 8 x 5 write = 105
-PER_PARTICLE_MIXED = dict(PER_PARTICLE, bin=20, fluid_pair=71, fluid_update=89, shift_pass=42, shift_last=73,
+PER_PARTICLE_MIXED = dict(PER_PARTICLE, bin=20, bin_solid=20, fluid_pair=71, fluid_update=89, shift_pass=42, shift_last=73,
                           solid_deformation=160, solid_force=77, solid_update=105)
 
 
@@ -95,7 +96,7 @@ def step_bytes(nf: int, ns: int, nv: int, shifts: int, substeps: int, mixed: boo
     virtual particles' data, and for solids the coupling pass (with fluid) and
     k sub-steps of deformation, force and update."""
     t = PER_PARTICLE_MIXED if mixed else PER_PARTICLE
-    b = (nf + ns + nv) * t["bin"]
+    b = (nf + nv) * t["bin"] + ns * t["bin_solid"]
     if nf:
         b += nf * (t["rebuild"] + t["sort"] / 50 + t["fluid_pair"] + t["fluid_update"] + shifts * t["shift_pass"]
                    + (shifts > 0) * t["shift_last"] + (shifts & 1) * t["shift_copy_back"])
