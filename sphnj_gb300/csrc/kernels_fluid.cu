@@ -26,7 +26,8 @@
 // stencil in the reference's order, reading fluid neighbours from shared
 // memory (solid and virtual neighbours, rare, from global memory), so the
 // per-particle sums are the same sums in the same order as the per-particle
-// form.  Particles that are in no cell list (moved more than one cell since
+// form.  The shifting passes also stage the tile's virtual strips, so that a
+// particle next to a wall walks a stored list like any other.  Particles that are in no cell list (moved more than one cell since
 // the last sort) are handled by per-particle fallback kernels, which return
 // at once when every particle is listed.
 //
@@ -362,13 +363,83 @@ __device__ __forceinline__ void store_pair(const DevState &d, int i, const FAcc 
     d.f_dudx[i] = a.du_dx;
 }
 
-// findFluidPair for particle i (fluid.cu:193-254), in frame fr
-template <class F, class Src>
+// ---- tile geometry ---------------------------------------------------------
+// Block b owns home cells (ci, cj0 .. cj1-1) of one column.  Its fluid
+// neighbours are the cells (ci-1..ci+1, cj0-1..cj1): per column one
+// contiguous CSR range ("strip"), and so are its virtual neighbours.  The
+// staged entries of a tile are its fluid strips at slots 0 .. total-1 and,
+// in the shifting passes, its virtual strips after them (slots total ..
+// total + total_v - 1) when both fit (virt_staged).
+struct TileGeom {
+    int home_b, home_e, total, total_v;
+    int col, row0;  // the tile's column and first row (its frame origin in the mixed form)
+};
+
+// Per column strip s: first CSR position and first slot, of the fluid
+// (base, off) and of the virtual entries (vbase, voff); in shared memory.
+struct TileStrips {
+    int base[3], off[3], vbase[3], voff[3];
+};
+
+// Whether a tile's virtual strips are staged (after its fluid strips) in a
+// staging area of cap entries.  The pair pass stores virtual slots in the
+// neighbour lists of the tile's particles exactly when the shifting passes,
+// which see the same cell lists and the same cap, stage them.
+__device__ __forceinline__ bool virt_staged(const TileGeom &g, int cap) { return g.total + g.total_v <= cap; }
+
+__device__ __forceinline__ float list_radius2(const sphnj_params &p) {
+    return p.impact_distance_square * ((1.0f + kSkin) * (1.0f + kSkin));
+}
+
+// Writes one particle's list: 16-bit entries (byte offset 8 t of tile slot
+// t < 8192), in chunks of eight at col[c nf], through an 8-entry FIFO in four
+// registers - each push shifts the 128-bit value down by 16 bits and inserts
+// at the top, so after 8 pushes the first entry is in the low half of b0 and
+// the full chunk goes out as one 16-byte store.
+struct ListWriter {
+    uint4 *col;
+    size_t nf;
+    unsigned b0 = 0u, b1 = 0u, b2 = 0u, b3 = 0u;
+    int n = 0;
+    __device__ __forceinline__ ListWriter(uint4 *c, size_t stride) : col(c), nf(stride) {}
+    __device__ __forceinline__ void push(int t) {
+        if (n < kNbrCap) {
+            b0 = __funnelshift_r(b0, b1, 16);
+            b1 = __funnelshift_r(b1, b2, 16);
+            b2 = __funnelshift_r(b2, b3, 16);
+            b3 = __funnelshift_r(b3, (unsigned)t << 3, 16);
+            if ((n & 7) == 7) col[(n >> 3) * nf] = make_uint4(b0, b1, b2, b3);
+        }
+        ++n;
+    }
+    // stores the last, partial chunk; false when the list is over kNbrCap
+    __device__ __forceinline__ bool finish() {
+        if (n > kNbrCap) return false;
+        if (n & 7) {  // move the partial chunk's entries to the low end
+            for (int e = n & 7; e < 8; ++e) {
+                b0 = __funnelshift_r(b0, b1, 16);
+                b1 = __funnelshift_r(b1, b2, 16);
+                b2 = __funnelshift_r(b2, b3, 16);
+                b3 = b3 >> 16;
+            }
+            col[(n >> 3) * nf] = make_uint4(b0, b1, b2, b3);
+        }
+        return true;
+    }
+};
+
+// findFluidPair for particle i (fluid.cu:193-254), in frame fr.  kRecord
+// (tile source only): when vs is set, also writes the particle's list for
+// the shifting passes through lw - every fluid and virtual candidate within
+// the list radius, in the walk's order, the fluid ones by tile slot, the
+// virtual ones by their slot in the tile's staged virtual strips vs.
+template <class F, bool kRecord = false, class Src>
 __device__ __forceinline__ void pair_particle(const sphnj_params &p, const DevState &d, const Src &src, int i,
-                                              Frame fr) {
+                                              Frame fr, ListWriter *lw = nullptr, const TileStrips *vs = nullptr) {
     const int nf = p.fluid_number_total;
     const int nx = p.cell_number[0], ny = p.cell_number[1];
-    const float R2 = p.impact_distance_square, hinv2 = p.smoothing_length_inverse_square;
+    const float R2 = p.impact_distance_square;
+    [[maybe_unused]] const float Rs2 = list_radius2(p);
     const bool viscid = p.is_fluid_viscid != 0;
     const PairI si = load_pair_i(p, d, i, F::f_home(p, d, fr, i));
     const float2 x_i = si.x, u_i = si.u;
@@ -385,6 +456,8 @@ __device__ __forceinline__ void pair_particle(const sphnj_params &p, const DevSt
         for (int t = rf.x; t < rf.x + rf.y; ++t) {
             const int k = src.key(t);
             const float2 dx = sub2(src.x(k, sh), x_i);
+            if constexpr (kRecord)
+                if (vs && sqn(dx) < Rs2) lw->push(k);  // a tile source's key is the slot
             if (sqn(dx) < R2) fluid_term<F>(p, src, k, si, dx, a);
         }
         const int2 rs = __ldg(&d.rng_s[m]);
@@ -403,6 +476,8 @@ __device__ __forceinline__ void pair_particle(const sphnj_params &p, const DevSt
         for (int t = rv.x; t < rv.x + rv.y; ++t) {
             const int j = __ldg(&d.lst_v[t]);
             const float2 dx = sub2(F::v_nbr(d, j, sh), x_i);
+            if constexpr (kRecord)
+                if (vs && sqn(dx) < Rs2) lw->push(vs->voff[n / 3] + t - vs->vbase[n / 3]);
             if (!(sqn(dx) < R2)) continue;
             const float kc = F::gw(p, sqn(dx));
             const float rho_j = by_phase(p.reference_density, __ldg(&d.v_phase[j]));
@@ -428,7 +503,7 @@ template <class F, class Src>
 __device__ __forceinline__ float2 shift_particle(const sphnj_params &p, const DevState &d, const Src &src, float2 x_i,
                                                  int c, Frame fr) {
     const int nx = p.cell_number[0], ny = p.cell_number[1];
-    const float R2 = p.impact_distance_square, hinv2 = p.smoothing_length_inverse_square;
+    const float R2 = p.impact_distance_square;
     float2 g = make_float2(0.f, 0.f);
     for (int n = 0; n < 9; ++n) {
         const int m = neighbour_cell(c, n, nx, ny);
@@ -476,17 +551,25 @@ __device__ __forceinline__ float2 shift_particle(const sphnj_params &p, const De
 // those entries - in the same order, with the exact cutoff test - while the
 // positions have moved by less than half the skin.  The tile staging is the
 // same in every pass of a step (same lists, same tile height), so the slots
-// stay valid.
+// stay valid.  A particle next to a wall (virtual entries in its stencil,
+// no solid ones) gets a list for the shifting passes too, cell by cell -
+// the fluid entries of a cell, then its virtual entries, as the stencil
+// walk visits them - with virtual slots in the staging of its tile.
 struct Strips {
     int base[3], len[3];
 };
 
-__device__ __forceinline__ Strips strips_of(const sphnj_params &p, const DevState &d, int c, bool &only_fluid) {
+// What a particle's stencil holds (strips_of): only fluid entries; fluid
+// and virtual entries; or something that takes the stencil walk (solid
+// entries, or a column strip of more than 64 fluid entries).
+enum StencilKind { kStencilFluid = 0, kStencilVirt = 1, kStencilWalk = 2 };
+
+__device__ __forceinline__ Strips strips_of(const sphnj_params &p, const DevState &d, int c, int &kind) {
     const int nx = p.cell_number[0], ny = p.cell_number[1];
     const int ci = c / ny, cj = c - ci * ny;
     const int r0 = max(cj - 1, 0), r1 = min(cj + 1, ny - 1);
     Strips S;
-    only_fluid = true;
+    bool walk = false, virt = false;
 #pragma unroll
     for (int s = 0; s < 3; ++s) {
         const int col = ci + s - 1;
@@ -496,70 +579,57 @@ __device__ __forceinline__ Strips strips_of(const sphnj_params &p, const DevStat
         const int2 a = __ldg(&d.rng_f[col * ny + r0]), b = __ldg(&d.rng_f[col * ny + r1]);
         S.base[s] = a.x;
         S.len[s] = b.x + b.y - a.x;
-        if (S.len[s] > 64) only_fluid = false;
+        if (S.len[s] > 64) walk = true;
         for (int r = r0; r <= r1; ++r) {
             const int m = col * ny + r;
-            if (__ldg(&d.rng_s[m]).y | __ldg(&d.rng_v[m]).y) only_fluid = false;
+            if (__ldg(&d.rng_s[m]).y) walk = true;
+            if (__ldg(&d.rng_v[m]).y) virt = true;
         }
     }
+    kind = walk ? kStencilWalk : virt ? kStencilVirt : kStencilFluid;
     return S;
 }
 
-__device__ __forceinline__ float list_radius2(const sphnj_params &p) {
-    return p.impact_distance_square * ((1.0f + kSkin) * (1.0f + kSkin));
-}
-
 // Pair pass for particle i at CSR position h; records its neighbour list
-// when `listable` (its tile was staged, so the source is the tile).
+// when `listable` (its tile was staged, so the source is the tile).  vs:
+// the tile's virtual strips when the shifting passes stage them (else null).
 template <class F, class Src>
 __device__ __forceinline__ void pair_particle_listed(const sphnj_params &p, const DevState &d, const Src &src, int i,
-                                                     int h, bool listable, Frame fr) {
-    bool ok = false;
+                                                     int h, bool listable, Frame fr, const TileStrips *vs) {
+    int kind = kStencilWalk;
     Strips S;
-    if (listable) S = strips_of(p, d, d.f_cell[i], ok);
-    if (!ok) {
-        d.f_nbr_cnt[h] = kNbrNone;
-        pair_particle<F>(p, d, src, i, fr);
+    if (listable) S = strips_of(p, d, d.f_cell[i], kind);
+    if (kind != kStencilFluid) {
+        // the pair terms by the stencil walk, which next to a wall also
+        // records the list of the shifting passes
+        if constexpr (std::is_same<Src, SrcTile>::value) {
+            const TileStrips *rec = kind == kStencilVirt ? vs : nullptr;
+            ListWriter lw(d.f_nbr + h, (size_t)p.fluid_number_total);
+            pair_particle<F, true>(p, d, src, i, fr, &lw, rec);
+            d.f_nbr_cnt[h] = rec && lw.finish() ? (uint8_t)lw.n : kNbrNone;
+        } else {
+            d.f_nbr_cnt[h] = kNbrNone;
+            pair_particle<F>(p, d, src, i, fr);
+        }
         return;
     }
     const float R2 = p.impact_distance_square, Rs2 = list_radius2(p);
     const PairI si = load_pair_i(p, d, i, F::f_home(p, d, fr, i));
     const size_t nf = (size_t)p.fluid_number_total;
     uint4 *col = d.f_nbr + h;  // chunk c at col[c nf]
-    // 8-slot FIFO in four registers: each push shifts the 128-bit value down
-    // by 16 bits and inserts at the top, so after 8 pushes the first slot is
-    // in the low half of b0; full chunks go out as one 16-byte store.
-    unsigned b0 = 0u, b1 = 0u, b2 = 0u, b3 = 0u;
-    int n = 0;
+    ListWriter lw(col, nf);
 #pragma unroll
     for (int s = 0; s < 3; ++s) {
         const int2 rr = src.range(s, make_int2(S.base[s], S.len[s]));
         for (int t = rr.x; t < rr.x + rr.y; ++t)
-            if (sqn(sep<F>(src.x(src.key(t)), si.x)) < Rs2) {
-                if (n < kNbrCap) {
-                    b0 = __funnelshift_r(b0, b1, 16);
-                    b1 = __funnelshift_r(b1, b2, 16);
-                    b2 = __funnelshift_r(b2, b3, 16);
-                    b3 = __funnelshift_r(b3, (unsigned)t << 3, 16);  // byte offset 8 t (t < 8192)
-                    if ((n & 7) == 7) col[(n >> 3) * nf] = make_uint4(b0, b1, b2, b3);
-                }
-                ++n;
-            }
+            if (sqn(sep<F>(src.x(src.key(t)), si.x)) < Rs2) lw.push(t);
     }
-    if (n > kNbrCap) {
+    if (!lw.finish()) {
         d.f_nbr_cnt[h] = kNbrNone;
         pair_particle<F>(p, d, src, i, fr);
         return;
     }
-    if (n & 7) {  // last, partial chunk: move its slots to the low end
-        for (int e = n & 7; e < 8; ++e) {
-            b0 = __funnelshift_r(b0, b1, 16);
-            b1 = __funnelshift_r(b1, b2, 16);
-            b2 = __funnelshift_r(b2, b3, 16);
-            b3 = b3 >> 16;
-        }
-        col[(n >> 3) * nf] = make_uint4(b0, b1, b2, b3);
-    }
+    const int n = lw.n;
     d.f_nbr_cnt[h] = (uint8_t)n;
     FAcc a;
     zero(a);
@@ -804,17 +874,8 @@ __device__ __forceinline__ unsigned int shift_update_particle(const sphnj_params
 }
 
 // ---- tiles ---------------------------------------------------------------
-// Block b owns home cells (ci, cj0 .. cj1-1) of one column.  Its fluid
-// neighbours are the cells (ci-1..ci+1, cj0-1..cj1): per column one
-// contiguous CSR range ("strip").  Returns false (uniformly) when the block
-// has no home particle.
-struct TileGeom {
-    int home_b, home_e, total;
-    int col, row0;  // the tile's column and first row (its frame origin in the mixed form)
-};
-
 __device__ __forceinline__ bool tile_setup(const sphnj_params &p, const DevState &d, int blk, int tile_h,
-                                           int *s_base, int *s_off, TileGeom &g) {
+                                           TileStrips &ts, TileGeom &g) {
     const int nx = p.cell_number[0], ny = p.cell_number[1];
     const int tiles_y = (ny + tile_h - 1) / tile_h;
     const int ci = blk / tiles_y, cj0 = (blk - ci * tiles_y) * tile_h;
@@ -825,26 +886,35 @@ __device__ __forceinline__ bool tile_setup(const sphnj_params &p, const DevState
     g.home_b = h0.x;
     g.home_e = h1.x + h1.y;
     if (g.home_e <= g.home_b) return false;
-    __shared__ int s_len[3];
+    __shared__ int s_len[6];
     if (threadIdx.x < 3) {
         const int col = ci + (int)threadIdx.x - 1;
-        int base = 0, len = 0;
+        int base = 0, len = 0, vbase = 0, vlen = 0;
         if (col >= 0 && col < nx) {
             const int r0 = max(cj0 - 1, 0), r1 = min(cj1, ny - 1);
             const int2 a = __ldg(&d.rng_f[col * ny + r0]), b = __ldg(&d.rng_f[col * ny + r1]);
+            const int2 va = __ldg(&d.rng_v[col * ny + r0]), vb = __ldg(&d.rng_v[col * ny + r1]);
             base = a.x;
             len = b.x + b.y - a.x;
+            vbase = va.x;
+            vlen = vb.x + vb.y - va.x;
         }
-        s_base[threadIdx.x] = base;
+        ts.base[threadIdx.x] = base;
+        ts.vbase[threadIdx.x] = vbase;
         s_len[threadIdx.x] = len;
+        s_len[3 + threadIdx.x] = vlen;
     }
     __syncthreads();
-    if (threadIdx.x == 0) {
-        s_off[0] = 0;
-        s_off[1] = s_len[0];
-        s_off[2] = s_len[0] + s_len[1];
-    }
     g.total = s_len[0] + s_len[1] + s_len[2];
+    g.total_v = s_len[3] + s_len[4] + s_len[5];
+    if (threadIdx.x == 0) {
+        ts.off[0] = 0;
+        ts.off[1] = s_len[0];
+        ts.off[2] = s_len[0] + s_len[1];
+        ts.voff[0] = g.total;
+        ts.voff[1] = g.total + s_len[3];
+        ts.voff[2] = g.total + s_len[3] + s_len[4];
+    }
     __syncthreads();
     return true;
 }
@@ -879,6 +949,23 @@ __device__ __forceinline__ float2 tile_pos_l(const sphnj_params &p, const DevSta
     }
 }
 
+// The same for the virtual entry at CSR position t of column strip s: its
+// position as the stencil walk of a home particle of the tile forms it
+// (F::v_nbr with the frame shift of its cell, which is v_cell[j]: the
+// virtual particles keep the cells they were listed by).
+template <class F>
+__device__ __forceinline__ float2 tile_vpos(const sphnj_params &p, const DevState &d, const TileGeom &g, int s,
+                                            int t) {
+    const int j = __ldg(&d.lst_v[t]);
+    if constexpr (F::kMixed) {
+        const int col = g.col + s - 1;
+        const int row = __ldg(&d.v_cell[j]) - col * p.cell_number[1];
+        return F::v_nbr(d, j, cells_to_len(p, s - 1, row - g.row0));
+    } else {
+        return F::v_nbr(d, j, make_float2(0.f, 0.f));
+    }
+}
+
 // Frame of home particle i in tile g (mixed form: the tile's origin cell).
 template <class F>
 __device__ __forceinline__ Frame tile_frame(const sphnj_params &p, const DevState &d, const TileGeom &g, int i) {
@@ -897,12 +984,12 @@ __device__ __forceinline__ Frame tile_frame_c(const sphnj_params &p, const TileG
 // sweeps tile b, returning at once if it is empty.
 template <class G, class F, bool kList, int kThreads, int kMinBlocks>
 __global__ void __launch_bounds__(kThreads, kMinBlocks)
-    k_fluid_pair_tiled(const __grid_constant__ G gs, int cap) {
+    k_fluid_pair_tiled(const __grid_constant__ G gs, int cap, int shift_cap) {
     int n_active = 0;
     SPHNJ_SCENE_SWEEP(gs, kList, n_active);
     const int tile_h = S.tile_h, use_lists = S.lists;
     extern __shared__ __align__(16) unsigned char smem[];
-    __shared__ int s_base[3], s_off[3];
+    __shared__ TileStrips ts;
     float2 *s_pos = reinterpret_cast<float2 *>(smem);
     float2 *s_vel = s_pos + cap;
     float2 *s_rp = s_vel + cap;
@@ -910,12 +997,12 @@ __global__ void __launch_bounds__(kThreads, kMinBlocks)
     uint8_t *s_fl = reinterpret_cast<uint8_t *>(s_idx + cap);
     auto sweep = [&](int tile) {
         TileGeom g;
-        if (!tile_setup(p, d, tile, tile_h, s_base, s_off, g)) return;
+        if (!tile_setup(p, d, tile, tile_h, ts, g)) return;
         const bool staged = g.total <= cap;
         if (staged) {
             for (int k = threadIdx.x; k < g.total; k += blockDim.x) {
-                const int s = tile_strip(s_off, k);
-                const int j = __ldg(&d.lst_f[s_base[s] + k - s_off[s]]);
+                const int s = tile_strip(ts.off, k);
+                const int j = __ldg(&d.lst_f[ts.base[s] + k - ts.off[s]]);
                 s_pos[k] = tile_pos<F>(p, d, g, s, j);
                 s_vel[k] = __ldg(&d.f_vel[j]);
                 s_rp[k] = make_float2(__ldg(&d.f_rho[j]), __ldg(&d.f_p[j]));
@@ -925,15 +1012,18 @@ __global__ void __launch_bounds__(kThreads, kMinBlocks)
         }
         __syncthreads();
         if (staged) {
-            const SrcTile src{s_pos, s_vel, s_rp, s_fl, s_idx, s_base, s_off};
+            const SrcTile src{s_pos, s_vel, s_rp, s_fl, s_idx, ts.base, ts.off};
+            // the shifting passes stage this tile's virtual strips too: its
+            // particles next to a wall get lists with virtual slots
+            const TileStrips *vs = virt_staged(g, shift_cap) ? &ts : nullptr;
             for (int h = g.home_b + threadIdx.x; h < g.home_e; h += blockDim.x) {
                 const int i = d.lst_f[h];
-                pair_particle_listed<F>(p, d, src, i, h, use_lists != 0, tile_frame<F>(p, d, g, i));
+                pair_particle_listed<F>(p, d, src, i, h, use_lists != 0, tile_frame<F>(p, d, g, i), vs);
             }
         } else {
             const SrcGlobal<F> src{&d};
             for (int h = g.home_b + threadIdx.x; h < g.home_e; h += blockDim.x)
-                pair_particle_listed<F>(p, d, src, d.lst_f[h], h, false, Frame{0, 0});
+                pair_particle_listed<F>(p, d, src, d.lst_f[h], h, false, Frame{0, 0}, nullptr);
         }
     };
     if constexpr (kList) {
@@ -962,7 +1052,7 @@ __global__ void __launch_bounds__(kThreads, 2048 / kThreads)
     const int tile_h = S.tile_h;
     const bool last = pass + 1 >= p.shift_per_step;
     extern __shared__ __align__(16) unsigned char smem[];
-    __shared__ int s_base[3], s_off[3];
+    __shared__ TileStrips ts;
     float2 *s_pos = reinterpret_cast<float2 *>(smem);
     // A block of a list launch, which sweeps several tiles, sums on its first
     // tile with work, after that tile's setup has issued its loads; a block
@@ -974,21 +1064,29 @@ __global__ void __launch_bounds__(kThreads, 2048 / kThreads)
     unsigned int moved2 = 0u;
     auto sweep = [&](int tile) {
         TileGeom g;
-        if (!tile_setup(p, d, tile, tile_h, s_base, s_off, g)) return;
+        if (!tile_setup(p, d, tile, tile_h, ts, g)) return;
         // every thread of the block is here (tile_setup returns uniformly)
         if constexpr (kList)
             if (first_ok < 0) first_ok = lists_valid(p, moved_share, pass) ? 1 : 0;
         const bool use_list = kList ? first_ok != 0 : entry_ok;
         const bool staged = g.total <= cap;
         if (staged) {
-            for (int k = threadIdx.x; k < g.total; k += blockDim.x) {
-                const int s = tile_strip(s_off, k);
-                s_pos[k] = tile_pos_l<F>(p, d, g, s, s_base[s] + k - s_off[s]);
+            // the fluid strips, then (when they fit) the virtual strips, which
+            // the lists of the tile's particles next to a wall refer to
+            const int n_staged = virt_staged(g, cap) ? g.total + g.total_v : g.total;
+            for (int k = threadIdx.x; k < n_staged; k += blockDim.x) {
+                if (k < g.total) {
+                    const int s = tile_strip(ts.off, k);
+                    s_pos[k] = tile_pos_l<F>(p, d, g, s, ts.base[s] + k - ts.off[s]);
+                } else {
+                    const int s = tile_strip(ts.voff, k);
+                    s_pos[k] = tile_vpos<F>(p, d, g, s, ts.vbase[s] + k - ts.voff[s]);
+                }
             }
         }
         __syncthreads();
         if (staged) {
-            const SrcTile src{s_pos, nullptr, nullptr, nullptr, nullptr, s_base, s_off};
+            const SrcTile src{s_pos, nullptr, nullptr, nullptr, nullptr, ts.base, ts.off};
             for (int h = g.home_b + threadIdx.x; h < g.home_e; h += blockDim.x) {
                 const int c = d.f_celll[h];
                 const Frame fr = tile_frame_c<F>(p, g, c);
@@ -1249,7 +1347,7 @@ namespace {
 // block per tile the fluid can fill (twice that at 128 threads), a dense
 // scene one block per tile.  Each scene sweeps tiles of its own height.
 template <class F, class G, bool kList, class Sh>
-int pair_tiled(cudaStream_t st, G &g, int cap, size_t smem) {
+int pair_tiled(cudaStream_t st, G &g, int cap, int shift_cap, size_t smem) {
     using D = typename G::Dev;
     const long long key = site_key(SITE_PAIR_TILED, Sh::threads);
     if constexpr (kList)
@@ -1259,18 +1357,19 @@ int pair_tiled(cudaStream_t st, G &g, int cap, size_t smem) {
                 return std::min<unsigned>(tile_blocks(s.p, s.tile_h),
                                           sweep_blocks(s.p, s.tile_h) * (kTileBlock / Sh::threads));
             },
-            k_fluid_pair_tiled<D, F, true, Sh::threads, Sh::min_blocks>, Sh::threads, smem, st, cap);
+            k_fluid_pair_tiled<D, F, true, Sh::threads, Sh::min_blocks>, Sh::threads, smem, st, cap, shift_cap);
     else
         return launch(
             g, key, [](const Scene &s) { return tile_blocks(s.p, s.tile_h); },
-            k_fluid_pair_tiled<D, F, false, Sh::threads, Sh::min_blocks>, Sh::threads, smem, st, cap);
+            k_fluid_pair_tiled<D, F, false, Sh::threads, Sh::min_blocks>, Sh::threads, smem, st, cap, shift_cap);
 }
 
-template <class F, class G, bool kList> int pair_tiled_shape(cudaStream_t st, G &g, const TileConfig &tc, int cap) {
+template <class F, class G, bool kList>
+int pair_tiled_shape(cudaStream_t st, G &g, const TileConfig &tc, int cap, int shift_cap) {
     const size_t smem = cap * kPairSmemPerEntry;
-    if (tc.pair_block == 128) return pair_tiled<F, G, kList, PairBlock<F, kList, 128>>(st, g, cap, smem);
-    if (tc.pair_block == 256) return pair_tiled<F, G, kList, PairBlock<F, kList, 256>>(st, g, cap, smem);
-    return pair_tiled<F, G, kList, PairShape<G, kList, F>>(st, g, cap, smem);
+    if (tc.pair_block == 128) return pair_tiled<F, G, kList, PairBlock<F, kList, 128>>(st, g, cap, shift_cap, smem);
+    if (tc.pair_block == 256) return pair_tiled<F, G, kList, PairBlock<F, kList, 256>>(st, g, cap, shift_cap, smem);
+    return pair_tiled<F, G, kList, PairShape<G, kList, F>>(st, g, cap, shift_cap, smem);
 }
 
 template <class F, class G> int fluid_pair(cudaStream_t st, G &g, const TileConfig &tc) {
@@ -1281,13 +1380,14 @@ template <class F, class G> int fluid_pair(cudaStream_t st, G &g, const TileConf
             k_fluid_pair_each<D, F>, kPairBlock, 0, st, 0);
     const bool list = use_tile_list(g);
     const int cap = tile_cap(max_tile_h(g), pair_per_cell(g, list));
+    const int shift_cap = tile_cap(max_tile_h(g));  // the shifting passes' staging (shift_pass)
     // this step's active tiles (the cell lists are final), used by the pair
     // pass and every shifting pass of the step
     int n = launch_tile_compact(st, g, std::is_same<G, GroupMany>::value);
     if (list) {
-        n += pair_tiled_shape<F, G, true>(st, g, tc, cap);
+        n += pair_tiled_shape<F, G, true>(st, g, tc, cap, shift_cap);
     } else if constexpr (!std::is_same<G, GroupMany>::value) {  // batches always sweep their lists
-        n += pair_tiled_shape<F, G, false>(st, g, tc, cap);
+        n += pair_tiled_shape<F, G, false>(st, g, tc, cap, shift_cap);
     }
     n += launch(
         g, site_key(SITE_PAIR_FALLBACK), [](const Scene &s) { return fallback_blocks(s.p.fluid_number_total); },
@@ -1335,7 +1435,7 @@ template <class F, class G> int shift_pass(cudaStream_t st, G &g, const TileConf
                    g, site_key(SITE_SHIFT_FALLBACK, pass),
                    [&](const Scene &s) { return active(s) ? fallback_blocks(s.p.fluid_number_total) : 0u; },
                    k_shift_gradient_each<D, F>, kPairBlock, 0, st, 1, pass);
-    const int cap = tile_cap(max_tile_h(g));
+    const int cap = tile_cap(max_tile_h(g));  // also the pair pass's shift_cap (fluid_pair)
     const size_t smem = cap * sizeof(float2);
     // batched list launches: blocks of kListBlock threads, kTileBlock / kListBlock
     // times as many (a sparse scene swept alone, one short launch, keeps the
