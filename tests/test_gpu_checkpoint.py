@@ -77,12 +77,17 @@ def test_checkpoint_of_another_layout_is_refused():
         assert e.value.code == abi.ERR_IO
 
 
+@pytest.mark.parametrize("form", [abi.FORM_PLAIN, abi.FORM_MIXED])
 @pytest.mark.parametrize("name", list(CASES))
-def test_stencil_walk_equals_stored_lists(name):
+def test_stencil_walk_equals_stored_lists(name, form):
+    """The stored lists visit the stencil walk's terms in its order, in both
+    forms - also for the particles next to a wall, whose lists hold virtual
+    slots (a quarter of the small gas tank's particles); the gate's particles
+    next to the solid keep the walk."""
     p, arr = load(CASES[name]())
     out = []
     for lists in (True, False):
-        with S.Simulation(p) as g:
+        with S.Simulation(p, form) as g:
             g.set_neighbour_lists(lists)
             assert g.sweeps()["lists"] == lists
             g.upload(arr)
