@@ -77,13 +77,14 @@ struct DevState {
     int *stamp;
     // neighbour lists of this step, indexed by the particle's position h in
     // the fluid CSR list: the tile slots t (as uint16 byte offsets 8 t into
-    // the tile's staged positions) of the fluid entries that
+    // the tile's staged positions) of the fluid entries - and, next to a
+    // wall, of the virtual entries, staged after the fluid ones - that
     // were within the cutoff plus skin when the pair pass ran, in the
     // reference's order, up to 128 bytes per particle moved in 16-byte chunks
     // of 8 slots, chunk c of particle h at f_nbr[c nf + h] (a warp's
     // consecutive particles read one contiguous run per chunk), and their count
-    // (kNbrNone: no list - the stencil holds solid or virtual entries, the
-    // tile was not staged, or the list would exceed kNbrCap)
+    // (kNbrNone: no list - the stencil holds solid entries, the tile's
+    // strips were not staged, or the list would exceed kNbrCap)
     uint4 *f_nbr;
     uint8_t *f_nbr_cnt;
     // max |displacement|^2 (float bits) of each position update since the
