@@ -460,7 +460,8 @@ def run_ours(args):
                 "frac": achieved / peak,
                 "traffic": byte_model.measured_traffic_per_launch(dom, nf, mixed) if args.tile_h == 16 and not args.untiled
                 else None,
-                "traffic_source": "ncu dram bytes of one launch at 2.08M particles, scaled by particle count",
+                "traffic_source": "ncu dram bytes of one launch at 2.08M particles, scaled by particle count "
+                                  "(captured before the particles next to a wall got neighbour lists)",
                 "peak_source": "MEASURED_PEAKS.json hbm_gbs (measured)" if peaks else "fallback 6.8 TB/s",
                 "bytes_per_launch": bpl, "avg_launch_ms": avg_ms,
                 # the DRAM bytes ncu measured for such a launch over the same

@@ -119,7 +119,9 @@ def bytes_per_step(nf: int, ns: int, nv: int, shifts: int, substeps: int) -> flo
 # before the step's last); it grows in proportion to the particle count (same
 # tile shape, same list length per particle).  Well above the compulsory
 # bytes above: the pair pass writes the per-step neighbour lists and every
-# shifting pass reads them back (about 96 B per particle).
+# shifting pass reads them back (about 96 B per particle).  The captures
+# predate the lists of the particles next to a wall, whose tiles' shifting
+# passes also stage their virtual strips (about 1% of that scene's tiles).
 MEASURED_TRAFFIC_PER_PARTICLE = {
     "fluid_pair": 148.9,
     "shift_pass": 154.1,
