@@ -121,7 +121,7 @@ def bytes_per_step(nf: int, ns: int, nv: int, shifts: int, substeps: int) -> flo
 # bytes above: the pair pass writes the per-step neighbour lists and every
 # shifting pass reads them back (about 96 B per particle).  The captures
 # predate the lists of the particles next to a wall, whose tiles' shifting
-# passes also stage their virtual strips (about 1% of that scene's tiles).
+# passes also stage their virtual strips (7% of that scene's tiles).
 MEASURED_TRAFFIC_PER_PARTICLE = {
     "fluid_pair": 148.9,
     "shift_pass": 154.1,
